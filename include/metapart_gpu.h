@@ -1,0 +1,131 @@
+/*
+ * metapart_gpu.h -- C ABI of the GB300 read-partitioning path (libmetapart_gpu.so).
+ *
+ * The reference (MetaPart) exposes this path as three stage programs that talk
+ * through files, plus a link-time k-mer module.  Each entry point below names
+ * the reference interface it replaces.  Plain pointers and sizes only; host
+ * buffers are caller-owned, device memory is owned by the job.  Every call
+ * returns 0 or a negative MP_E* code (never aborts); mp_last_error() gives the
+ * message of the calling thread's last failure.
+ *
+ * Limits (the reference's own, made explicit): k in [11, 31]; m is 10
+ * (4^10 buckets); read ids below 2^32 - 1; an even read count for the mate
+ * union; metapart reads shorter than 300 + k; the 3-minimizer variant with
+ * numScans == 1; single-end or interleaved input (no two-file paired end).
+ */
+#ifndef METAPART_GPU_H
+#define METAPART_GPU_H
+#include <stddef.h>
+#include <stdint.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MP_OK 0
+#define MP_EARG (-1)      /* invalid argument */
+#define MP_EIO (-2)       /* file read/write failed */
+#define MP_EFMT (-3)      /* malformed FASTQ / index / histogram */
+#define MP_ENOMEM (-4)    /* host or device allocation failed, or HBM budget exceeded */
+#define MP_EUNSUP (-5)    /* configuration outside the supported limits */
+#define MP_ECUDA (-6)     /* CUDA runtime error */
+#define MP_EDEVICE (-7)   /* a kernel's bounded wait or capacity check failed */
+
+#define MP_NUM_BUCKETS 1048576u   /* 4^10 */
+#define MP_INDEX_RECORD_BYTES 4194344u
+#define MP_NUM_OUT_PARTITIONS 16
+
+typedef struct mp_ctx mp_ctx;
+typedef struct mp_job mp_job;
+
+/* Thread-local message of the last failed call. */
+const char *mp_last_error(void);
+
+/* One context per device: stream pool, HBM budget accounting. */
+int mp_ctx_create(int device, uint64_t hbm_budget_bytes, mp_ctx **out);
+void mp_ctx_destroy(mp_ctx *ctx);
+uint64_t mp_ctx_hbm_in_use(const mp_ctx *ctx);
+
+/* Chunk index of FASTQ files in memory.
+ * Replaces genFastqIdx main (genFastqIdx.c:142-376) and getFileIndex (:28-53).
+ * files[i]/sizes[i]: file contents; out_offsets receives (fileNo, offset) pairs of
+ * up to num_chunks+1 index records (last = end sentinel); *out_count their number. */
+int mp_fastq_index(int num_chunks, int n_pe, int n_se, int n_il, int nfiles, const char *const *files,
+                   const uint64_t *sizes, int32_t *out_file_no, uint64_t *out_offsets, int *out_count);
+
+/* A partition job: reads resident in HBM plus all stage state, on its own stream. */
+int mp_job_create(mp_ctx *ctx, mp_job **out);
+void mp_job_destroy(mp_job *job);
+
+/* Upload and parse FASTQ on the GPU (records of header, sequence, '+', quality).
+ * Replaces the per-chunk FASTQ walks getNextRead (genHistograms.c:60-80, metapart.c:296-369),
+ * loadChunk (metapart.c:371-500) and getNextFullRead (metapart.c:211-294).
+ * bytes: the files concatenated; file_sizes: each file's length (each ends on a record end). */
+int mp_job_load_fastq(mp_job *job, const char *bytes, uint64_t nbytes, const uint64_t *file_sizes, int nfiles,
+                      int interleaved);
+/* Same, for bytes already in device memory (copied into the job). */
+int mp_job_load_fastq_device(mp_job *job, const void *dev_bytes, uint64_t nbytes, const uint64_t *file_sizes,
+                             int nfiles, int interleaved);
+uint64_t mp_job_num_reads(const mp_job *job);
+
+/* Releases the job's reads and stage state (device memory) and keeps its stream, so one job can
+ * run many inputs back to back.  No reference counterpart (the reference runs one input per process). */
+int mp_job_reset(mp_job *job);
+
+/* The job's CUDA stream (cudaStream_t), for callers that order their own work or events around it. */
+void *mp_job_stream(mp_job *job);
+
+/* Number of kernels this library has launched in the process (instrumentation). */
+uint64_t mp_launch_count(void);
+
+/* m-mer histogram and per-chunk bucket counts of the loaded reads.
+ * Replaces genHistograms main (genHistograms.c:82-575) with the count module
+ * getCanonKmers/getMmerPrefix (countMmers.c:60-217; countMmers_3minimizers.c:83-271).
+ * chunk_starts: nchunks+1 absolute byte offsets (record starts; last = end of input).
+ * hist_out: 1048577 exclusive prefix sums (the .kmerHist layout, genHistograms.c:325-342);
+ * chunk_counts_out (nullable): nchunks x 1048576 bucket counts (fileIndex.kmerFreqCount);
+ * chunk_reads_out (nullable): reads per chunk. */
+int mp_job_count(mp_job *job, int k, int min3, const uint64_t *chunk_starts, int nchunks, uint64_t *hist_out,
+                 uint32_t *chunk_counts_out, uint64_t *chunk_reads_out);
+
+typedef struct {
+    int k;            /* kmerSize */
+    int min3;         /* 1: 3-minimizer variant (enumerateKmers_3minimizers.c) */
+    int num_scans;    /* numScans: semantic passes over the m-mer space */
+    int num_threads;  /* numThreads: chunk-to-thread map, k-mer thread ranges, output file split */
+} mp_part_params;
+
+/* Read partitioning: enumerate -> stable sort -> mischief filter -> union-find per scan,
+ * then mate union and the 16 work partitions.
+ * Replaces metapart main (metapart.c:3544-4100): generateKmersInScan (:1192), sortKmerList (:1852),
+ * markMischiefKmers (:2270), unionFindPar2 (:2520), unionFind (:2736), printStats (:3227),
+ * unionFindPeReads (:2801), the work-partition planner (:4016-4053), and the enum module
+ * getCanonKmers (enumerateKmers.c:127; enumerateKmers_3minimizers.c:129).
+ * chunk_first_read: nchunks+1 read ids (fileIndex readId/readIdExtra; last = read count).
+ * hist: the 1048577-entry .kmerHist of the same k and variant.  bounds_out: 17 read-id bounds. */
+int mp_job_partition(mp_job *job, const mp_part_params *p, const uint64_t *chunk_starts,
+                     const uint64_t *chunk_first_read, int nchunks, const uint64_t *hist, uint64_t *bounds_out);
+
+/* Final component label (root read id) of every read after mp_job_partition (the reference's
+ * compressed parent array, metapart.c:4026-4030).  out: mp_job_num_reads() entries. */
+int mp_job_labels(mp_job *job, uint32_t *out);
+
+/* Partition FASTQ output, grouped by file j = partition * num_threads + tid in the order of the
+ * reference's FromTid<tid>_ToRank<partition>.paired.fastq files.
+ * Replaces writeOutput3 (metapart.c:956-1066).  With out == NULL only file_sizes/total are filled. */
+int mp_job_output(mp_job *job, char *out, uint64_t capacity, uint64_t *file_sizes, uint64_t *total);
+
+/* Optional stage dumps in the reference's formats (the files oracle/ref_hooks.c writes),
+ * for parity testing.  NULL disables. */
+int mp_job_set_dump_dir(mp_job *job, const char *dir);
+
+/* Device time of the last count/partition/output calls per stage, in ms:
+ * [0] parse [1] count [2] enumerate [3] sort [4] filter [5] union-find [6] mate union+partition [7] output. */
+int mp_job_stage_ms(const mp_job *job, double *ms, int n);
+
+/* Algorithmic bytes and device time of the last sort's digit passes (roofline reporting). */
+int mp_job_sort_stats(const mp_job *job, uint64_t *tuples, int *passes, double *pass_ms, uint64_t *bytes);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

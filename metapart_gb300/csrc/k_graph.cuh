@@ -1,0 +1,29 @@
+#pragma once
+#include <vector>
+
+#include "k_reads.cuh"
+
+namespace mp {
+
+// Sorted tuples of one scan (views into the sort buffers) plus the run-head bitmask.
+struct Tuples {
+    uint64_t *lo = nullptr;   // kmer << 8 | adj
+    uint8_t *hi = nullptr;    // kmer >> 56 (nullable)
+    uint32_t *id = nullptr;   // read id / component label
+    uint64_t n = 0;
+    uint32_t *heads = nullptr;
+};
+
+// K4: markMischiefKmers over the scan; range_bounds = T + 1 tuple bounds of the thread ranges.
+int filter_scan(Tuples &tp, const std::vector<uint64_t> &range_bounds, uint32_t *parent, uint8_t *filtered,
+                DeviceArena &arena, cudaStream_t st);
+// K5: unionFindPar2 + unionFind + printStats compression for the scan.
+int union_scan(Tuples &tp, const std::vector<uint64_t> &range_bounds, uint32_t *parent, uint64_t n_reads,
+               DeviceArena &arena, cudaStream_t st);
+// K6: sizes, unionFindPeReads(1000), final compression and the 17 partition bounds (host).
+int mate_union_and_plan(uint32_t *parent, uint64_t n_reads, uint32_t *size, uint64_t *bounds_out, DeviceArena &arena,
+                        cudaStream_t st, int *rounds_out);
+int plan_partitions(const uint32_t *parent, const uint32_t *size, uint64_t n_reads, uint64_t *bounds_host,
+                    DeviceArena &arena, cudaStream_t st);
+
+}  // namespace mp

@@ -1,0 +1,353 @@
+// K1 (m-mer histogram) and K2 (tuple enumeration) kernels.
+//
+// Plain variant: one warp per read.  Each round of 32 bases is loaded with one
+// coalesced byte load per lane and turned into bit-planes with __ballot_sync: the
+// 2-bit base codes (packed most-significant-first into a 64-bit word), an N mask,
+// and the five character bits the adjacency byte uses.  Lane j of round t then
+// owns k-mer position 32t+j: its forward code is a funnel shift of two packed
+// words, its reverse complement a bit reversal (countMmers.c:83-217,
+// enumerateKmers.c:127-371 compute the same codes with a rolling update).
+//
+// 3-minimizer variant: one thread per read running the reference's window logic
+// (countMmers_3minimizers.c:83-271, enumerateKmers_3minimizers.c:129-470); it
+// emits about three k-mers per read, so the base scan dominates either way.
+#include "k_kmers.cuh"
+
+namespace mp {
+
+constexpr unsigned FULL = 0xFFFFFFFFu;
+
+struct Round {
+    uint64_t W;     // codes of positions 32t..32t+31, position 32t in bits 63..62
+    uint32_t N;     // bit j: position 32t+j is 'N'
+    uint32_t A[5];  // bit b of a5 (char bits 1..5) per position
+};
+
+template <bool ADJ>
+__device__ __forceinline__ void load_round(const uint8_t *s, uint32_t L, int t, int lane, Round &r)
+{
+    const uint32_t p = 32u * (uint32_t)t + (uint32_t)lane;
+    const uint32_t c = p < L ? (uint32_t)s[p] : 0x41u;
+    const uint32_t f = fcode(c);
+    const uint32_t P1 = __ballot_sync(FULL, f & 2), P0 = __ballot_sync(FULL, f & 1);
+    r.W = (spread32(__brev(P1)) << 1) | spread32(__brev(P0));
+    r.N = __ballot_sync(FULL, p < L && c == 'N');
+    if (ADJ) {
+        const uint32_t a = a5_of(c);
+#pragma unroll
+        for (int b = 0; b < 5; b++) r.A[b] = __ballot_sync(FULL, (a >> b) & 1);
+    }
+}
+
+__device__ __forceinline__ uint32_t a5_at(const uint32_t *A, int bit)
+{
+    uint32_t v = 0;
+#pragma unroll
+    for (int b = 0; b < 5; b++) v |= ((A[b] >> bit) & 1u) << b;
+    return v;
+}
+
+// Forward code, validity (no N in the window) of the k-mer at lane's position of round t.
+__device__ __forceinline__ bool kmer_at(int lane, int k, const Round &c, const Round &n, uint64_t &fwd)
+{
+    const uint64_t x = lane ? ((c.W << (2 * lane)) | (n.W >> (64 - 2 * lane))) : c.W;
+    fwd = x >> (64 - 2 * k);
+    const uint64_t n64 = (uint64_t)c.N | ((uint64_t)n.N << 32);
+    return ((n64 >> lane) & ((1ull << k) - 1)) == 0;
+}
+
+__device__ __forceinline__ uint32_t chunk_of(const uint64_t *chunk_rec, int nchunks, uint64_t r)
+{
+    int lo = 0, hi = nchunks - 1;  // largest c with chunk_rec[c] <= r
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (chunk_rec[mid] <= r) lo = mid; else hi = mid - 1;
+    }
+    return (uint32_t)lo;
+}
+
+// ------------------------------------------------------------ K1 plain
+
+__global__ void __launch_bounds__(256) k_count_plain(const uint8_t *fq, const uint64_t *seq_off, const uint32_t *seq_len,
+                                                     uint64_t r0, uint64_t r1, int k, const uint64_t *chunk_rec,
+                                                     int nchunks, uint32_t *cc, unsigned long long *glob, uint32_t *err)
+{
+    const int lane = threadIdx.x & 31;
+    const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    const int sh = 2 * (k - 10);
+    for (uint64_t r = r0 + (((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5); r < r1; r += nw) {
+        const uint32_t L = seq_len[r];
+        if (L <= (uint32_t)k) continue;
+        if (L > (uint32_t)MAX_READ_COUNT) {
+            if (lane == 0) atomicOr(err, DERR_LONG_READ);
+            continue;
+        }
+        const uint8_t *s = fq + seq_off[r];
+        uint32_t *ccc = cc ? cc + (size_t)chunk_of(chunk_rec, nchunks, r) * NB : nullptr;
+        const int last = (int)L - k;
+        Round cur, nxt;
+        load_round<false>(s, L, 0, lane, cur);
+        load_round<false>(s, L, 1, lane, nxt);
+        for (int t = 0; 32 * t <= last; t++) {
+            const int i = 32 * t + lane;
+            uint64_t fwd;
+            bool v = kmer_at(lane, k, cur, nxt, fwd) && i <= last;
+            const uint64_t rc = revcomp(fwd, k);
+            const uint32_t b = (uint32_t)((fwd < rc ? fwd : rc) >> sh);
+            const uint32_t act = __ballot_sync(FULL, v);
+            if (v) {
+                const uint32_t peers = __match_any_sync(act, b);
+                if (lane == __ffs(peers) - 1) {
+                    if (ccc) atomicAdd(&ccc[b], (uint32_t)__popc(peers));
+                    else atomicAdd(&glob[b], (unsigned long long)__popc(peers));
+                }
+            }
+            cur = nxt;
+            load_round<false>(s, L, t + 2, lane, nxt);
+        }
+    }
+}
+
+// ------------------------------------------------------- 3-minimizer core
+
+// One read, thread-sequential.  ENUM: apply the scan range and produce adjacency bytes.
+template <bool ENUM, class Emit>
+__device__ __forceinline__ void min3_read(const uint8_t *s, int L, int k, uint32_t lo, uint32_t hi, Emit emit)
+{
+    if (L <= k) return;
+    const int last = L - k, sh = 2 * (k - 10), win = last / 3;
+    const uint64_t mask = kmer_mask(k);
+    uint64_t fwd = 0, rc = 0, mn = 0;
+    uint32_t mps = 0, mns = 0;  // stored adjacency a5 values of the current minimum
+    int lastN = -1;
+    for (int j = 0; j < k; j++) {
+        const uint32_t c = s[j];
+        if (c == 'N') lastN = j;
+        rc |= (uint64_t)(3u - fcode(c)) << (2 * j);
+        fwd = (fwd << 2) | fcode(c);
+    }
+    if (lastN == -1) {
+        const bool f = fwd < rc;
+        const uint64_t v = f ? fwd : rc;
+        const uint32_t b = (uint32_t)(v >> sh);
+        if (!ENUM || (b >= lo && b < hi)) {
+            mn = v;
+            if (ENUM) {
+                const uint32_t pa = 7u, na = a5_of(s[k]);
+                mps = f ? pa : a5_cmpl(pa);
+                mns = f ? na : a5_cmpl(na);
+            }
+        }
+    }
+    int next_win = win;
+    for (int i = 1; i <= last; i++) {
+        const uint32_t c = s[i + k - 1];
+        rc = (rc >> 2) | ((uint64_t)(3u - fcode(c)) << (2 * (k - 1)));
+        fwd = ((fwd << 2) | fcode(c)) & mask;
+        if (c == 'N') lastN = i + k - 1;
+        if (!(i > lastN)) continue;
+        const bool f = fwd < rc;
+        const uint64_t v = f ? fwd : rc;
+        const uint32_t b = (uint32_t)(v >> sh);
+        if (ENUM && !(b >= lo && b < hi)) continue;
+        uint32_t pa = 0, na = 0;
+        if (ENUM) {
+            pa = a5_of(s[i - 1]);
+            na = (i == last) ? 7u : a5_of(s[i + k]);
+            if (!f) { pa = a5_cmpl(pa); na = a5_cmpl(na); }
+        }
+        if (i > next_win) {
+            if (mn != 0) emit(mn, f ? ((mps << 3) | (mns & 7)) : ((mns << 3) | (mps & 7)));
+            mn = v; mps = pa; mns = na;
+            next_win += win;
+            if (next_win + win > last) next_win = last;
+        } else if (v < mn || mn == 0) {
+            mn = v; mps = pa; mns = na;
+        }
+    }
+    if (mn != 0) emit(mn, (mns << 3) | (mps & 7));
+}
+
+__global__ void k_count_min3(const uint8_t *fq, const uint64_t *seq_off, const uint32_t *seq_len, uint64_t r0, uint64_t r1,
+                             int k, const uint64_t *chunk_rec, int nchunks, uint32_t *cc, unsigned long long *glob,
+                             uint32_t *err)
+{
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    const int sh = 2 * (k - 10);
+    for (uint64_t r = r0 + (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; r < r1; r += stride) {
+        const uint32_t L = seq_len[r];
+        if (L > (uint32_t)MAX_READ_COUNT) { atomicOr(err, DERR_LONG_READ); continue; }
+        uint32_t *ccc = cc ? cc + (size_t)chunk_of(chunk_rec, nchunks, r) * NB : nullptr;
+        min3_read<false>(fq + seq_off[r], (int)L, k, 0, 0, [&](uint64_t v, uint32_t) {
+            const uint32_t b = (uint32_t)(v >> sh);
+            if (ccc) atomicAdd(&ccc[b], 1u); else atomicAdd(&glob[b], 1ull);
+        });
+    }
+}
+
+// Global histogram from per-chunk counts: hist_cnt[b] = sum over chunks.
+__global__ void k_sum_chunks(const uint32_t *cc, int nchunks, unsigned long long *glob)
+{
+    const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= NB) return;
+    unsigned long long s = 0;
+    for (int c = 0; c < nchunks; c++) s += cc[(size_t)c * NB + b];
+    glob[b] = s;
+}
+
+// ------------------------------------------------------------ K2 plain
+
+template <bool WRITE>
+__global__ void __launch_bounds__(256) k_enum_plain(const uint8_t *fq, const uint64_t *seq_off, const uint32_t *seq_len,
+                                                    uint64_t n_reads, int k, uint32_t lo, uint32_t hi,
+                                                    const uint32_t *label, const uint64_t *out_off, uint32_t *cnt,
+                                                    uint64_t *o_lo, uint8_t *o_hi, uint32_t *o_id, uint32_t *err)
+{
+    const int lane = threadIdx.x & 31;
+    const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    const int sh = 2 * (k - 10);
+    for (uint64_t r = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < n_reads; r += nw) {
+        const uint32_t L = seq_len[r];
+        if (L <= (uint32_t)k) {
+            if (!WRITE && lane == 0) cnt[r] = 0;
+            continue;
+        }
+        if (L > 32u * MAX_ROUNDS_ENUM || L - (uint32_t)k >= 300u) {
+            if (lane == 0) { atomicOr(err, DERR_LONG_READ); if (!WRITE) cnt[r] = 0; }
+            continue;
+        }
+        const uint8_t *s = fq + seq_off[r];
+        const int last = (int)L - k;
+        uint64_t base = WRITE ? out_off[r] : 0;
+        uint32_t id = (uint32_t)r;
+        if (WRITE && label) {
+            const uint32_t p = label[r];
+            id = (p == BAD) ? (uint32_t)r : p;  // findRoot after full compression (metapart.c:543-568)
+        }
+        Round prv, cur, nxt;
+        load_round<WRITE>(s, L, 0, lane, cur);
+        load_round<WRITE>(s, L, 1, lane, nxt);
+        prv = cur;
+        uint32_t total = 0;
+        for (int t = 0; 32 * t <= last; t++) {
+            const int i = 32 * t + lane;
+            uint64_t fwd;
+            const bool v0 = kmer_at(lane, k, cur, nxt, fwd) && i <= last;
+            const uint64_t rc = revcomp(fwd, k);
+            const bool f = fwd < rc;
+            const uint64_t canon = f ? fwd : rc;
+            const uint32_t b = (uint32_t)(canon >> sh);
+            const bool v = v0 && b >= lo && b < hi;
+            const uint32_t bal = __ballot_sync(FULL, v);
+            if (WRITE && v) {
+                uint32_t pa = 7u, na = 7u;  // 'N' at the read ends (enumerateKmers.c:177, 252-255)
+                if (i > 0) pa = lane ? a5_at(cur.A, lane - 1) : a5_at(prv.A, 31);
+                if (i < last) {
+                    const int q = lane + k;
+                    na = q < 32 ? a5_at(cur.A, q) : a5_at(nxt.A, q - 32);
+                }
+                const uint32_t adj = f ? adj_fwd(pa, na) : adj_rc(pa, na);
+                const uint64_t pos = base + __popc(bal & ((1u << lane) - 1));
+                o_lo[pos] = (canon << 8) | adj;
+                if (o_hi) o_hi[pos] = (uint8_t)(canon >> 56);
+                o_id[pos] = id;
+            }
+            base += __popc(bal);
+            total += __popc(bal);
+            prv = cur;
+            cur = nxt;
+            load_round<WRITE>(s, L, t + 2, lane, nxt);
+        }
+        if (!WRITE && lane == 0) {
+            cnt[r] = total;
+            if (total > 255) atomicOr(err, DERR_TOO_MANY);  // the reference's per-read counter is a uint8_t
+        }
+    }
+}
+
+// ------------------------------------------------------------- K2 3-min
+
+template <bool WRITE>
+__global__ void k_enum_min3(const uint8_t *fq, const uint64_t *seq_off, const uint32_t *seq_len, uint64_t n_reads, int k,
+                            uint32_t lo, uint32_t hi, const uint32_t *label, const uint64_t *out_off, uint32_t *cnt,
+                            uint64_t *o_lo, uint8_t *o_hi, uint32_t *o_id, uint32_t *err)
+{
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n_reads; r += stride) {
+        const uint32_t L = seq_len[r];
+        if (L > (uint32_t)k && L - (uint32_t)k >= 300u) {
+            atomicOr(err, DERR_LONG_READ);
+            if (!WRITE) cnt[r] = 0;
+            continue;
+        }
+        uint32_t id = (uint32_t)r;
+        if (WRITE && label) { const uint32_t p = label[r]; id = (p == BAD) ? (uint32_t)r : p; }
+        uint64_t pos = WRITE ? out_off[r] : 0;
+        const uint64_t end = WRITE ? out_off[r + 1] : 0;
+        uint32_t c = 0;
+        min3_read<true>(fq + seq_off[r], (int)L, k, lo, hi, [&](uint64_t v, uint32_t adj) {
+            if (WRITE) {
+                if (pos < end) {
+                    o_lo[pos] = (v << 8) | adj;
+                    if (o_hi) o_hi[pos] = (uint8_t)(v >> 56);
+                    o_id[pos] = id;
+                } else {
+                    atomicOr(err, DERR_OVERFLOW);
+                }
+                pos++;
+            }
+            c++;
+        });
+        if (!WRITE) {
+            cnt[r] = c;
+            if (c > 255) atomicOr(err, DERR_TOO_MANY);
+        }
+    }
+}
+
+// ------------------------------------------------------------- host side
+
+static unsigned grid_for(uint64_t work, int per_block, int max_blocks = 152 * 16)
+{
+    uint64_t g = (work + per_block - 1) / per_block;
+    if (g < 1) g = 1;
+    if (g > (uint64_t)max_blocks) g = max_blocks;
+    return (unsigned)g;
+}
+
+void launch_count(const uint8_t *fq, const ParsedReads &pr, int k, int min3, const uint64_t *chunk_rec, int nchunks,
+                  uint32_t *cc, unsigned long long *glob, uint32_t *err, cudaStream_t st)
+{
+    if (min3)
+        (mp::count_launch(), k_count_min3<<<grid_for(pr.n_reads, 128, 152 * 32), 128, 0, st>>>(fq, pr.seq_off, pr.seq_len, 0, pr.n_reads, k,
+                                                                          chunk_rec, nchunks, cc, glob, err));
+    else
+        (mp::count_launch(), k_count_plain<<<grid_for(pr.n_reads, 8), 256, 0, st>>>(fq, pr.seq_off, pr.seq_len, 0, pr.n_reads, k, chunk_rec,
+                                                               nchunks, cc, glob, err));
+    if (cc) (mp::count_launch(), k_sum_chunks<<<NB / 256, 256, 0, st>>>(cc, nchunks, glob));
+}
+
+void launch_enum_count(const uint8_t *fq, const ParsedReads &pr, int k, int min3, uint32_t lo, uint32_t hi,
+                       uint32_t *cnt, uint32_t *err, cudaStream_t st)
+{
+    if (min3)
+        (mp::count_launch(), k_enum_min3<false><<<grid_for(pr.n_reads, 128, 152 * 32), 128, 0, st>>>(
+            fq, pr.seq_off, pr.seq_len, pr.n_reads, k, lo, hi, nullptr, nullptr, cnt, nullptr, nullptr, nullptr, err));
+    else
+        (mp::count_launch(), k_enum_plain<false><<<grid_for(pr.n_reads, 8), 256, 0, st>>>(fq, pr.seq_off, pr.seq_len, pr.n_reads, k, lo, hi,
+                                                                     nullptr, nullptr, cnt, nullptr, nullptr, nullptr, err));
+}
+
+void launch_enum_write(const uint8_t *fq, const ParsedReads &pr, int k, int min3, uint32_t lo, uint32_t hi,
+                       const uint32_t *label, const uint64_t *off, uint64_t *o_lo, uint8_t *o_hi, uint32_t *o_id,
+                       uint32_t *err, cudaStream_t st)
+{
+    if (min3)
+        (mp::count_launch(), k_enum_min3<true><<<grid_for(pr.n_reads, 128, 152 * 32), 128, 0, st>>>(
+            fq, pr.seq_off, pr.seq_len, pr.n_reads, k, lo, hi, label, off, nullptr, o_lo, o_hi, o_id, err));
+    else
+        (mp::count_launch(), k_enum_plain<true><<<grid_for(pr.n_reads, 8), 256, 0, st>>>(fq, pr.seq_off, pr.seq_len, pr.n_reads, k, lo, hi,
+                                                                    label, off, nullptr, o_lo, o_hi, o_id, err));
+}
+
+}  // namespace mp

@@ -1,0 +1,21 @@
+#pragma once
+#include "k_reads.cuh"
+
+namespace mp {
+
+// K1: bucket counts.  cc (nullable): per-chunk u32 counts [nchunks][NB]; glob: u64 counts [NB]
+// (summed from cc when cc is given).
+void launch_count(const uint8_t *fq, const ParsedReads &pr, int k, int min3, const uint64_t *chunk_rec, int nchunks,
+                  uint32_t *cc, unsigned long long *glob, uint32_t *err, cudaStream_t st);
+
+// K2a: tuples per read in the bucket range [lo, hi).
+void launch_enum_count(const uint8_t *fq, const ParsedReads &pr, int k, int min3, uint32_t lo, uint32_t hi,
+                       uint32_t *cnt, uint32_t *err, cudaStream_t st);
+
+// K2b: tuples at off[read]: o_lo = kmer << 8 | adj, o_hi = kmer >> 56 (nullable when k <= 28),
+// o_id = read id (scan 0, label == nullptr) or its component label.
+void launch_enum_write(const uint8_t *fq, const ParsedReads &pr, int k, int min3, uint32_t lo, uint32_t hi,
+                       const uint32_t *label, const uint64_t *off, uint64_t *o_lo, uint8_t *o_hi, uint32_t *o_id,
+                       uint32_t *err, cudaStream_t st);
+
+}  // namespace mp

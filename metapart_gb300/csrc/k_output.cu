@@ -1,0 +1,161 @@
+// K7: partition FASTQ output (writeOutput3, metapart.c:956-1066).
+//
+// Output file j = partition * T + tid holds, in input order, every record whose
+// component root falls in the partition's read-id range, written by thread tid (the
+// thread owning the record's chunk).  An interleaved pair is written to the partition of
+// mate 1's root and, when mate 2's root differs, again to mate 2's (:1006-1047).  On the
+// GPU each (file, unit) entry is generated in input order, entries are stably sorted by
+// file, their byte offsets come from one exclusive scan, and a warp copies each record.
+#include "k_output.cuh"
+#include "k_sort.cuh"
+
+namespace mp {
+
+__device__ __forceinline__ uint32_t part_of(const uint64_t *bounds, uint32_t root)
+{
+    uint32_t p = 0;
+    while (p < 16 && !((uint64_t)root < bounds[p + 1])) p++;
+    return p;
+}
+
+struct OutCtx {
+    const uint64_t *rec_start;
+    const uint32_t *label;
+    const uint64_t *bounds;    // 17
+    const uint64_t *chunk_rec; // nchunks + 1
+    int nchunks, T, per_thread, interleaved;
+    uint64_t units;
+};
+
+__device__ __forceinline__ uint32_t tid_of(const OutCtx &c, uint64_t rec)
+{
+    int lo = 0, hi = c.nchunks - 1;
+    while (lo < hi) {
+        int m = (lo + hi + 1) >> 1;
+        if (c.chunk_rec[m] <= rec) lo = m; else hi = m - 1;
+    }
+    return (uint32_t)(lo / c.per_thread);
+}
+
+// entries per unit (1 or 2) and the file of each
+__global__ void k_out_dest(OutCtx c, uint32_t *nent, uint32_t *f1, uint32_t *f2)
+{
+    const uint64_t u = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (u >= c.units) return;
+    const uint64_t r = c.interleaved ? 2 * u : u;
+    const uint32_t t = tid_of(c, r);
+    const uint32_t pu = c.label[r];
+    f1[u] = part_of(c.bounds, pu) * c.T + t;
+    uint32_t ne = 1;
+    if (c.interleaved) {
+        const uint32_t pv = c.label[r + 1];
+        if (pu != pv) {
+            f2[u] = part_of(c.bounds, pv) * c.T + t;
+            ne = 2;
+        }
+    }
+    nent[u] = ne;
+}
+
+__global__ void k_out_entries(OutCtx c, const uint32_t *f1, const uint32_t *f2, const uint32_t *nent,
+                              const uint64_t *eoff, uint64_t *key, uint32_t *val)
+{
+    const uint64_t u = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (u >= c.units) return;
+    const uint64_t o = eoff[u];
+    key[o] = f1[u];
+    val[o] = (uint32_t)u;
+    if (nent[u] == 2) {
+        key[o + 1] = f2[u];
+        val[o + 1] = (uint32_t)u;
+    }
+}
+
+__global__ void k_out_len(OutCtx c, const uint32_t *val, uint64_t n, uint64_t *len, const uint64_t *key,
+                          unsigned long long *file_bytes)
+{
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint64_t u = val[i];
+    const uint64_t r0 = c.interleaved ? 2 * u : u, r1 = c.interleaved ? 2 * u + 2 : u + 1;
+    const uint64_t l = c.rec_start[r1] - c.rec_start[r0];
+    len[i] = l;
+    atomicAdd(&file_bytes[key[i]], (unsigned long long)l);
+}
+
+__global__ void k_out_copy(OutCtx c, const uint8_t *fq, const uint32_t *val, const uint64_t *off, uint64_t n, uint8_t *out)
+{
+    const uint64_t w = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (w >= n) return;
+    const uint64_t u = val[w];
+    const uint64_t r0 = c.interleaved ? 2 * u : u, r1 = c.interleaved ? 2 * u + 2 : u + 1;
+    const uint64_t s = c.rec_start[r0], l = c.rec_start[r1] - s, o = off[w];
+    for (uint64_t q = lane; q < l; q += 32) out[o + q] = fq[s + q];
+}
+
+int gather_output(const uint8_t *d_fq, const ParsedReads &pr, const uint32_t *d_label, const uint64_t *bounds_host,
+                  const uint64_t *chunk_rec_host, int nchunks, int T, int interleaved, uint8_t **d_out,
+                  uint64_t *total_out, std::vector<uint64_t> &file_sizes, DeviceArena &arena, cudaStream_t st)
+{
+    const uint64_t units = interleaved ? pr.n_reads / 2 : pr.n_reads;
+    const int nf = 16 * T;
+    file_sizes.assign(nf, 0);
+    OutCtx c;
+    c.rec_start = pr.rec_start;
+    c.label = d_label;
+    c.nchunks = nchunks;
+    c.T = T;
+    c.per_thread = nchunks / T;
+    c.interleaved = interleaved;
+    c.units = units;
+    uint64_t *bounds = arena.alloc<uint64_t>(17), *chunk_rec = arena.alloc<uint64_t>(nchunks + 1);
+    uint32_t *nent = arena.alloc<uint32_t>(units + 1), *f1 = arena.alloc<uint32_t>(units + 1),
+             *f2 = arena.alloc<uint32_t>(units + 1);
+    uint64_t *eoff = arena.alloc<uint64_t>(units + 1), *ntot = arena.alloc<uint64_t>(1);
+    unsigned long long *fbytes = arena.alloc<unsigned long long>(nf);
+    size_t tb = scan_tmp_bytes(2 * units + 2);
+    void *tmp = arena.alloc<uint8_t>(tb);
+    if (!bounds || !chunk_rec || !nent || !f1 || !f2 || !eoff || !ntot || !fbytes || !tmp)
+        return set_error(MP_ENOMEM, "device memory for the output gather");
+    MP_CUDA(cudaMemcpyAsync(bounds, bounds_host, 17 * sizeof(uint64_t), cudaMemcpyHostToDevice, st));
+    MP_CUDA(cudaMemcpyAsync(chunk_rec, chunk_rec_host, (nchunks + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, st));
+    MP_CUDA(cudaMemsetAsync(fbytes, 0, nf * sizeof(unsigned long long), st));
+    c.bounds = bounds;
+    c.chunk_rec = chunk_rec;
+    const unsigned gb = (unsigned)((units + 255) / 256);
+    (mp::count_launch(), k_out_dest<<<gb, 256, 0, st>>>(c, nent, f1, f2));
+    scan_u32_to_u64(nent, eoff, units, ntot, tmp, tb, st);
+    uint64_t n = 0;
+    MP_CUDA(cudaMemcpyAsync(&n, ntot, sizeof n, cudaMemcpyDeviceToHost, st));
+    MP_CUDA(cudaStreamSynchronize(st));
+    SortBufs sb;
+    for (int i = 0; i < 2; i++) {
+        sb.lo[i] = arena.alloc<uint64_t>(n + 1);
+        sb.id[i] = arena.alloc<uint32_t>(n + 1);
+        if (!sb.lo[i] || !sb.id[i]) return set_error(MP_ENOMEM, "device memory for the output entries");
+    }
+    (mp::count_launch(), k_out_entries<<<gb, 256, 0, st>>>(c, f1, f2, nent, eoff, sb.lo[0], sb.id[0]));
+    int rc = radix_sort(sb, n, false, arena, st, nullptr);
+    if (rc) return rc;
+    uint64_t *len = arena.alloc<uint64_t>(n + 1), *off = arena.alloc<uint64_t>(n + 1);
+    size_t tb2 = scan_tmp_bytes(n + 1);
+    void *tmp2 = arena.alloc<uint8_t>(tb2);
+    if (!len || !off || !tmp2) return set_error(MP_ENOMEM, "device memory for the output offsets");
+    const unsigned ge = (unsigned)((n + 255) / 256);
+    (mp::count_launch(), k_out_len<<<ge, 256, 0, st>>>(c, sb.id[sb.cur], n, len, sb.lo[sb.cur], fbytes));
+    scan_u64(len, off, n, ntot, tmp2, tb2, st);
+    uint64_t total = 0;
+    MP_CUDA(cudaMemcpyAsync(&total, ntot, sizeof total, cudaMemcpyDeviceToHost, st));
+    MP_CUDA(cudaMemcpyAsync(file_sizes.data(), fbytes, nf * sizeof(uint64_t), cudaMemcpyDeviceToHost, st));
+    MP_CUDA(cudaStreamSynchronize(st));
+    uint8_t *out = arena.alloc_persistent<uint8_t>(total + 16);
+    if (!out) return set_error(MP_ENOMEM, "device memory for the output bytes");
+    if (n) (mp::count_launch(), k_out_copy<<<(unsigned)((n * 32 + 255) / 256), 256, 0, st>>>(c, d_fq, sb.id[sb.cur], off, n, out));
+    MP_CUDA(cudaGetLastError());
+    *d_out = out;
+    *total_out = total;
+    return 0;
+}
+
+}  // namespace mp

@@ -1,0 +1,710 @@
+// C ABI of libmetapart_gpu.so (include/metapart_gpu.h): contexts, jobs and the stage drivers.
+#include <atomic>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "k_graph.cuh"
+#include "k_kmers.cuh"
+#include "k_output.cuh"
+#include "k_reads.cuh"
+#include "k_sort.cuh"
+
+namespace mp {
+
+static thread_local std::string g_err;
+
+int set_error(int code, const char *fmt, ...)
+{
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return code;
+}
+
+int set_cuda_error(cudaError_t e, const char *what, const char *file, int line)
+{
+    return set_error(MP_ECUDA, "%s: %s (%s:%d)", what, cudaGetErrorString(e), file, line);
+}
+
+constexpr uint64_t UMAX32 = 4294967295ull;
+
+static std::atomic<uint64_t> g_launches{0};
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
+}  // namespace mp
+
+using namespace mp;
+
+struct mp_ctx {
+    int device = 0;
+    uint64_t budget = ~0ull;
+    uint64_t used = 0;
+    std::mutex mu;
+};
+
+struct mp_job {
+    mp_ctx *ctx = nullptr;
+    cudaStream_t st = nullptr;
+    DeviceArena arena;
+    uint8_t *d_fq = nullptr;
+    uint64_t fq_bytes = 0;
+    int interleaved = 0;
+    ParsedReads pr;
+    // partition state
+    uint32_t *d_parent = nullptr;
+    uint32_t *d_size = nullptr;
+    uint8_t *d_filtered = nullptr;
+    int T = 0, nchunks = 0;
+    std::vector<uint64_t> chunk_rec;
+    uint64_t bounds[17] = {0};
+    bool partitioned = false;
+    // output
+    uint8_t *d_out = nullptr;
+    uint64_t out_total = 0;
+    std::vector<uint64_t> out_sizes;
+    bool output_ready = false;
+    std::string dump_dir;
+    double stage_ms[8] = {0};
+    SortStats sort_stats;
+    int sort_passes_total = 0;
+    double sort_ms_total = 0;
+    uint64_t sort_bytes_total = 0, sort_tuples_total = 0;
+    int pe_rounds = 0;
+};
+
+// ------------------------------------------------------------------ helpers
+
+namespace {
+
+struct StageTimer {
+    cudaEvent_t a, b;
+    cudaStream_t st;
+    double *acc;
+    StageTimer(cudaStream_t s, double *slot) : st(s), acc(slot)
+    {
+        cudaEventCreate(&a);
+        cudaEventCreate(&b);
+        cudaEventRecord(a, st);
+    }
+    ~StageTimer()
+    {
+        cudaEventRecord(b, st);
+        cudaEventSynchronize(b);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, a, b);
+        *acc += ms;
+        cudaEventDestroy(a);
+        cudaEventDestroy(b);
+    }
+};
+
+int write_file(const std::string &path, const void *buf, size_t n)
+{
+    FILE *f = fopen(path.c_str(), "wb");
+    if (!f) return set_error(MP_EIO, "cannot write %s", path.c_str());
+    size_t w = n ? fwrite(buf, 1, n, f) : 0;
+    fclose(f);
+    if (w != n) return set_error(MP_EIO, "short write %s", path.c_str());
+    return 0;
+}
+
+// Dump of tuples in the reference's 14-byte record format (enumerateKmers.c:352-365).
+int dump_tuples(mp_job *j, const char *name, const uint64_t *lo, const uint8_t *hi, const uint32_t *id, uint64_t n)
+{
+    if (j->dump_dir.empty()) return 0;
+    std::vector<uint64_t> hl(n);
+    std::vector<uint8_t> hh(hi ? n : 0);
+    std::vector<uint32_t> hid(n);
+    if (n) {
+        MP_CUDA(cudaMemcpyAsync(hl.data(), lo, n * 8, cudaMemcpyDeviceToHost, j->st));
+        if (hi) MP_CUDA(cudaMemcpyAsync(hh.data(), hi, n, cudaMemcpyDeviceToHost, j->st));
+        MP_CUDA(cudaMemcpyAsync(hid.data(), id, n * 4, cudaMemcpyDeviceToHost, j->st));
+        MP_CUDA(cudaStreamSynchronize(j->st));
+    }
+    std::vector<uint8_t> b(n * 14);
+    for (uint64_t i = 0; i < n; i++) {
+        uint64_t kmer = (hl[i] >> 8) | (hi ? ((uint64_t)hh[i] << 56) : 0);
+        uint16_t w4 = (uint16_t)(hl[i] & 0xFF);
+        memcpy(&b[i * 14], &kmer, 8);
+        memcpy(&b[i * 14 + 8], &w4, 2);
+        memcpy(&b[i * 14 + 10], &hid[i], 4);
+    }
+    return write_file(j->dump_dir + "/" + name, b.data(), b.size());
+}
+
+// Parent (5-byte encoding, BAD = 0xBADBADBAD) and sizes, as printStats leaves them.
+int dump_state(mp_job *j, const char *pname, const char *sname, bool with_parent = true)
+{
+    if (j->dump_dir.empty()) return 0;
+    const uint64_t n = j->pr.n_reads;
+    std::vector<uint32_t> p(n), s(n);
+    MP_CUDA(cudaMemcpyAsync(p.data(), j->d_parent, n * 4, cudaMemcpyDeviceToHost, j->st));
+    MP_CUDA(cudaMemcpyAsync(s.data(), j->d_size, n * 4, cudaMemcpyDeviceToHost, j->st));
+    MP_CUDA(cudaStreamSynchronize(j->st));
+    int rc = 0;
+    if (with_parent) {
+        std::vector<uint8_t> b(n * 5);
+        for (uint64_t i = 0; i < n; i++) {
+            uint64_t v = p[i] == BAD ? 0xBADBADBADull : p[i];
+            uint32_t rem = (uint32_t)(v % UMAX32);
+            b[i * 5] = (uint8_t)(v / UMAX32);
+            memcpy(&b[i * 5 + 1], &rem, 4);
+        }
+        rc = write_file(j->dump_dir + "/" + pname, b.data(), b.size());
+    }
+    if (!rc && sname) rc = write_file(j->dump_dir + "/" + sname, s.data(), n * 4);
+    return rc;
+}
+
+__global__ void k_init_parent(uint32_t *parent, uint64_t n)
+{
+    const uint64_t x = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (x < n) parent[x] = (uint32_t)x;
+}
+
+__global__ void k_sizes_raw(const uint32_t *parent, uint64_t n, uint32_t *size)
+{
+    const uint64_t x = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= n) return;
+    const uint32_t p = parent[x];
+    atomicAdd(&size[(p == BAD || p == x) ? (uint32_t)x : p], 1u);
+}
+
+// The reference's scan / thread k-mer range planner at one rank (metapart.c:3720-3791).
+int plan_ranges(const uint64_t *hist, int S, int T, std::vector<uint64_t> &scanR, std::vector<uint64_t> &thrR)
+{
+    const uint64_t total = hist[NB];
+    if (total == 0) return set_error(MP_EUNSUP, "the histogram holds no k-mers");
+    scanR.assign(S + 1, 0);
+    thrR.assign((size_t)S * T + 1, 0);
+    const uint64_t avg = total / (uint64_t)S + (total % (uint64_t)S ? 1 : 0);
+    uint64_t cr = 1, i;
+    for (i = 0; i < NB; i++)
+        if (hist[i] >= avg * cr) {
+            if (cr <= (uint64_t)S) scanR[cr] = i;
+            cr++;
+        }
+    if (cr == (uint64_t)S) scanR[cr] = i;
+    const uint64_t avgT = avg / (uint64_t)T;
+    cr = 1;
+    for (i = 0; i < NB; i++)
+        if (hist[i] >= cr * avgT) {
+            if (cr <= (uint64_t)S * T) thrR[cr] = (cr % (uint64_t)T == 0) ? scanR[cr / T] : i;
+            cr++;
+        }
+    if (cr == (uint64_t)S * T) thrR[cr] = i;
+    return 0;
+}
+
+// Tuple-index bounds of the thread ranges of one scan: the range partition bins a bucket
+// to the last range whose start is not above it (metapart.c:2019-2022); the reference
+// sizes its bins from [start_t, start_t+1) (metapart.c:1810-1850), so the two must agree.
+int range_bounds(const uint64_t *hist, const uint64_t *ltr, int T, uint64_t scan_lo, uint64_t scan_hi,
+                 std::vector<uint64_t> &bounds)
+{
+    std::vector<uint64_t> cnt(T, 0);
+    for (uint64_t b = scan_lo; b < scan_hi; b++) {
+        const uint64_t c = hist[b + 1] - hist[b];
+        if (!c) continue;
+        int cb = 0;
+        while (cb <= T && b >= ltr[cb]) cb++;
+        cb--;
+        if (cb < 0 || cb >= T) return set_error(MP_EUNSUP, "thread k-mer ranges do not cover bucket %llu", (unsigned long long)b);
+        cnt[cb] += c;
+    }
+    bounds.assign(T + 1, 0);
+    for (int t = 0; t < T; t++) {
+        const uint64_t ref = ltr[t + 1] > ltr[t] ? hist[ltr[t + 1]] - hist[ltr[t]] : 0;
+        if (ref != cnt[t]) return set_error(MP_EUNSUP, "thread k-mer ranges are not monotone over populated buckets");
+        bounds[t + 1] = bounds[t] + cnt[t];
+    }
+    return 0;
+}
+
+int chunk_records(mp_job *j, const uint64_t *chunk_starts, int nchunks, std::vector<uint64_t> &rec)
+{
+    rec.assign(nchunks + 1, 0);
+    for (int c = 0; c < nchunks; c++)
+        if (chunk_starts[c + 1] < chunk_starts[c]) return set_error(MP_EFMT, "chunk offsets are not ascending");
+    if (chunk_starts[0] != 0 || chunk_starts[nchunks] != j->fq_bytes)
+        return set_error(MP_EFMT, "chunks do not cover the input");
+    return records_at_offsets(&j->pr, chunk_starts, nchunks + 1, rec.data(), j->arena, j->st);
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ C ABI
+
+extern "C" {
+
+const char *mp_last_error(void) { return g_err.c_str(); }
+
+int mp_ctx_create(int device, uint64_t hbm_budget_bytes, mp_ctx **out)
+{
+    if (!out) return set_error(MP_EARG, "null output pointer");
+    int n = 0;
+    MP_CUDA(cudaGetDeviceCount(&n));
+    if (device < 0 || device >= n) return set_error(MP_EARG, "no CUDA device %d", device);
+    MP_CUDA(cudaSetDevice(device));
+    cudaDeviceProp prop;
+    MP_CUDA(cudaGetDeviceProperties(&prop, device));
+    if (prop.major < 10) return set_error(MP_EUNSUP, "device %d (%s) is not a Blackwell GPU", device, prop.name);
+    mp_ctx *c = new mp_ctx;
+    c->device = device;
+    c->budget = hbm_budget_bytes ? hbm_budget_bytes : ~0ull;
+    // keep freed stream-ordered memory in the pool between jobs
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+        uint64_t thr = ~0ull;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+    }
+    *out = c;
+    return 0;
+}
+
+void mp_ctx_destroy(mp_ctx *ctx) { delete ctx; }
+
+uint64_t mp_ctx_hbm_in_use(const mp_ctx *ctx) { return ctx ? ctx->used : 0; }
+
+int mp_job_create(mp_ctx *ctx, mp_job **out)
+{
+    if (!ctx || !out) return set_error(MP_EARG, "null argument");
+    MP_CUDA(cudaSetDevice(ctx->device));
+    mp_job *j = new mp_job;
+    j->ctx = ctx;
+    if (cudaStreamCreateWithFlags(&j->st, cudaStreamNonBlocking) != cudaSuccess) {
+        delete j;
+        return set_error(MP_ECUDA, "cannot create a stream");
+    }
+    j->arena.st = j->st;
+    j->arena.budget_used = &ctx->used;
+    j->arena.budget_limit = ctx->budget;
+    *out = j;
+    return 0;
+}
+
+void mp_job_destroy(mp_job *job)
+{
+    if (!job) return;
+    cudaSetDevice(job->ctx->device);
+    job->arena.release_all();
+    cudaStreamSynchronize(job->st);
+    cudaStreamDestroy(job->st);
+    delete job;
+}
+
+static int load_common(mp_job *j, uint64_t nbytes, const uint64_t *file_sizes, int nfiles, int interleaved)
+{
+    uint64_t tot = 0;
+    for (int f = 0; f < nfiles; f++) tot += file_sizes[f];
+    if (tot != nbytes) return set_error(MP_EARG, "file sizes do not add up to the input size");
+    j->fq_bytes = nbytes;
+    j->interleaved = interleaved;
+    {
+        StageTimer tm(j->st, &j->stage_ms[0]);
+        int rc = parse_fastq(j->d_fq, nbytes, &j->pr, j->arena, j->st);
+        if (rc) return rc;
+    }
+    // each file must end on a record end
+    std::vector<uint64_t> ends;
+    uint64_t acc = 0;
+    for (int f = 0; f < nfiles; f++) { acc += file_sizes[f]; ends.push_back(acc); }
+    ends.pop_back();
+    if (!ends.empty()) {
+        std::vector<uint64_t> rec(ends.size());
+        int rc = records_at_offsets(&j->pr, ends.data(), (int)ends.size(), rec.data(), j->arena, j->st);
+        if (rc) return set_error(MP_EFMT, "a FASTQ file does not end on a record boundary");
+    }
+    if (interleaved && (j->pr.n_reads & 1)) return set_error(MP_EFMT, "interleaved input with an odd record count");
+    if (j->pr.n_reads >= UMAX32) return set_error(MP_EUNSUP, "more than 2^32 - 2 reads");
+    return 0;
+}
+
+int mp_job_load_fastq(mp_job *j, const char *bytes, uint64_t nbytes, const uint64_t *file_sizes, int nfiles,
+                      int interleaved)
+{
+    if (!j || !bytes || !file_sizes || nfiles < 1) return set_error(MP_EARG, "null argument");
+    MP_CUDA(cudaSetDevice(j->ctx->device));
+    if (j->d_fq) return set_error(MP_EARG, "the job already holds reads");
+    j->d_fq = j->arena.alloc_persistent<uint8_t>(nbytes + 64);
+    if (!j->d_fq) return set_error(MP_ENOMEM, "device memory for %llu FASTQ bytes", (unsigned long long)nbytes);
+    MP_CUDA(cudaMemcpyAsync(j->d_fq, bytes, nbytes, cudaMemcpyHostToDevice, j->st));
+    MP_CUDA(cudaMemsetAsync(j->d_fq + nbytes, 0, 64, j->st));
+    return load_common(j, nbytes, file_sizes, nfiles, interleaved);
+}
+
+int mp_job_load_fastq_device(mp_job *j, const void *dev_bytes, uint64_t nbytes, const uint64_t *file_sizes, int nfiles,
+                             int interleaved)
+{
+    if (!j || !dev_bytes || !file_sizes || nfiles < 1) return set_error(MP_EARG, "null argument");
+    MP_CUDA(cudaSetDevice(j->ctx->device));
+    if (j->d_fq) return set_error(MP_EARG, "the job already holds reads");
+    j->d_fq = j->arena.alloc_persistent<uint8_t>(nbytes + 64);
+    if (!j->d_fq) return set_error(MP_ENOMEM, "device memory for %llu FASTQ bytes", (unsigned long long)nbytes);
+    MP_CUDA(cudaMemcpyAsync(j->d_fq, dev_bytes, nbytes, cudaMemcpyDeviceToDevice, j->st));
+    MP_CUDA(cudaMemsetAsync(j->d_fq + nbytes, 0, 64, j->st));
+    return load_common(j, nbytes, file_sizes, nfiles, interleaved);
+}
+
+uint64_t mp_job_num_reads(const mp_job *j) { return j ? j->pr.n_reads : 0; }
+
+int mp_job_reset(mp_job *j)
+{
+    if (!j) return set_error(MP_EARG, "null job");
+    MP_CUDA(cudaSetDevice(j->ctx->device));
+    j->arena.release_all();
+    MP_CUDA(cudaStreamSynchronize(j->st));
+    j->d_fq = nullptr;
+    j->fq_bytes = 0;
+    j->pr = ParsedReads{};
+    j->d_parent = j->d_size = nullptr;
+    j->d_filtered = nullptr;
+    j->d_out = nullptr;
+    j->partitioned = j->output_ready = false;
+    return 0;
+}
+
+void *mp_job_stream(mp_job *j) { return j ? (void *)j->st : nullptr; }
+
+uint64_t mp_launch_count(void) { return g_launches.load(); }
+
+int mp_job_count(mp_job *j, int k, int min3, const uint64_t *chunk_starts, int nchunks, uint64_t *hist_out,
+                 uint32_t *chunk_counts_out, uint64_t *chunk_reads_out)
+{
+    if (!j || !j->d_fq || !chunk_starts || !hist_out || nchunks < 1) return set_error(MP_EARG, "bad argument");
+    if (k < 11 || k > 31) return set_error(MP_EARG, "k must be in [11, 31]");
+    MP_CUDA(cudaSetDevice(j->ctx->device));
+    std::vector<uint64_t> rec;
+    int rc = chunk_records(j, chunk_starts, nchunks, rec);
+    if (rc) return rc;
+    j->stage_ms[1] = 0;
+    uint64_t *d_rec = j->arena.alloc<uint64_t>(nchunks + 1);
+    unsigned long long *glob = j->arena.alloc<unsigned long long>(NB);
+    uint32_t *cc = chunk_counts_out ? j->arena.alloc<uint32_t>((size_t)nchunks * NB) : nullptr;
+    uint32_t *err = j->arena.alloc<uint32_t>(1);
+    if (!d_rec || !glob || !err || (chunk_counts_out && !cc)) return set_error(MP_ENOMEM, "device memory for counting");
+    MP_CUDA(cudaMemcpyAsync(d_rec, rec.data(), (nchunks + 1) * 8, cudaMemcpyHostToDevice, j->st));
+    MP_CUDA(cudaMemsetAsync(glob, 0, NB * 8, j->st));
+    MP_CUDA(cudaMemsetAsync(err, 0, 4, j->st));
+    if (cc) MP_CUDA(cudaMemsetAsync(cc, 0, (size_t)nchunks * NB * 4, j->st));
+    {
+        StageTimer tm(j->st, &j->stage_ms[1]);
+        launch_count(j->d_fq, j->pr, k, min3, d_rec, nchunks, cc, glob, err, j->st);
+    }
+    std::vector<unsigned long long> g(NB);
+    uint32_t herr = 0;
+    MP_CUDA(cudaMemcpyAsync(g.data(), glob, NB * 8, cudaMemcpyDeviceToHost, j->st));
+    MP_CUDA(cudaMemcpyAsync(&herr, err, 4, cudaMemcpyDeviceToHost, j->st));
+    if (cc) MP_CUDA(cudaMemcpyAsync(chunk_counts_out, cc, (size_t)nchunks * NB * 4, cudaMemcpyDeviceToHost, j->st));
+    MP_CUDA(cudaStreamSynchronize(j->st));
+    MP_CUDA(cudaGetLastError());
+    j->arena.release_scratch();
+    if (herr & DERR_LONG_READ) return set_error(MP_EUNSUP, "a read is longer than %d bases", MAX_READ_COUNT);
+    hist_out[0] = 0;
+    for (uint32_t b = 1; b <= NB; b++) hist_out[b] = hist_out[b - 1] + g[b - 1];
+    if (chunk_reads_out)
+        for (int c = 0; c < nchunks; c++) chunk_reads_out[c] = rec[c + 1] - rec[c];
+    return 0;
+}
+
+int mp_job_partition(mp_job *j, const mp_part_params *p, const uint64_t *chunk_starts, const uint64_t *chunk_first_read,
+                     int nchunks, const uint64_t *hist, uint64_t *bounds_out)
+{
+    if (!j || !j->d_fq || !p || !chunk_starts || !chunk_first_read || !hist || nchunks < 1)
+        return set_error(MP_EARG, "bad argument");
+    const int k = p->k, S = p->num_scans, T = p->num_threads;
+    if (k < 11 || k > 31) return set_error(MP_EARG, "k must be in [11, 31]");
+    if (S < 1 || T < 1 || T > 256) return set_error(MP_EARG, "numScans must be >= 1 and numThreads in [1, 256]");
+    if (nchunks % T) return set_error(MP_EARG, "numThreads must divide the number of chunks");
+    if (p->min3 && S != 1) return set_error(MP_EUNSUP, "the 3-minimizer variant needs numScans == 1");
+    MP_CUDA(cudaSetDevice(j->ctx->device));
+    const uint64_t N = j->pr.n_reads;
+    std::vector<uint64_t> rec;
+    int rc = chunk_records(j, chunk_starts, nchunks, rec);
+    if (rc) return rc;
+    for (int c = 0; c <= nchunks; c++)
+        if (chunk_first_read[c] != rec[c])
+            return set_error(MP_EFMT, "index read id of chunk %d (%llu) does not match the FASTQ (%llu)", c,
+                             (unsigned long long)chunk_first_read[c], (unsigned long long)rec[c]);
+    if (N & 1) return set_error(MP_EUNSUP, "the mate union needs an even read count");
+    if (j->interleaved)
+        for (int c = 0; c < nchunks; c++)
+            if ((rec[c + 1] - rec[c]) & 1) return set_error(MP_EFMT, "interleaved chunk %d has an odd record count", c);
+    std::vector<uint64_t> scanR, thrR;
+    if ((rc = plan_ranges(hist, S, T, scanR, thrR))) return rc;
+    j->T = T;
+    j->nchunks = nchunks;
+    j->chunk_rec = rec;
+    j->partitioned = false;
+    j->output_ready = false;
+    for (int s = 2; s < 8; s++) j->stage_ms[s] = 0;
+    j->sort_passes_total = 0;
+    j->sort_ms_total = 0;
+    j->sort_bytes_total = 0;
+    j->sort_tuples_total = 0;
+    if (j->d_parent) { j->arena.free_persistent(j->d_parent); j->d_parent = nullptr; }
+    if (j->d_size) { j->arena.free_persistent(j->d_size); j->d_size = nullptr; }
+    if (j->d_filtered) { j->arena.free_persistent(j->d_filtered); j->d_filtered = nullptr; }
+    if (j->d_out) { j->arena.free_persistent(j->d_out); j->d_out = nullptr; }
+    j->d_parent = j->arena.alloc_persistent<uint32_t>(N + 1);
+    j->d_size = j->arena.alloc_persistent<uint32_t>(N + 1);
+    j->d_filtered = j->arena.alloc_persistent<uint8_t>(N + 1);
+    uint32_t *err = j->arena.alloc_persistent<uint32_t>(1);
+    if (!j->d_parent || !j->d_size || !j->d_filtered || !err) return set_error(MP_ENOMEM, "device memory for the forest");
+    const unsigned gN = (unsigned)((N + 255) / 256);
+    (mp::count_launch(), k_init_parent<<<gN, 256, 0, j->st>>>(j->d_parent, N));
+    MP_CUDA(cudaMemsetAsync(j->d_filtered, 0, N + 1, j->st));
+    MP_CUDA(cudaMemsetAsync(err, 0, 4, j->st));
+    const bool has_hi = 2 * k + 8 > 64;
+    char name[64], name2[64];
+    for (int s = 0; s < S; s++) {
+        const uint64_t lo = scanR[s], hi = scanR[s + 1];
+        const uint64_t expect = hist[hi] - hist[lo];
+        uint32_t *cnt = j->arena.alloc<uint32_t>(N + 1);
+        uint64_t *off = j->arena.alloc<uint64_t>(N + 2), *ntot = j->arena.alloc<uint64_t>(1);
+        size_t tb = scan_tmp_bytes(N + 1);
+        void *tmp = j->arena.alloc<uint8_t>(tb);
+        if (!cnt || !off || !ntot || !tmp) return set_error(MP_ENOMEM, "device memory for enumeration offsets");
+        SortBufs sb;
+        uint64_t n = 0;
+        {
+            StageTimer tm(j->st, &j->stage_ms[2]);
+            launch_enum_count(j->d_fq, j->pr, k, p->min3, (uint32_t)lo, (uint32_t)hi, cnt, err, j->st);
+            MP_CUDA(cudaMemsetAsync(cnt + N, 0, 4, j->st));
+            scan_u32_to_u64(cnt, off, N + 1, ntot, tmp, tb, j->st);
+            uint32_t cerr = 0;
+            MP_CUDA(cudaMemcpyAsync(&n, ntot, 8, cudaMemcpyDeviceToHost, j->st));
+            MP_CUDA(cudaMemcpyAsync(&cerr, err, 4, cudaMemcpyDeviceToHost, j->st));
+            MP_CUDA(cudaStreamSynchronize(j->st));
+            if (cerr & DERR_LONG_READ) return set_error(MP_EUNSUP, "a read has 300 or more k-mer positions");
+            if (cerr & DERR_TOO_MANY)
+                return set_error(MP_EUNSUP, "a read has 256 or more k-mers in scan %d (the reference counts them "
+                                            "in 8 bits, enumerateKmers.c:152)", s);
+            if (n != expect)
+                return set_error(MP_EFMT, "scan %d: %llu tuples but the histogram holds %llu", s, (unsigned long long)n,
+                                 (unsigned long long)expect);
+            for (int b = 0; b < 2; b++) {
+                sb.lo[b] = j->arena.alloc<uint64_t>(n + 1);
+                sb.id[b] = j->arena.alloc<uint32_t>(n + 1);
+                sb.hi[b] = has_hi ? j->arena.alloc<uint8_t>(n + 1) : nullptr;
+                if (!sb.lo[b] || !sb.id[b] || (has_hi && !sb.hi[b]))
+                    return set_error(MP_ENOMEM, "device memory for %llu tuples", (unsigned long long)n);
+            }
+            launch_enum_write(j->d_fq, j->pr, k, p->min3, (uint32_t)lo, (uint32_t)hi, s ? j->d_parent : nullptr, off,
+                              sb.lo[0], sb.hi[0], sb.id[0], err, j->st);
+        }
+        uint32_t herr = 0;
+        MP_CUDA(cudaMemcpyAsync(&herr, err, 4, cudaMemcpyDeviceToHost, j->st));
+        MP_CUDA(cudaStreamSynchronize(j->st));
+        if (herr & DERR_LONG_READ) return set_error(MP_EUNSUP, "a read has 300 or more k-mer positions");
+        if (herr & DERR_TOO_MANY)
+            return set_error(MP_EUNSUP, "a read has 256 or more k-mers in scan %d (the reference counts them in 8 bits, "
+                                        "enumerateKmers.c:152)", s);
+        if (herr) return set_error(MP_EDEVICE, "enumeration flags 0x%x", herr);
+        snprintf(name, sizeof name, "scan%d_enum.bin", s);
+        if ((rc = dump_tuples(j, name, sb.lo[0], sb.hi[0], sb.id[0], n))) return rc;
+        {
+            StageTimer tm(j->st, &j->stage_ms[3]);
+            SortStats ss;
+            if ((rc = radix_sort(sb, n, has_hi, j->arena, j->st, &ss))) return rc;
+            j->sort_stats = ss;
+            j->sort_passes_total += ss.passes;
+            j->sort_ms_total += ss.pass_ms;
+            j->sort_bytes_total += ss.bytes;
+            j->sort_tuples_total += n;
+        }
+        Tuples tp;
+        tp.lo = sb.lo[sb.cur];
+        tp.hi = has_hi ? sb.hi[sb.cur] : nullptr;
+        tp.id = sb.id[sb.cur];
+        tp.n = n;
+        snprintf(name, sizeof name, "scan%d_sorted.bin", s);
+        if ((rc = dump_tuples(j, name, tp.lo, tp.hi, tp.id, n))) return rc;
+        std::vector<uint64_t> rb;
+        if ((rc = range_bounds(hist, thrR.data() + (size_t)s * T, T, lo, hi, rb))) return rc;
+        {
+            StageTimer tm(j->st, &j->stage_ms[4]);
+            if ((rc = filter_scan(tp, rb, j->d_parent, j->d_filtered, j->arena, j->st))) return rc;
+        }
+        snprintf(name, sizeof name, "scan%d_filtered.bin", s);
+        if ((rc = dump_tuples(j, name, tp.lo, tp.hi, tp.id, n))) return rc;
+        if (!j->dump_dir.empty()) {
+            std::vector<uint8_t> f(N);
+            MP_CUDA(cudaMemcpyAsync(f.data(), j->d_filtered, N, cudaMemcpyDeviceToHost, j->st));
+            MP_CUDA(cudaStreamSynchronize(j->st));
+            snprintf(name, sizeof name, "scan%d_bad.bin", s);
+            if ((rc = write_file(j->dump_dir + "/" + name, f.data(), N))) return rc;
+        }
+        {
+            StageTimer tm(j->st, &j->stage_ms[5]);
+            if ((rc = union_scan(tp, rb, j->d_parent, N, j->arena, j->st))) return rc;
+        }
+        j->arena.release_scratch();
+        snprintf(name, sizeof name, "stats%d_parent.bin", s);
+        if ((rc = dump_state(j, name, nullptr))) return rc;
+    }
+    {
+        StageTimer tm(j->st, &j->stage_ms[6]);
+        if (!j->dump_dir.empty()) {
+            MP_CUDA(cudaMemsetAsync(j->d_size, 0, N * 4, j->st));
+            (mp::count_launch(), k_sizes_raw<<<gN, 256, 0, j->st>>>(j->d_parent, N, j->d_size));
+            snprintf(name, sizeof name, "stats%d_parent.bin", S);
+            snprintf(name2, sizeof name2, "stats%d_sizes.bin", S);
+            if ((rc = dump_state(j, name, name2))) return rc;
+        }
+        if ((rc = mate_union_and_plan(j->d_parent, N, j->d_size, j->bounds, j->arena, j->st, &j->pe_rounds))) return rc;
+    }
+    j->arena.release_scratch();
+    snprintf(name, sizeof name, "stats%d_parent.bin", S + 1);
+    snprintf(name2, sizeof name2, "stats%d_sizes.bin", S + 1);
+    if ((rc = dump_state(j, name, name2))) return rc;
+    j->partitioned = true;
+    if (bounds_out) memcpy(bounds_out, j->bounds, sizeof j->bounds);
+    return 0;
+}
+
+int mp_job_labels(mp_job *j, uint32_t *out)
+{
+    if (!j || !out || !j->partitioned) return set_error(MP_EARG, "no partition result in this job");
+    MP_CUDA(cudaMemcpyAsync(out, j->d_parent, j->pr.n_reads * 4, cudaMemcpyDeviceToHost, j->st));
+    MP_CUDA(cudaStreamSynchronize(j->st));
+    return 0;
+}
+
+int mp_job_output(mp_job *j, char *out, uint64_t capacity, uint64_t *file_sizes, uint64_t *total)
+{
+    if (!j || !j->partitioned) return set_error(MP_EARG, "no partition result in this job");
+    MP_CUDA(cudaSetDevice(j->ctx->device));
+    if (!j->output_ready) {
+        StageTimer tm(j->st, &j->stage_ms[7]);
+        j->stage_ms[7] = 0;
+        int rc = gather_output(j->d_fq, j->pr, j->d_parent, j->bounds, j->chunk_rec.data(), j->nchunks, j->T,
+                               j->interleaved, &j->d_out, &j->out_total, j->out_sizes, j->arena, j->st);
+        j->arena.release_scratch();
+        if (rc) return rc;
+        j->output_ready = true;
+    }
+    if (file_sizes) memcpy(file_sizes, j->out_sizes.data(), j->out_sizes.size() * 8);
+    if (total) *total = j->out_total;
+    if (out) {
+        if (capacity < j->out_total) return set_error(MP_EARG, "output buffer too small");
+        MP_CUDA(cudaMemcpyAsync(out, j->d_out, j->out_total, cudaMemcpyDeviceToHost, j->st));
+        MP_CUDA(cudaStreamSynchronize(j->st));
+    }
+    return 0;
+}
+
+int mp_job_set_dump_dir(mp_job *j, const char *dir)
+{
+    if (!j) return set_error(MP_EARG, "null job");
+    j->dump_dir = dir ? dir : "";
+    return 0;
+}
+
+int mp_job_stage_ms(const mp_job *j, double *ms, int n)
+{
+    if (!j || !ms) return set_error(MP_EARG, "null argument");
+    for (int i = 0; i < n && i < 8; i++) ms[i] = j->stage_ms[i];
+    return 0;
+}
+
+int mp_job_sort_stats(const mp_job *j, uint64_t *tuples, int *passes, double *pass_ms, uint64_t *bytes)
+{
+    if (!j) return set_error(MP_EARG, "null job");
+    if (tuples) *tuples = j->sort_tuples_total;
+    if (passes) *passes = j->sort_passes_total;
+    if (pass_ms) *pass_ms = j->sort_ms_total;
+    if (bytes) *bytes = j->sort_bytes_total;
+    return 0;
+}
+
+// ------------------------------------------------------------- chunk index
+
+// genFastqIdx (genFastqIdx.c:142-376) for single-end / interleaved files held in memory.
+int mp_fastq_index(int num_chunks, int n_pe, int n_se, int n_il, int nfiles, const char *const *files,
+                   const uint64_t *sizes, int32_t *out_file_no, uint64_t *out_offsets, int *out_count)
+{
+    if (!files || !sizes || !out_file_no || !out_offsets || !out_count || nfiles < 1 || num_chunks < 1)
+        return set_error(MP_EARG, "bad argument");
+    if (n_pe != 0) return set_error(MP_EUNSUP, "two-file paired-end input is not supported");
+    if (n_se + n_il != nfiles || n_se < 0 || n_il < 0) return set_error(MP_EARG, "file counts do not match the file list");
+    if (n_se && n_il) return set_error(MP_EUNSUP, "mixing single-end and interleaved files is not supported");
+    uint64_t total = 0;
+    for (int i = 0; i < nfiles; i++) total += sizes[i];
+    const uint64_t per = total / (uint64_t)num_chunks;
+    int max_read = 300, interleaved = 0, nrec = 0;
+    int32_t fno = 0;
+    uint64_t ofs = 0;
+    for (int c = 0; c < num_chunks; c++) {
+        uint64_t rem = per * (uint64_t)c;  // getFileIndex (:28-53)
+        fno = 0;
+        while (rem >= sizes[fno]) { rem -= sizes[fno]; fno++; }
+        ofs = rem;
+        if (fno >= n_se) interleaved = 1;
+        if (sizes[fno] - ofs < (uint64_t)max_read) {
+            if (fno + 1 == nfiles) break;
+            fno++;
+            ofs = 0;
+        }
+        if (c == 0) {
+            out_file_no[nrec] = fno;
+            out_offsets[nrec++] = ofs;
+            continue;
+        }
+        // record boundary search in a 3000-byte read of the file (:254-307); bytes past the
+        // read count as zero, as in a zero-filled buffer
+        const char *base = files[fno] + ofs;
+        const uint64_t avail = sizes[fno] - ofs, nread = avail < 3000 ? avail : 3000;
+        if (nread <= (uint64_t)max_read) return set_error(MP_EFMT, "chunk %d starts too close to a file end", c);
+        const uint64_t CAP = 5000;
+        auto at = [&](uint64_t i) -> int { return i < nread ? (unsigned char)base[i] : 0; };
+        uint64_t jj = 0;
+        int flag = 0, kk = 0, found = 0;
+        for (jj = 0; jj < nread; jj++) {
+            if (at(jj) == '\n' && at(jj + 1) == '+') {
+                flag = 1;
+                jj += 2;
+                while (jj < CAP && at(jj) != '\n') jj++;
+                jj++;
+            }
+            kk = 0;
+            if (flag && at(jj) == '\n') {
+                jj++;
+                kk++;
+                if (interleaved) {
+                    uint64_t q = jj;
+                    std::string a, b;
+                    while (q < CAP && at(q) != '/' && at(q) != ' ') a.push_back((char)at(q++));
+                    for (int l = 0; l < 4; l++) {
+                        while (q < CAP && at(q) != '\n') q++;
+                        q++;
+                    }
+                    const uint64_t j2 = q;
+                    while (q < CAP && at(q) != ' ' && at(q) != '/') b.push_back((char)at(q++));
+                    if (q >= CAP) return set_error(MP_EFMT, "mate names not found near chunk %d", c);
+                    kk = (int)q;
+                    if (a != b) jj = j2;
+                }
+                found = 1;
+                break;
+            }
+        }
+        if (!found) return set_error(MP_EFMT, "no record boundary within 3000 bytes of chunk %d", c);
+        if (2 * kk + 30 < max_read) max_read = 2 * kk + 30;
+        out_file_no[nrec] = fno;
+        out_offsets[nrec++] = ofs + jj;
+    }
+    out_file_no[nrec] = nfiles - 1;
+    out_offsets[nrec++] = sizes[nfiles - 1];
+    *out_count = nrec;
+    return 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,268 @@
+"""ctypes front end of libmetapart_gpu.so (include/metapart_gpu.h).
+
+The stage functions mirror the reference programs' interfaces on in-memory data:
+``fastq_index`` <-> genFastqIdx, ``Job.count`` <-> genHistograms (count module), ``Job.partition`` <->
+metapart (enumerate, sort, filter, union-find, mate union), ``Job.output`` <-> writeOutput3.  Errors raise
+``MetapartError`` with the library's message; there is no CPU fallback: without the CUDA library or a GPU
+every call fails.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+from pathlib import Path
+
+import numpy as np
+
+from . import build
+
+NB = 1 << 20
+REC = 4194344
+_lib = None
+
+
+class MetapartError(RuntimeError):
+    pass
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = build.BUILD / "libmetapart_gpu.so"
+        if not path.exists():
+            raise MetapartError(f"{path} is missing: run metapart_gb300.build.build_all() first")
+        L = C.CDLL(str(path))
+        u64p, u32p, i32p = C.POINTER(C.c_uint64), C.POINTER(C.c_uint32), C.POINTER(C.c_int32)
+        L.mp_last_error.restype = C.c_char_p
+        L.mp_ctx_create.argtypes = [C.c_int, C.c_uint64, C.POINTER(C.c_void_p)]
+        L.mp_ctx_destroy.argtypes = [C.c_void_p]
+        L.mp_ctx_hbm_in_use.argtypes = [C.c_void_p]
+        L.mp_ctx_hbm_in_use.restype = C.c_uint64
+        L.mp_fastq_index.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_char_p), u64p, i32p,
+                                     u64p, C.POINTER(C.c_int)]
+        L.mp_job_create.argtypes = [C.c_void_p, C.POINTER(C.c_void_p)]
+        L.mp_job_destroy.argtypes = [C.c_void_p]
+        L.mp_job_load_fastq.argtypes = [C.c_void_p, C.c_char_p, C.c_uint64, u64p, C.c_int, C.c_int]
+        L.mp_job_load_fastq_device.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64, u64p, C.c_int, C.c_int]
+        L.mp_job_reset.argtypes = [C.c_void_p]
+        L.mp_job_stream.argtypes = [C.c_void_p]
+        L.mp_job_stream.restype = C.c_void_p
+        L.mp_launch_count.restype = C.c_uint64
+        L.mp_job_num_reads.argtypes = [C.c_void_p]
+        L.mp_job_num_reads.restype = C.c_uint64
+        L.mp_job_count.argtypes = [C.c_void_p, C.c_int, C.c_int, u64p, C.c_int, u64p, u32p, u64p]
+        L.mp_job_partition.argtypes = [C.c_void_p, C.c_void_p, u64p, u64p, C.c_int, u64p, u64p]
+        L.mp_job_labels.argtypes = [C.c_void_p, u32p]
+        L.mp_job_output.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64, u64p, u64p]
+        L.mp_job_set_dump_dir.argtypes = [C.c_void_p, C.c_char_p]
+        L.mp_job_stage_ms.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.c_int]
+        L.mp_job_sort_stats.argtypes = [C.c_void_p, u64p, C.POINTER(C.c_int), C.POINTER(C.c_double), u64p]
+        _lib = L
+    return _lib
+
+
+def _check(rc: int, what: str):
+    if rc != 0:
+        msg = lib().mp_last_error().decode(errors="replace")
+        raise MetapartError(f"{what} failed ({rc}): {msg}")
+
+
+def _p64(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_uint64))
+
+
+class PartParams(C.Structure):
+    _fields_ = [("k", C.c_int), ("min3", C.c_int), ("num_scans", C.c_int), ("num_threads", C.c_int)]
+
+
+class Context:
+    def __init__(self, device: int = 0, hbm_budget: int = 0):
+        self.h = C.c_void_p()
+        _check(lib().mp_ctx_create(device, hbm_budget, C.byref(self.h)), "mp_ctx_create")
+
+    def hbm_in_use(self) -> int:
+        return lib().mp_ctx_hbm_in_use(self.h)
+
+    def close(self):
+        if self.h:
+            lib().mp_ctx_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
+def fastq_index(num_chunks: int, files: list[bytes], interleaved: bool = False):
+    """genFastqIdx: (file_no, offset) of the num_chunks + 1 index records (fewer if files are short)."""
+    n = len(files)
+    arr = (C.c_char_p * n)(*files)
+    sizes = np.array([len(f) for f in files], dtype=np.uint64)
+    fno = np.zeros(num_chunks + 1, dtype=np.int32)
+    ofs = np.zeros(num_chunks + 1, dtype=np.uint64)
+    cnt = C.c_int()
+    nse, nil = (0, n) if interleaved else (n, 0)
+    _check(lib().mp_fastq_index(num_chunks, 0, nse, nil, n, arr, _p64(sizes),
+                                fno.ctypes.data_as(C.POINTER(C.c_int32)), _p64(ofs), C.byref(cnt)), "mp_fastq_index")
+    return fno[:cnt.value].copy(), ofs[:cnt.value].copy()
+
+
+@dataclass
+class CountResult:
+    hist: np.ndarray          # 1048577 exclusive prefix sums (.kmerHist)
+    chunk_reads: np.ndarray   # reads per chunk
+    chunk_counts: np.ndarray | None  # [chunks, 1048576] u32 bucket counts
+
+    @property
+    def chunk_first_read(self) -> np.ndarray:
+        return np.concatenate([[0], np.cumsum(self.chunk_reads)]).astype(np.uint64)
+
+
+class Job:
+    """One partition job: reads resident in HBM and the stage state, on its own CUDA stream."""
+
+    def __init__(self, ctx: Context):
+        self.ctx = ctx
+        self.h = C.c_void_p()
+        _check(lib().mp_job_create(ctx.h, C.byref(self.h)), "mp_job_create")
+
+    def close(self):
+        if self.h:
+            lib().mp_job_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def load(self, data: bytes, file_sizes=None, interleaved: bool = False):
+        fs = np.array(file_sizes if file_sizes is not None else [len(data)], dtype=np.uint64)
+        _check(lib().mp_job_load_fastq(self.h, data, len(data), _p64(fs), len(fs), int(interleaved)), "load")
+
+    def load_device(self, dev_ptr: int, nbytes: int, file_sizes=None, interleaved: bool = False):
+        fs = np.array(file_sizes if file_sizes is not None else [nbytes], dtype=np.uint64)
+        _check(lib().mp_job_load_fastq_device(self.h, C.c_void_p(dev_ptr), nbytes, _p64(fs), len(fs), int(interleaved)),
+               "load_device")
+
+    def load_ptr(self, host_ptr: int, nbytes: int, interleaved: bool = False):
+        """Upload from a host address (pinned memory for full copy bandwidth)."""
+        fs = np.array([nbytes], dtype=np.uint64)
+        _check(lib().mp_job_load_fastq(self.h, C.cast(C.c_void_p(host_ptr), C.c_char_p), nbytes, _p64(fs), 1,
+                                       int(interleaved)), "load")
+
+    def prepare_output(self):
+        """Builds the partition files in device memory; returns (file sizes, total bytes)."""
+        sizes = np.zeros(16 * self.num_threads, dtype=np.uint64)
+        total = C.c_uint64()
+        _check(lib().mp_job_output(self.h, None, 0, _p64(sizes), C.byref(total)), "output")
+        return sizes, total.value
+
+    def output_to(self, host_ptr: int, capacity: int) -> int:
+        """Copies the partition files to a host address; returns the byte count."""
+        total = C.c_uint64()
+        _check(lib().mp_job_output(self.h, C.c_void_p(host_ptr), capacity, None, C.byref(total)), "output")
+        return total.value
+
+    def reset(self):
+        _check(lib().mp_job_reset(self.h), "reset")
+
+    @property
+    def stream(self) -> int:
+        return lib().mp_job_stream(self.h) or 0
+
+    @property
+    def num_reads(self) -> int:
+        return lib().mp_job_num_reads(self.h)
+
+    def set_dump_dir(self, d: str | Path | None):
+        _check(lib().mp_job_set_dump_dir(self.h, str(d).encode() if d else None), "set_dump_dir")
+
+    def count(self, k: int, chunk_starts, min3: bool = False, want_chunk_counts: bool = False) -> CountResult:
+        starts = np.ascontiguousarray(chunk_starts, dtype=np.uint64)
+        nch = len(starts) - 1
+        hist = np.zeros(NB + 1, dtype=np.uint64)
+        reads = np.zeros(nch, dtype=np.uint64)
+        cc = np.zeros((nch, NB), dtype=np.uint32) if want_chunk_counts else None
+        ccp = cc.ctypes.data_as(C.POINTER(C.c_uint32)) if cc is not None else None
+        _check(lib().mp_job_count(self.h, k, int(min3), _p64(starts), nch, _p64(hist), ccp, _p64(reads)), "count")
+        return CountResult(hist, reads, cc)
+
+    def partition(self, k: int, num_scans: int, num_threads: int, chunk_starts, chunk_first_read, hist,
+                  min3: bool = False) -> np.ndarray:
+        p = PartParams(k, int(min3), num_scans, num_threads)
+        starts = np.ascontiguousarray(chunk_starts, dtype=np.uint64)
+        first = np.ascontiguousarray(chunk_first_read, dtype=np.uint64)
+        h = np.ascontiguousarray(hist, dtype=np.uint64)
+        bounds = np.zeros(17, dtype=np.uint64)
+        _check(lib().mp_job_partition(self.h, C.byref(p), _p64(starts), _p64(first), len(starts) - 1, _p64(h),
+                                      _p64(bounds)), "partition")
+        self.num_threads = num_threads
+        return bounds
+
+    def labels(self) -> np.ndarray:
+        out = np.zeros(self.num_reads, dtype=np.uint32)
+        _check(lib().mp_job_labels(self.h, out.ctypes.data_as(C.POINTER(C.c_uint32))), "labels")
+        return out
+
+    def output(self, into: np.ndarray | None = None):
+        """Partition file bytes (file j = partition * T + tid) and their sizes."""
+        nf = 16 * self.num_threads
+        sizes = np.zeros(nf, dtype=np.uint64)
+        total = C.c_uint64()
+        _check(lib().mp_job_output(self.h, None, 0, _p64(sizes), C.byref(total)), "output")
+        buf = into if into is not None else np.empty(max(total.value, 1), dtype=np.uint8)
+        _check(lib().mp_job_output(self.h, buf.ctypes.data_as(C.c_void_p), buf.nbytes, _p64(sizes), C.byref(total)),
+               "output")
+        return buf[:total.value], sizes
+
+    def stage_ms(self) -> dict:
+        a = (C.c_double * 8)()
+        _check(lib().mp_job_stage_ms(self.h, a, 8), "stage_ms")
+        names = ["parse", "count", "enumerate", "sort", "filter", "union_find", "mate_union_plan", "output"]
+        return dict(zip(names, list(a)))
+
+    def sort_stats(self) -> dict:
+        t, b = C.c_uint64(), C.c_uint64()
+        p, ms = C.c_int(), C.c_double()
+        _check(lib().mp_job_sort_stats(self.h, C.byref(t), C.byref(p), C.byref(ms), C.byref(b)), "sort_stats")
+        return {"tuples": t.value, "passes": p.value, "pass_ms": ms.value, "bytes": b.value}
+
+
+def fastq_index_ptr(num_chunks: int, host_ptr: int, nbytes: int, interleaved: bool = False):
+    """genFastqIdx on one FASTQ held at a host address."""
+    arr = (C.c_char_p * 1)(C.cast(C.c_void_p(host_ptr), C.c_char_p))
+    sizes = np.array([nbytes], dtype=np.uint64)
+    fno = np.zeros(num_chunks + 1, dtype=np.int32)
+    ofs = np.zeros(num_chunks + 1, dtype=np.uint64)
+    cnt = C.c_int()
+    nse, nil = (0, 1) if interleaved else (1, 0)
+    _check(lib().mp_fastq_index(num_chunks, 0, nse, nil, 1, arr, _p64(sizes),
+                                fno.ctypes.data_as(C.POINTER(C.c_int32)), _p64(ofs), C.byref(cnt)), "mp_fastq_index")
+    return fno[:cnt.value].copy(), ofs[:cnt.value].copy()
+
+
+def launch_count() -> int:
+    return lib().mp_launch_count()
+
+
+def chunk_starts_of(fno: np.ndarray, ofs: np.ndarray, file_sizes) -> np.ndarray:
+    base = np.concatenate([[0], np.cumsum(np.asarray(file_sizes, dtype=np.uint64))]).astype(np.uint64)
+    return (base[fno.astype(np.int64)] + ofs).astype(np.uint64)
+
+
+def run_pipeline(ctx: Context, fastq: bytes, k: int, num_chunks: int, num_scans: int, num_threads: int,
+                 min3: bool = False, interleaved: bool = False, dump_dir=None):
+    """genFastqIdx -> genHistograms -> metapart on one in-memory FASTQ; returns (job, bounds, count)."""
+    fno, ofs = fastq_index(num_chunks, [fastq], interleaved)
+    starts = chunk_starts_of(fno, ofs, [len(fastq)])
+    job = Job(ctx)
+    if dump_dir:
+        job.set_dump_dir(dump_dir)
+    job.load(fastq, interleaved=interleaved)
+    cnt = job.count(k, starts, min3)
+    bounds = job.partition(k, num_scans, num_threads, starts, cnt.chunk_first_read, cnt.hist, min3)
+    return job, bounds, cnt

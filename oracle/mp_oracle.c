@@ -833,12 +833,17 @@ int mpo_metapart(const char *out_prefix, uint64_t fastq_buffer_size, int k, int 
                 for (uint64_t r = 0; r < cvs[c].nr; r++, rid++) {
                     const unsigned char *sq = (const unsigned char *)cvs[c].buf + cvs[c].r[r].seq;
                     uint64_t id = g_parent ? find_root(rid) : rid;          /* SCAN_OPT :543-568 */
+                    const uint64_t before = per[t].n;
                     int e = min3 ? enum_min3(sq, (int)cvs[c].r[r].len, k, lo, hi, (uint32_t)id, &per[t])
                                  : enum_plain(sq, (int)cvs[c].r[r].len, k, lo, hi, (uint32_t)id, &per[t]);
                     if (e) err = 1;
+                    /* the reference counts a read's tuples in a uint8_t (enumerateKmers.c:152, 212, 343):
+                       256 or more in one scan overlap the next read's */
+                    if (per[t].n - before > 255) err = 2;
                 }
             }
         }
+        if (err == 2) { rc = fail(MPO_EUNSUP, "a read has 256 or more k-mers in one scan"); goto out; }
         if (err) { rc = fail(MPO_ENOMEM, "out of memory enumerating"); goto out; }
         uint64_t n = 0;
         for (int t = 0; t < T; t++) n += per[t].n;

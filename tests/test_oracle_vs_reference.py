@@ -1,0 +1,29 @@
+"""The CPU oracle against the reference programs themselves on fresh seeded inputs (only where the
+reference sources could be built: oracle/_ref exists)."""
+from pathlib import Path
+
+import pytest
+
+import pipeline_util as pu
+from metapart_gb300 import synth
+
+REF = Path(__file__).resolve().parent.parent / "oracle" / "_ref" / "metapart_dump"
+
+CASES = [
+    ("plain_small", 3000, 21, pu.Params(k=23, chunks=8, scans=2, threads=4)),
+    ("plain_large", 4000, 22, pu.Params(k=31, chunks=3, scans=1, threads=3)),
+    ("min3", 2000, 23, pu.Params(k=29, chunks=2, scans=1, threads=1, min3=True)),
+    ("interleaved_small", 3000, 24, pu.Params(k=17, chunks=4, scans=3, threads=2, interleaved=True)),
+]
+
+
+@pytest.mark.parametrize("name,n,seed,p", CASES, ids=[c[0] for c in CASES])
+def test_oracle_equals_reference(tmp_path, built, name, n, seed, p):
+    if not REF.exists():
+        pytest.skip("reference programs not built here")
+    fq = tmp_path / "in.fastq"
+    synth.write_fastq(synth.workload(name, n, seed=seed), fq)
+    a = pu.outputs(pu.run("ref", tmp_path, [fq], p), p, "in.fastq")
+    b = pu.outputs(pu.run("oracle", tmp_path, [fq], p), p, "in.fastq")
+    assert sorted(a) == sorted(b)
+    assert pu.diff_keys(a, b) == []
