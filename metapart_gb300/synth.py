@@ -109,7 +109,8 @@ def fastq_bytes(spec: ReadSpec) -> bytes:
     if rc:
         raise RuntimeError(f"mp_synth_fastq failed: {rc}")
     try:
-        return C.string_at(p, n.value)
+        # ctypes.string_at takes a C int size; copy through an array type for inputs above 2 GiB
+        return bytes(memoryview((C.c_char * n.value).from_address(p.value)))
     finally:
         lib.mp_synth_free(p)
 
