@@ -114,6 +114,14 @@ int mp_job_labels(mp_job *job, uint32_t *out);
  * Replaces writeOutput3 (metapart.c:956-1066).  With out == NULL only file_sizes/total are filled. */
 int mp_job_output(mp_job *job, char *out, uint64_t capacity, uint64_t *file_sizes, uint64_t *total);
 
+/* Stable sort of k-mer tuples by (k-mer, adjacency byte) on the device (onesweep LSD radix sort).
+ * Replaces radixPass and the range-partition + 9-pass driver of sortKmerList (metapart.c:1494-1598,
+ * 1852-2200).  All pointers are device pointers: lo = kmer << 8 | adj, hi = kmer >> 56 (both NULL when
+ * 2k + 8 <= 64), id = read id.  Ties keep input order.  Scratch comes from the context's stream-ordered
+ * pool; the call returns after the sort completed on `stream` (a cudaStream_t, NULL = legacy stream). */
+int mp_sort_tuples(mp_ctx *ctx, const uint64_t *lo_in, const uint8_t *hi_in, const uint32_t *id_in, uint64_t *lo_out,
+                   uint8_t *hi_out, uint32_t *id_out, uint64_t n, void *stream);
+
 /* Optional stage dumps in the reference's formats (the files oracle/ref_hooks.c writes),
  * for parity testing.  NULL disables. */
 int mp_job_set_dump_dir(mp_job *job, const char *dir);

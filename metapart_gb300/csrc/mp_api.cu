@@ -625,6 +625,46 @@ int mp_job_sort_stats(const mp_job *j, uint64_t *tuples, int *passes, double *pa
     return 0;
 }
 
+int mp_sort_tuples(mp_ctx *ctx, const uint64_t *lo_in, const uint8_t *hi_in, const uint32_t *id_in, uint64_t *lo_out,
+                   uint8_t *hi_out, uint32_t *id_out, uint64_t n, void *stream)
+{
+    if (!ctx || !lo_in || !id_in || !lo_out || !id_out) return set_error(MP_EARG, "null argument");
+    if ((hi_in == nullptr) != (hi_out == nullptr)) return set_error(MP_EARG, "hi_in and hi_out must both be given or both NULL");
+    MP_CUDA(cudaSetDevice(ctx->device));
+    cudaStream_t st = (cudaStream_t)stream;
+    DeviceArena arena;
+    arena.st = st;
+    arena.budget_used = &ctx->used;
+    arena.budget_limit = ctx->budget;
+    const bool has_hi = hi_in != nullptr;
+    SortBufs b;
+    b.lo[0] = lo_out;
+    b.id[0] = id_out;
+    b.hi[0] = hi_out;
+    b.lo[1] = arena.alloc<uint64_t>(n + 1);
+    b.id[1] = arena.alloc<uint32_t>(n + 1);
+    b.hi[1] = has_hi ? arena.alloc<uint8_t>(n + 1) : nullptr;
+    if (!b.lo[1] || !b.id[1] || (has_hi && !b.hi[1])) {
+        arena.release_all();
+        return set_error(MP_ENOMEM, "device memory for sorting %llu tuples", (unsigned long long)n);
+    }
+    if (n) {
+        MP_CUDA(cudaMemcpyAsync(lo_out, lo_in, n * 8, cudaMemcpyDeviceToDevice, st));
+        MP_CUDA(cudaMemcpyAsync(id_out, id_in, n * 4, cudaMemcpyDeviceToDevice, st));
+        if (has_hi) MP_CUDA(cudaMemcpyAsync(hi_out, hi_in, n, cudaMemcpyDeviceToDevice, st));
+    }
+    int rc = radix_sort(b, n, has_hi, arena, st, nullptr);
+    if (!rc && b.cur == 1 && n) {
+        cudaMemcpyAsync(lo_out, b.lo[1], n * 8, cudaMemcpyDeviceToDevice, st);
+        cudaMemcpyAsync(id_out, b.id[1], n * 4, cudaMemcpyDeviceToDevice, st);
+        if (has_hi) cudaMemcpyAsync(hi_out, b.hi[1], n, cudaMemcpyDeviceToDevice, st);
+    }
+    arena.release_all();
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (!rc && e != cudaSuccess) rc = set_cuda_error(e, "mp_sort_tuples", __FILE__, __LINE__);
+    return rc;
+}
+
 // ------------------------------------------------------------- chunk index
 
 // genFastqIdx (genFastqIdx.c:142-376) for single-end / interleaved files held in memory.

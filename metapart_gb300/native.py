@@ -57,6 +57,8 @@ def lib():
         L.mp_job_set_dump_dir.argtypes = [C.c_void_p, C.c_char_p]
         L.mp_job_stage_ms.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.c_int]
         L.mp_job_sort_stats.argtypes = [C.c_void_p, u64p, C.POINTER(C.c_int), C.POINTER(C.c_double), u64p]
+        L.mp_sort_tuples.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                     C.c_void_p, C.c_uint64, C.c_void_p]
         _lib = L
     return _lib
 
@@ -243,6 +245,13 @@ def fastq_index_ptr(num_chunks: int, host_ptr: int, nbytes: int, interleaved: bo
     _check(lib().mp_fastq_index(num_chunks, 0, nse, nil, 1, arr, _p64(sizes),
                                 fno.ctypes.data_as(C.POINTER(C.c_int32)), _p64(ofs), C.byref(cnt)), "mp_fastq_index")
     return fno[:cnt.value].copy(), ofs[:cnt.value].copy()
+
+
+def sort_tuples(ctx: Context, lo_in: int, hi_in: int | None, id_in: int, lo_out: int, hi_out: int | None,
+                id_out: int, n: int, stream: int = 0):
+    """mp_sort_tuples on device addresses (e.g. torch tensors' data_ptr())."""
+    _check(lib().mp_sort_tuples(ctx.h, lo_in, hi_in, id_in, lo_out, hi_out, id_out, n, stream or None),
+           "mp_sort_tuples")
 
 
 def launch_count() -> int:
