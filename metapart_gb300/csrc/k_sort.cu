@@ -11,6 +11,7 @@
 // counts, looks back over earlier tiles for its global offsets, reorders the tile in
 // shared memory and writes each digit's run contiguously.
 #include <cstdio>
+#include <mutex>
 #include <vector>
 
 #include "k_sort.cuh"
@@ -280,4 +281,139 @@ int radix_sort(SortBufs &b, uint64_t n, bool has_hi, DeviceArena &arena, cudaStr
     return 0;
 }
 
+// ---------------------------------------------------------------------------
+// Allocation-free sort (mp_sort_tuples_noalloc).
+//
+// For callers that cannot allocate device memory once they are running -- a host that
+// hands this library only pre-allocated buffers from its own allocator, or code that must
+// not allocate inside a latency-critical loop -- the sort's scratch (the second tuple
+// buffer, the look-back status words, the digit histograms) lives in one fixed device
+// array declared here.  Every GPU that loads the library holds it (about 14 MB) until the
+// process exits.  Calls share the array: two calls in flight at the same time on the GPU
+// (different streams, or host threads) race on it and corrupt each other's results.
+constexpr uint64_t NOALLOC_MAX_TUPLES = 1ull << 20;
+constexpr uint64_t NOALLOC_TILES = (NOALLOC_MAX_TUPLES + STILE - 1) / STILE;
+
+struct NoAllocScratch {
+    uint64_t lo[NOALLOC_MAX_TUPLES];
+    uint32_t id[NOALLOC_MAX_TUPLES];
+    uint8_t hi[NOALLOC_MAX_TUPLES];
+    unsigned long long status[NOALLOC_TILES * 256];
+    unsigned long long ghist[9 * 256];
+    uint64_t dbase[9 * 256];
+    uint32_t ctr[16];
+    uint32_t err;
+};
+
+static __device__ __align__(256) NoAllocScratch g_noalloc_scratch;
+
+// Device address of g_noalloc_scratch per device ordinal (host code cannot use the symbol
+// itself: in host code it names a host-side shadow, not device memory).
+static NoAllocScratch *g_noalloc_addr[256];
+static std::mutex g_noalloc_mu;
+
+static int noalloc_scratch(NoAllocScratch **out)
+{
+    int dev = 0;
+    MP_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 256) return set_error(MP_EUNSUP, "device ordinal %d out of range", dev);
+    std::lock_guard<std::mutex> g(g_noalloc_mu);
+    if (!g_noalloc_addr[dev]) {
+        void *p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) return set_cuda_error(e, "cudaGetSymbolAddress(scratch)", __FILE__, __LINE__);
+        g_noalloc_addr[dev] = (NoAllocScratch *)p;
+    }
+    *out = g_noalloc_addr[dev];
+    return 0;
+}
+
+int sort_tuples_noalloc(const uint64_t *lo_in, const uint8_t *hi_in, const uint32_t *id_in, uint64_t *lo_out,
+                        uint8_t *hi_out, uint32_t *id_out, uint64_t n, cudaStream_t st)
+{
+    if (!lo_in || !id_in || !lo_out || !id_out) return set_error(MP_EARG, "null argument");
+    if ((hi_in == nullptr) != (hi_out == nullptr))
+        return set_error(MP_EARG, "hi_in and hi_out must both be given or both NULL");
+    if (n > NOALLOC_MAX_TUPLES)
+        return set_error(MP_EARG, "%llu tuples exceed the fixed scratch of the allocation-free sort (%llu tuples)",
+                         (unsigned long long)n, (unsigned long long)NOALLOC_MAX_TUPLES);
+    NoAllocScratch *S = nullptr;
+    int rc = noalloc_scratch(&S);
+    if (rc) return rc;
+    const bool has_hi = hi_in != nullptr;
+    if (n == 0) return 0;
+    const uint64_t tiles = (n + STILE - 1) / STILE;
+    // the array keeps the previous call's contents: clear what must start at zero
+    MP_CUDA(cudaMemsetAsync(S->ghist, 0, sizeof S->ghist, st));
+    MP_CUDA(cudaMemsetAsync(S->ctr, 0, sizeof S->ctr, st));
+    MP_CUDA(cudaMemsetAsync(&S->err, 0, sizeof S->err, st));
+    MP_CUDA(cudaMemsetAsync(S->status, 0, tiles * 256 * sizeof(unsigned long long), st));
+    (mp::count_launch(), k_hist_upfront<<<152 * 2, 256, 0, st>>>(lo_in, hi_in, n, S->ghist));
+    unsigned long long h[9 * 256];
+    MP_CUDA(cudaMemcpyAsync(h, S->ghist, sizeof h, cudaMemcpyDeviceToHost, st));
+    MP_CUDA(cudaStreamSynchronize(st));
+    int passes[9], np = 0;
+    uint64_t base[9 * 256];
+    for (int dgt = 0; dgt < (has_hi ? 9 : 8); dgt++) {
+        uint64_t acc = 0;
+        bool constant = false;
+        for (int v = 0; v < 256; v++) {
+            base[dgt * 256 + v] = acc;
+            if (h[dgt * 256 + v] == n) constant = true;
+            acc += h[dgt * 256 + v];
+        }
+        if (acc != n) return set_error(MP_EDEVICE, "radix histogram does not add up");
+        if (!constant) passes[np++] = dgt;
+    }
+    if (np == 0) {  // every digit constant: the input is already in order
+        MP_CUDA(cudaMemcpyAsync(lo_out, lo_in, n * 8, cudaMemcpyDeviceToDevice, st));
+        MP_CUDA(cudaMemcpyAsync(id_out, id_in, n * 4, cudaMemcpyDeviceToDevice, st));
+        if (has_hi) MP_CUDA(cudaMemcpyAsync(hi_out, hi_in, n, cudaMemcpyDeviceToDevice, st));
+        MP_CUDA(cudaStreamSynchronize(st));
+        return 0;
+    }
+    MP_CUDA(cudaMemcpyAsync(S->dbase, base, sizeof base, cudaMemcpyHostToDevice, st));
+    static bool attr = false;
+    if (!attr) {
+        MP_CUDA(cudaFuncSetAttribute(k_onesweep<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SortSmem)));
+        MP_CUDA(cudaFuncSetAttribute(k_onesweep<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SortSmem)));
+        attr = true;
+    }
+    // pass i writes the caller's output when (np - 1 - i) is even, the scratch otherwise,
+    // so the last pass always lands in the output
+    const uint64_t *src_lo = lo_in;
+    const uint8_t *src_hi = hi_in;
+    const uint32_t *src_id = id_in;
+    for (int i = 0; i < np; i++) {
+        const bool to_out = ((np - 1 - i) & 1) == 0;
+        uint64_t *d_lo = to_out ? lo_out : S->lo;
+        uint32_t *d_id = to_out ? id_out : S->id;
+        uint8_t *d_hi = has_hi ? (to_out ? hi_out : S->hi) : nullptr;
+        const int dgt = passes[i];
+        if (dgt < 8)
+            (mp::count_launch(), k_onesweep<0><<<(unsigned)tiles, ST, sizeof(SortSmem), st>>>(
+                src_lo, src_hi, src_id, d_lo, d_hi, d_id, n, 8 * dgt, S->dbase + dgt * 256, S->status, S->ctr + i,
+                (uint32_t)(i + 1), &S->err));
+        else
+            (mp::count_launch(), k_onesweep<1><<<(unsigned)tiles, ST, sizeof(SortSmem), st>>>(
+                src_lo, src_hi, src_id, d_lo, d_hi, d_id, n, 0, S->dbase + dgt * 256, S->status, S->ctr + i,
+                (uint32_t)(i + 1), &S->err));
+        src_lo = d_lo;
+        src_hi = d_hi;
+        src_id = d_id;
+    }
+    uint32_t herr = 0;
+    MP_CUDA(cudaMemcpyAsync(&herr, &S->err, sizeof herr, cudaMemcpyDeviceToHost, st));
+    MP_CUDA(cudaStreamSynchronize(st));
+    MP_CUDA(cudaGetLastError());
+    if (herr) return set_error(MP_EDEVICE, "radix sort look-back gave up (device error flags 0x%x)", herr);
+    return 0;
+}
+
 }  // namespace mp
+
+extern "C" int mp_sort_tuples_noalloc(const uint64_t *lo_in, const uint8_t *hi_in, const uint32_t *id_in,
+                                      uint64_t *lo_out, uint8_t *hi_out, uint32_t *id_out, uint64_t n, void *stream)
+{
+    return mp::sort_tuples_noalloc(lo_in, hi_in, id_in, lo_out, hi_out, id_out, n, (cudaStream_t)stream);
+}
