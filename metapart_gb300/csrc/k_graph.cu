@@ -11,41 +11,16 @@
 
 namespace mp {
 
-constexpr int LONG_RUN = 256;    // runs longer than this go to the block-per-run kernels
+constexpr int SEG = 1024;          // tuples owned by one warp in the run kernels
 constexpr uint32_t UF_CAP = 1u << 20;
+constexpr unsigned FULLW = 0xFFFFFFFFu;
 
 __device__ __forceinline__ uint64_t kmer_of(const uint64_t *lo, const uint8_t *hi, uint64_t i)
 {
     return (lo[i] >> 8) | (hi ? ((uint64_t)hi[i] << 56) : 0ull);
 }
 
-// ----------------------------------------------------------------- runs
-
-__global__ void k_run_heads(const uint64_t *lo, const uint8_t *hi, uint64_t n, uint32_t *heads)
-{
-    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const bool h = i < n && (i == 0 || kmer_of(lo, hi, i) != kmer_of(lo, hi, i - 1));
-    const uint32_t b = __ballot_sync(0xFFFFFFFFu, h);
-    if ((threadIdx.x & 31) == 0 && i < n + 31) heads[i >> 5] = b;
-}
-
-// end of the run starting at s: the next head after s (or n)
-__device__ __forceinline__ uint64_t run_end(const uint32_t *heads, uint64_t n, uint64_t s)
-{
-    uint64_t i = s + 1;
-    if (i >= n) return n;
-    uint64_t w = i >> 5;
-    uint32_t m = heads[w] & (0xFFFFFFFFu << (i & 31));
-    const uint64_t nw = (n + 31) >> 5;
-    while (!m) {
-        if (++w >= nw) return n;
-        m = heads[w];
-    }
-    const uint64_t e = (w << 5) + (uint64_t)(__ffs(m) - 1);
-    return e < n ? e : n;
-}
-
-__device__ __forceinline__ bool is_head(const uint32_t *heads, uint64_t i) { return (heads[i >> 5] >> (i & 31)) & 1u; }
+__device__ __forceinline__ bool zbit(const uint32_t *z, uint64_t i) { return (z[i >> 5] >> (i & 31)) & 1u; }
 
 // e is a thread-range end (the reference never judges the last run of a range, metapart.c:2289-2467)
 __device__ __forceinline__ bool at_range_end(const uint64_t *ends, int T, uint64_t e)
@@ -59,104 +34,179 @@ __device__ __forceinline__ bool at_range_end(const uint64_t *ends, int T, uint64
     return false;
 }
 
+// lanes [s, e) of a window (s <= 31, e <= 32)
+__device__ __forceinline__ uint32_t lane_range(int s, int e)
+{
+    const uint32_t hi = e >= 32 ? FULLW : ((1u << e) - 1);
+    return hi & ~((1u << s) - 1);
+}
+
 // --------------------------------------------------------------- K4 filter
 
-struct Judge {
-    int nin, nout, mxi, mxo;
-    bool zero, ratio_bad;
-};
+// Decision of markMischiefKmers for one run (metapart.c:2296-2451), packed:
+// bit 0 branching (numIn > 1 or numOut > 1), 1 numIn > 1, 2 numOut > 1, 3-5 max in index,
+// 6-8 max out index, 9 zero the k-mer (both sides branch), 10 second-max ratio above 0.2.
+constexpr uint32_t J_ANY = 1, J_NIN = 2, J_NOUT = 4, J_ZERO = 1u << 9, J_RATIO = 1u << 10;
 
-// markMischiefKmers decision for one run (metapart.c:2296-2451)
-__device__ __forceinline__ Judge judge_run(const uint32_t *before, const uint32_t *after, uint32_t deg)
+// The reference's test (float)s / deg > 0.2, the float quotient compared as a double
+// (metapart.c:2346-2349).  The smallest float above 0.2 is 0.2f = 13421773 * 2^-26, and a
+// quotient rounds to at least that iff it exceeds the midpoint 26843545 * 2^-27 (a tie
+// rounds to the even neighbour below), so for s, deg exact in float (<= 2^24) the test is
+// s * 2^27 > 26843545 * deg in integers -- no FP64, which is slow on this GPU.
+__device__ __forceinline__ bool ratio_above_02(uint32_t s, uint32_t deg)
 {
-    Judge j{0, 0, 0, 0, false, false};
+    if (deg <= (1u << 24)) return ((uint64_t)s << 27) > 26843545ull * deg;
+    return (double)__fdiv_rn((float)s, (float)deg) > 0.2;
+}
+
+__device__ __forceinline__ uint32_t judge_run(const uint32_t *before, const uint32_t *after, uint32_t deg)
+{
+    int nin = 0, nout = 0, mxi = 0, mxo = 0;
     uint32_t cmi = 0, cmo = 0, smi = 0, smo = 0;
+#pragma unroll
     for (int q = 0; q < 7; q++) {
         if (before[q]) {
-            if (before[q] > cmi) { smi = cmi; cmi = before[q]; j.mxi = q; }
+            if (before[q] > cmi) { smi = cmi; cmi = before[q]; mxi = q; }
             else if (before[q] > smi) smi = before[q];
-            j.nin++;
+            nin++;
         }
         if (after[q]) {
-            if (after[q] > cmo) { smo = cmo; cmo = after[q]; j.mxo = q; }
+            if (after[q] > cmo) { smo = cmo; cmo = after[q]; mxo = q; }
             else if (after[q] > smo) smo = after[q];
-            j.nout++;
+            nout++;
         }
     }
-    j.zero = j.nin > 1 && j.nout > 1;
-    // (float)count / degree compared with 0.2 as double, as the reference does
-    const float r_in = __fdiv_rn((float)smi, (float)deg), r_out = __fdiv_rn((float)smo, (float)deg);
-    j.ratio_bad = ((double)r_in > 0.2) || ((double)r_out > 0.2);
-    return j;
+    if (nin <= 1 && nout <= 1) return 0;
+    uint32_t J = J_ANY | (nin > 1 ? J_NIN : 0) | (nout > 1 ? J_NOUT : 0) | ((uint32_t)mxi << 3) | ((uint32_t)mxo << 6);
+    if (nin > 1 && nout > 1) J |= J_ZERO;
+    if (ratio_above_02(smi, deg) || ratio_above_02(smo, deg)) J |= J_RATIO;
+    return J;
 }
 
-__device__ __forceinline__ void apply_marks(const Judge &jd, uint64_t s, uint64_t e, uint64_t *lo, uint8_t *hi,
-                                            const uint32_t *id, uint32_t *parent, uint8_t *filtered)
+// Marks of one tuple of a judged run: the zero flag goes to the z bitmask (the tuple array
+// stays read-only while other warps detect run heads), BAD to the read.
+__device__ __forceinline__ void mark_tuple(uint32_t J, uint64_t q, uint32_t adj, const uint32_t *id, uint32_t *parent,
+                                           uint8_t *filtered, uint32_t *z)
 {
-    for (uint64_t q = s; q < e; q++) {
-        const uint32_t adj = (uint32_t)(lo[q] & 0xFF);
-        if (jd.zero) {
-            lo[q] = adj;
-            if (hi) hi[q] = 0;
-            continue;
-        }
-        const uint32_t bi = adj & 7, ai = (adj >> 3) & 7;
-        bool bad = (jd.nin > 1 && bi != (uint32_t)jd.mxi) || (jd.nout > 1 && ai != (uint32_t)jd.mxo);
-        if (!bad) bad = jd.ratio_bad;
-        if (bad) {
-            const uint32_t r = id[q];
-            parent[r] = BAD;
-            filtered[r] = 1;
-        }
-    }
-}
-
-__global__ void k_filter(uint64_t *lo, uint8_t *hi, const uint32_t *id, uint64_t n, const uint32_t *heads,
-                         const uint64_t *range_ends, int T, uint32_t *parent, uint8_t *filtered, uint64_t *long_runs,
-                         unsigned long long *n_long)
-{
-    const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= n || !is_head(heads, s)) return;
-    const uint64_t e = run_end(heads, n, s);
-    if (at_range_end(range_ends, T, e)) return;
-    if (e - s > (uint64_t)LONG_RUN) {
-        long_runs[atomicAdd(n_long, 1ull)] = s;
+    if (!(J & J_ANY)) return;
+    if (J & J_ZERO) {
+        atomicOr(&z[q >> 5], 1u << (q & 31));
         return;
     }
-    uint32_t before[8] = {0}, after[8] = {0};
-    for (uint64_t q = s; q < e; q++) {
-        const uint32_t adj = (uint32_t)(lo[q] & 0xFF);
-        before[adj & 7]++;
-        after[(adj >> 3) & 7]++;
+    const uint32_t bi = adj & 7, ai = (adj >> 3) & 7;
+    bool bad = ((J & J_NIN) && bi != ((J >> 3) & 7)) || ((J & J_NOUT) && ai != ((J >> 6) & 7));
+    if (!bad) bad = (J & J_RATIO) != 0;
+    if (bad) {
+        const uint32_t r = id[q];
+        parent[r] = BAD;
+        filtered[r] = 1;
     }
-    const Judge jd = judge_run(before, after, (uint32_t)(e - s));
-    if (jd.nin > 1 || jd.nout > 1) apply_marks(jd, s, e, lo, hi, id, parent, filtered);
 }
 
-__global__ void k_filter_long(uint64_t *lo, uint8_t *hi, const uint32_t *id, uint64_t n, const uint32_t *heads,
-                              const uint64_t *long_runs, uint32_t *parent, uint8_t *filtered)
+// One warp per SEG tuples: the runs whose first tuple lies in the warp's segment.  In each
+// window of 32 tuples a lane finds whether its tuple starts a run (one shuffle), and 14
+// ballots give every run its before/after adjacency-code counts by popcount.  A run still
+// open at the end of a window is carried (its counts held by every lane); when a run spans
+// windows its marks are applied by one more pass over it after it is judged.
+__global__ void __launch_bounds__(256) k_filter_warp(const uint64_t *lo, const uint8_t *hi, const uint32_t *id,
+                                                     uint64_t n, const uint64_t *range_ends, int T, uint32_t *parent,
+                                                     uint8_t *filtered, uint32_t *z)
 {
-    __shared__ uint32_t cnt[16];
-    __shared__ Judge jd;
-    const uint64_t s = long_runs[blockIdx.x];
-    const uint64_t e = run_end(heads, n, s);
-    if (threadIdx.x < 16) cnt[threadIdx.x] = 0;
+    __shared__ uint64_t ends[256];
+    for (int t = threadIdx.x; t < T; t += blockDim.x) ends[t] = range_ends[t];
     __syncthreads();
-    uint32_t b[8] = {0}, a[8] = {0};
-    for (uint64_t q = s + threadIdx.x; q < e; q += blockDim.x) {
-        const uint32_t adj = (uint32_t)(lo[q] & 0xFF);
-        b[adj & 7]++;
-        a[(adj >> 3) & 7]++;
+    const int lane = threadIdx.x & 31;
+    const uint64_t c0 = (((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * SEG;
+    if (c0 >= n) return;
+    const uint64_t c1 = min(n, c0 + SEG);
+    const uint32_t le = (lane == 31) ? FULLW : ((2u << lane) - 1);  // lanes <= lane
+    bool open = false;
+    uint64_t rs = 0;
+    uint32_t cb[7], ca[7], deg = 0;
+#pragma unroll
+    for (int c = 0; c < 7; c++) cb[c] = ca[c] = 0;
+    uint64_t prev_km = c0 ? kmer_of(lo, hi, c0 - 1) : 0;
+    uint64_t nlv = c0 + lane < n ? lo[c0 + lane] : 0;  // next window's words, loaded one window ahead
+    uint8_t nhv = (hi && c0 + lane < n) ? hi[c0 + lane] : 0;
+    for (uint64_t p = c0;; p += 32) {
+        const bool owned = p < c1;
+        if (!owned && !open) break;
+        const uint64_t i = p + lane;
+        const bool valid = i < n;
+        const uint64_t lv = nlv;
+        const uint64_t km = valid ? ((lv >> 8) | ((uint64_t)nhv << 56)) : 0;
+        if (i + 32 < n) {
+            nlv = lo[i + 32];
+            if (hi) nhv = hi[i + 32];
+        }
+        uint64_t pk = __shfl_up_sync(FULLW, km, 1);
+        if (lane == 0) pk = prev_km;
+        const bool head = valid && (i == 0 || km != pk);
+        const uint32_t H = __ballot_sync(FULLW, head), V = __ballot_sync(FULLW, valid);
+        prev_km = __shfl_sync(FULLW, km, 31);
+        const uint32_t adj = (uint32_t)(lv & 0xFF);
+        uint32_t Bm[7], Am[7];
+#pragma unroll
+        for (int c = 0; c < 7; c++) {
+            Bm[c] = __ballot_sync(FULLW, valid && (adj & 7) == (uint32_t)c);
+            Am[c] = __ballot_sync(FULLW, valid && ((adj >> 3) & 7) == (uint32_t)c);
+        }
+        const int fh = H ? __ffs(H) - 1 : 32;
+        const bool arr_end = p + 32 >= n;
+        // the run carried into this window occupies lanes [0, fh)
+        if (open) {
+            const uint32_t m = lane_range(0, fh) & V;
+#pragma unroll
+            for (int c = 0; c < 7; c++) { cb[c] += __popc(Bm[c] & m); ca[c] += __popc(Am[c] & m); }
+            deg += __popc(m);
+            if (fh < 32 || arr_end) {
+                const uint64_t re = fh < 32 ? p + fh : n;
+                open = false;
+                if (!at_range_end(ends, T, re)) {
+                    const uint32_t J = judge_run(cb, ca, deg);
+                    if (J & J_ANY)
+                        for (uint64_t q = rs + lane; q < re; q += 32) mark_tuple(J, q, (uint32_t)(lo[q] & 0xFF), id, parent, filtered, z);
+                }
+            }
+        }
+        if (!owned) continue;
+        // runs that start in this window
+        uint32_t J = 0;
+        int s = -1;
+        if (H & le) s = 31 - __clz(H & le);
+        const uint32_t later = H & ~le;
+        const int nh = later ? __ffs(later) - 1 : 32;
+        if (head && (nh < 32 || arr_end)) {
+            const uint32_t m = lane_range(lane, nh) & V;
+            uint32_t b[7], a[7];
+#pragma unroll
+            for (int c = 0; c < 7; c++) { b[c] = __popc(Bm[c] & m); a[c] = __popc(Am[c] & m); }
+            const uint64_t re = nh < 32 ? p + nh : n;
+            if (!at_range_end(ends, T, re)) J = judge_run(b, a, __popc(m));
+        }
+        const uint32_t Js = __shfl_sync(FULLW, J, s < 0 ? 0 : s);
+        if (s >= 0 && valid) mark_tuple(Js, i, adj, id, parent, filtered, z);  // J == 0 for the still-open run
+        // the last run of the window stays open when the array continues past it
+        const int lh = H ? 31 - __clz(H) : -1;
+        if (lh >= 0 && !arr_end) {
+            const uint32_t m = lane_range(lh, 32) & V;
+#pragma unroll
+            for (int c = 0; c < 7; c++) { cb[c] = __popc(Bm[c] & m); ca[c] = __popc(Am[c] & m); }
+            deg = __popc(m);
+            rs = p + lh;
+            open = true;
+        }
     }
-    for (int x = 0; x < 8; x++) {
-        if (b[x]) atomicAdd(&cnt[x], b[x]);
-        if (a[x]) atomicAdd(&cnt[8 + x], a[x]);
+}
+
+// Applies the zero marks to the tuples (lo = adj, hi = 0): only for stage dumps.
+__global__ void k_apply_zero(uint64_t *lo, uint8_t *hi, uint64_t n, const uint32_t *z)
+{
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n && zbit(z, i)) {
+        lo[i] &= 0xFF;
+        if (hi) hi[i] = 0;
     }
-    __syncthreads();
-    if (threadIdx.x == 0) jd = judge_run(cnt, cnt + 8, (uint32_t)(e - s));
-    __syncthreads();
-    if (!(jd.nin > 1 || jd.nout > 1)) return;
-    for (uint64_t q = s + threadIdx.x; q < e; q += blockDim.x) apply_marks(jd, q, q + 1, lo, hi, id, parent, filtered);
 }
 
 // ---------------------------------------------------------- union-find
@@ -185,15 +235,15 @@ __device__ __forceinline__ void uf_union(uint32_t *parent, uint32_t a, uint32_t 
     atomicOr(err, DERR_SPIN);
 }
 
-// First tuple of each thread range whose k-mer is non-zero and whose read is not BAD.
-__global__ void k_range_first_valid(const uint64_t *lo, const uint8_t *hi, const uint32_t *id, const uint64_t *range_bounds,
-                                    int T, const uint32_t *parent, uint64_t *first)
+// First tuple of each thread range whose k-mer is not zero (nor zero-marked) and whose read is not BAD.
+__global__ void k_range_first_valid(const uint64_t *lo, const uint8_t *hi, const uint32_t *id, const uint32_t *z,
+                                    const uint64_t *range_bounds, int T, const uint32_t *parent, uint64_t *first)
 {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= T) return;
     uint64_t f = ~0ull;
     for (uint64_t q = range_bounds[t]; q < range_bounds[t + 1]; q++)
-        if (kmer_of(lo, hi, q) != 0 && parent[id[q]] != BAD) { f = q; break; }
+        if (!zbit(z, q) && kmer_of(lo, hi, q) != 0 && parent[id[q]] != BAD) { f = q; break; }
     first[t] = f;
 }
 
@@ -201,87 +251,102 @@ struct EdgeCtx {
     const uint64_t *lo;
     const uint8_t *hi;
     const uint32_t *id;
+    const uint32_t *z;             // zero marks of the filter
     uint64_t n;
-    const uint32_t *heads;
     const uint64_t *first_valid;   // per thread range
     const uint64_t *range_bounds;  // T + 1 tuple bounds
     int T;
-    uint64_t init_kmer;            // k-mer of the scan's last tuple (metapart.c:2541)
+    uint64_t init_kmer;            // k-mer of the scan's last tuple after the filter (metapart.c:2541)
     uint32_t init_min;             // read id of the scan's first tuple (metapart.c:2543-2545)
+    uint32_t init_min_ok;          // that read is not BAD
     uint32_t *parent;
     uint32_t *err;
 };
 
-// Anchor of a run: the first valid tuple's read, or -- for the first valid run of a thread
-// range whose k-mer equals the scan's last k-mer -- the first tuple's read (the reference
-// starts every range with that state, metapart.c:2539-2548).  Returns false when the run
-// yields no edges.
-__device__ __forceinline__ bool run_anchor(const EdgeCtx &c, uint64_t s, uint64_t e, uint64_t &first, uint32_t &anchor,
-                                           bool &quirk)
+// unionFindPar2 (metapart.c:2537-2727): in each run of equal k-mers the first valid tuple
+// (k-mer not zero, read not BAD) is the anchor and every later valid tuple is united with it.
+// For the first valid run of a thread range whose k-mer equals the scan's last k-mer, the
+// anchor is the scan's first read (the sweep's initial state, :2539-2548).  One warp per
+// SEG tuples, windows of 32 as in the filter; the anchor of a run still open at the end of a
+// window is carried.
+__global__ void __launch_bounds__(256) k_edges_warp(EdgeCtx c)
 {
-    const uint64_t km = kmer_of(c.lo, c.hi, s);
-    if (km == 0) return false;
-    uint64_t f = e;
-    for (uint64_t q = s; q < e; q++)
-        if (c.parent[c.id[q]] != BAD) { f = q; break; }
-    if (f == e) return false;
-    first = f;
-    anchor = c.id[f];
-    quirk = false;
-    if (km == c.init_kmer) {
-        int lo = 0, hi = c.T - 1;  // thread range containing s
-        while (lo < hi) {
-            int m = (lo + hi + 1) >> 1;
-            if (c.range_bounds[m] <= s) lo = m; else hi = m - 1;
+    const int lane = threadIdx.x & 31;
+    const uint64_t c0 = (((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * SEG;
+    if (c0 >= c.n) return;
+    const uint64_t c1 = min(c.n, c0 + SEG);
+    const uint32_t le = (lane == 31) ? FULLW : ((2u << lane) - 1);
+    bool open = false, has_anchor = false;
+    uint32_t anchor = 0;
+    uint64_t prev_km = c0 ? kmer_of(c.lo, c.hi, c0 - 1) : 0;
+    for (uint64_t p = c0;; p += 32) {
+        const bool owned = p < c1;
+        if (!owned && !open) break;
+        const uint64_t i = p + lane;
+        const bool valid = i < c.n;
+        const uint64_t km = valid ? kmer_of(c.lo, c.hi, i) : 0;
+        uint64_t pk = __shfl_up_sync(FULLW, km, 1);
+        if (lane == 0) pk = prev_km;
+        const bool head = valid && (i == 0 || km != pk);
+        const uint32_t H = __ballot_sync(FULLW, head);
+        prev_km = __shfl_sync(FULLW, km, 31);
+        const bool nz = valid && km != 0 && !zbit(c.z, i);
+        const uint32_t r = nz ? c.id[i] : 0;
+        const bool good = nz && c.parent[r] != BAD;
+        const uint32_t G = __ballot_sync(FULLW, good);
+        const int fh = H ? __ffs(H) - 1 : 32;
+        const bool arr_end = p + 32 >= c.n;
+        // anchor candidate of each lane's run in this window: first good lane of the run's lanes here
+        int s = -1;
+        if (H & le) s = 31 - __clz(H & le);
+        const bool carried = s < 0;
+        const uint32_t later = H & ~le;
+        const int nh = later ? __ffs(later) - 1 : 32;
+        const uint32_t runm = carried ? lane_range(0, fh) : lane_range(s, nh);
+        const uint32_t gm = G & runm;
+        const int fg = gm ? __ffs(gm) - 1 : -1;
+        // quirk check by the lane holding a run's first good tuple when the run has no anchor yet
+        uint32_t aval = r;
+        bool quirk = false;
+        if (good && lane == fg && !(carried && has_anchor) && km == c.init_kmer && c.init_min_ok) {
+            int lo = 0, hi = c.T - 1;
+            while (lo < hi) {
+                int m = (lo + hi + 1) >> 1;
+                if (c.range_bounds[m] <= i) lo = m; else hi = m - 1;
+            }
+            if (c.first_valid[lo] == i) { quirk = true; aval = c.init_min; }
         }
-        if (c.first_valid[lo] == f && c.parent[c.init_min] != BAD) {
-            anchor = c.init_min;
-            quirk = true;
+        const uint32_t av = __shfl_sync(FULLW, aval, fg < 0 ? 0 : fg);
+        const bool qk = __shfl_sync(FULLW, quirk, fg < 0 ? 0 : fg);
+        bool do_union = false;
+        uint32_t target = 0;
+        if (good) {
+            if (carried) {
+                if (open) {
+                    if (has_anchor) { do_union = true; target = anchor; }
+                    else if (lane != fg || qk) { do_union = true; target = av; }
+                }
+            } else if (owned) {
+                if (lane != fg || qk) { do_union = true; target = av; }
+            }
         }
-    }
-    return true;
-}
-
-__global__ void k_edges(EdgeCtx c, uint64_t *long_runs, unsigned long long *n_long)
-{
-    const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= c.n || !is_head(c.heads, s)) return;
-    const uint64_t e = run_end(c.heads, c.n, s);
-    if (e - s > (uint64_t)LONG_RUN) {
-        long_runs[atomicAdd(n_long, 1ull)] = s;
-        return;
-    }
-    uint64_t f;
-    uint32_t anchor;
-    bool quirk;
-    if (!run_anchor(c, s, e, f, anchor, quirk)) return;
-    for (uint64_t q = quirk ? f : f + 1; q < e; q++) {
-        const uint32_t r = c.id[q];
-        if (r == anchor || c.parent[r] == BAD) continue;
-        uf_union(c.parent, anchor, r, c.err);
-    }
-}
-
-__global__ void k_edges_long(EdgeCtx c, const uint64_t *long_runs)
-{
-    __shared__ uint64_t sf;
-    __shared__ uint32_t sa;
-    __shared__ int sq, ok;
-    const uint64_t s = long_runs[blockIdx.x];
-    const uint64_t e = run_end(c.heads, c.n, s);
-    if (threadIdx.x == 0) {
-        uint64_t f;
-        uint32_t a;
-        bool q;
-        ok = run_anchor(c, s, e, f, a, q);
-        sf = f; sa = a; sq = q;
-    }
-    __syncthreads();
-    if (!ok) return;
-    for (uint64_t q = (sq ? sf : sf + 1) + threadIdx.x; q < e; q += blockDim.x) {
-        const uint32_t r = c.id[q];
-        if (r == sa || c.parent[r] == BAD) continue;
-        uf_union(c.parent, sa, r, c.err);
+        if (do_union && target != r) uf_union(c.parent, target, r, c.err);
+        // carried run bookkeeping
+        if (open) {
+            if (!has_anchor) {
+                const uint32_t g0 = G & lane_range(0, fh);
+                if (g0) { has_anchor = true; anchor = __shfl_sync(FULLW, aval, __ffs(g0) - 1); }
+            }
+            if (fh < 32 || arr_end) open = false;
+        }
+        if (!owned) continue;
+        const int lh = H ? 31 - __clz(H) : -1;
+        if (lh >= 0 && !arr_end) {
+            const uint32_t g = G & lane_range(lh, 32);
+            has_anchor = g != 0;
+            anchor = has_anchor ? __shfl_sync(FULLW, aval, __ffs(g) - 1) : 0;
+            open = true;
+        }
     }
 }
 
@@ -417,25 +482,20 @@ __global__ void k_pe_bigsmall(uint32_t *parent, uint32_t *size, const uint32_t *
 static unsigned blocks_for(uint64_t n, int t) { return (unsigned)((n + t - 1) / t); }
 
 int filter_scan(Tuples &tp, const std::vector<uint64_t> &range_bounds, uint32_t *parent, uint8_t *filtered,
-                DeviceArena &arena, cudaStream_t st)
+                DeviceArena &arena, cudaStream_t st, bool apply_zero)
 {
     const uint64_t n = tp.n;
-    if (n == 0) return 0;
     const int T = (int)range_bounds.size() - 1;
-    tp.heads = arena.alloc<uint32_t>((n + 31) / 32 + 1);
+    tp.z = arena.alloc<uint32_t>((n + 31) / 32 + 1);
     uint64_t *ends = arena.alloc<uint64_t>(T);
-    uint64_t *long_runs = arena.alloc<uint64_t>(n / LONG_RUN + 2);
-    unsigned long long *nlong = arena.alloc<unsigned long long>(1);
-    if (!tp.heads || !ends || !long_runs || !nlong) return set_error(MP_ENOMEM, "device memory for the filter");
+    if (!tp.z || !ends) return set_error(MP_ENOMEM, "device memory for the filter");
+    MP_CUDA(cudaMemsetAsync(tp.z, 0, ((n + 31) / 32 + 1) * sizeof(uint32_t), st));
+    if (n == 0) return 0;
     MP_CUDA(cudaMemcpyAsync(ends, range_bounds.data() + 1, T * sizeof(uint64_t), cudaMemcpyHostToDevice, st));
-    MP_CUDA(cudaMemsetAsync(nlong, 0, sizeof *nlong, st));
-    (mp::count_launch(), k_run_heads<<<blocks_for(n, 256), 256, 0, st>>>(tp.lo, tp.hi, n, tp.heads));
-    (mp::count_launch(), k_filter<<<blocks_for(n, 256), 256, 0, st>>>(tp.lo, tp.hi, tp.id, n, tp.heads, ends, T, parent, filtered,
-                                                 long_runs, nlong));
-    unsigned long long hl = 0;
-    MP_CUDA(cudaMemcpyAsync(&hl, nlong, sizeof hl, cudaMemcpyDeviceToHost, st));
-    MP_CUDA(cudaStreamSynchronize(st));
-    if (hl) (mp::count_launch(), k_filter_long<<<(unsigned)hl, 256, 0, st>>>(tp.lo, tp.hi, tp.id, n, tp.heads, long_runs, parent, filtered));
+    const uint64_t warps = (n + SEG - 1) / SEG;
+    (mp::count_launch(), k_filter_warp<<<blocks_for(warps * 32, 256), 256, 0, st>>>(tp.lo, tp.hi, tp.id, n, ends, T, parent,
+                                                                                   filtered, tp.z));
+    if (apply_zero) (mp::count_launch(), k_apply_zero<<<blocks_for(n, 256), 256, 0, st>>>(tp.lo, tp.hi, n, tp.z));
     MP_CUDA(cudaGetLastError());
     return 0;
 }
@@ -450,31 +510,30 @@ int union_scan(Tuples &tp, const std::vector<uint64_t> &range_bounds, uint32_t *
     MP_CUDA(cudaMemsetAsync(err, 0, sizeof *err, st));
     if (n) {
         uint64_t *bounds = arena.alloc<uint64_t>(T + 1), *first = arena.alloc<uint64_t>(T);
-        uint64_t *long_runs = arena.alloc<uint64_t>(n / LONG_RUN + 2);
-        unsigned long long *nlong = arena.alloc<unsigned long long>(1);
-        if (!bounds || !first || !long_runs || !nlong) return set_error(MP_ENOMEM, "device memory for union-find");
+        if (!bounds || !first) return set_error(MP_ENOMEM, "device memory for union-find");
         MP_CUDA(cudaMemcpyAsync(bounds, range_bounds.data(), (T + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, st));
-        MP_CUDA(cudaMemsetAsync(nlong, 0, sizeof *nlong, st));
-        EdgeCtx c;
-        c.lo = tp.lo; c.hi = tp.hi; c.id = tp.id; c.n = n; c.heads = tp.heads;
-        c.first_valid = first; c.range_bounds = bounds; c.T = T; c.parent = parent; c.err = err;
-        // initial state of every range sweep: last tuple's k-mer, first tuple's read (post filter)
-        uint64_t last_lo = 0, id0 = 0;
+        // initial state of every range sweep: the last tuple's k-mer after the filter, the first tuple's read
+        uint64_t last_lo = 0;
         uint8_t last_hi = 0;
-        uint32_t first_id = 0;
+        uint32_t zw = 0, first_id = 0;
         MP_CUDA(cudaMemcpyAsync(&last_lo, tp.lo + (n - 1), 8, cudaMemcpyDeviceToHost, st));
         if (tp.hi) MP_CUDA(cudaMemcpyAsync(&last_hi, tp.hi + (n - 1), 1, cudaMemcpyDeviceToHost, st));
+        MP_CUDA(cudaMemcpyAsync(&zw, tp.z + ((n - 1) >> 5), 4, cudaMemcpyDeviceToHost, st));
         MP_CUDA(cudaMemcpyAsync(&first_id, tp.id, 4, cudaMemcpyDeviceToHost, st));
         MP_CUDA(cudaStreamSynchronize(st));
-        (void)id0;
-        c.init_kmer = (last_lo >> 8) | ((uint64_t)last_hi << 56);
-        c.init_min = first_id;
-        (mp::count_launch(), k_range_first_valid<<<blocks_for(T, 64), 64, 0, st>>>(tp.lo, tp.hi, tp.id, bounds, T, parent, first));
-        (mp::count_launch(), k_edges<<<blocks_for(n, 256), 256, 0, st>>>(c, long_runs, nlong));
-        unsigned long long hl = 0;
-        MP_CUDA(cudaMemcpyAsync(&hl, nlong, sizeof hl, cudaMemcpyDeviceToHost, st));
+        uint32_t first_parent = 0;
+        MP_CUDA(cudaMemcpyAsync(&first_parent, parent + first_id, 4, cudaMemcpyDeviceToHost, st));
         MP_CUDA(cudaStreamSynchronize(st));
-        if (hl) (mp::count_launch(), k_edges_long<<<(unsigned)hl, 256, 0, st>>>(c, long_runs));
+        EdgeCtx c;
+        c.lo = tp.lo; c.hi = tp.hi; c.id = tp.id; c.z = tp.z; c.n = n;
+        c.first_valid = first; c.range_bounds = bounds; c.T = T; c.parent = parent; c.err = err;
+        c.init_kmer = ((zw >> ((n - 1) & 31)) & 1u) ? 0 : ((last_lo >> 8) | ((uint64_t)last_hi << 56));
+        c.init_min = first_id;
+        c.init_min_ok = first_parent != BAD;
+        (mp::count_launch(), k_range_first_valid<<<blocks_for(T, 64), 64, 0, st>>>(tp.lo, tp.hi, tp.id, tp.z, bounds, T, parent,
+                                                                                  first));
+        const uint64_t warps = (n + SEG - 1) / SEG;
+        (mp::count_launch(), k_edges_warp<<<blocks_for(warps * 32, 256), 256, 0, st>>>(c));
     }
     (mp::count_launch(), k_compress<<<blocks_for(n_reads, 256), 256, 0, st>>>(parent, n_reads));
     uint32_t herr = 0;

@@ -5,18 +5,18 @@
 
 namespace mp {
 
-// Sorted tuples of one scan (views into the sort buffers) plus the run-head bitmask.
+// Sorted tuples of one scan (views into the sort buffers) plus the filter's zero marks.
 struct Tuples {
     uint64_t *lo = nullptr;   // kmer << 8 | adj
     uint8_t *hi = nullptr;    // kmer >> 56 (nullable)
     uint32_t *id = nullptr;   // read id / component label
     uint64_t n = 0;
-    uint32_t *heads = nullptr;
+    uint32_t *z = nullptr;    // zero marks of the filter, one bit per tuple
 };
 
 // K4: markMischiefKmers over the scan; range_bounds = T + 1 tuple bounds of the thread ranges.
 int filter_scan(Tuples &tp, const std::vector<uint64_t> &range_bounds, uint32_t *parent, uint8_t *filtered,
-                DeviceArena &arena, cudaStream_t st);
+                DeviceArena &arena, cudaStream_t st, bool apply_zero);
 // K5: unionFindPar2 + unionFind + printStats compression for the scan.
 int union_scan(Tuples &tp, const std::vector<uint64_t> &range_bounds, uint32_t *parent, uint64_t n_reads,
                DeviceArena &arena, cudaStream_t st);

@@ -10,6 +10,7 @@
 // pass: a CTA ranks its 4096-tuple tile with warp-level multi-split, publishes its digit
 // counts, looks back over earlier tiles for its global offsets, reorders the tile in
 // shared memory and writes each digit's run contiguously.
+#include <algorithm>
 #include <cstdio>
 #include <mutex>
 #include <vector>
@@ -68,6 +69,16 @@ __global__ void __launch_bounds__(256) k_hist_upfront(const uint64_t *__restrict
     }
 }
 
+// Digit of a tuple for one pass: SRC 0 = byte of lo at `shift`, 1 = the hi byte,
+// 2 = byte of the k-mer value (lo >> 8 | hi << 56) at `shift` (the m-mer bucket digits).
+template <int SRC>
+__device__ __forceinline__ uint32_t digit_of(uint64_t lo, uint32_t hi, int shift)
+{
+    if (SRC == 0) return (uint32_t)((lo >> shift) & 0xFF);
+    if (SRC == 1) return hi;
+    return (uint32_t)((((lo >> 8) | ((uint64_t)hi << 56)) >> shift) & 0xFF);
+}
+
 template <int SRC>
 __global__ void __launch_bounds__(ST) k_onesweep(const uint64_t *__restrict__ in_lo, const uint8_t *__restrict__ in_hi,
                                                  const uint32_t *__restrict__ in_id, uint64_t *__restrict__ out_lo,
@@ -96,7 +107,7 @@ __global__ void __launch_bounds__(ST) k_onesweep(const uint64_t *__restrict__ in
         key[j] = v ? in_lo[idx] : 0ull;
         val[j] = v ? in_id[idx] : 0u;
         hv[j] = (has_hi && v) ? in_hi[idx] : (uint8_t)0;
-        dg[j] = v ? (SRC == 0 ? (uint32_t)((key[j] >> shift) & 0xFF) : (uint32_t)hv[j]) : 256u;
+        dg[j] = v ? digit_of<SRC>(key[j], hv[j], shift) : 256u;
     }
     // warp-level multi-split: stable rank of each tuple among equal digits of its warp
     const uint32_t lt = (1u << lane) - 1;
@@ -177,7 +188,7 @@ __global__ void __launch_bounds__(ST) k_onesweep(const uint64_t *__restrict__ in
     const uint32_t nv = sm.nvalid;
     for (uint32_t s = threadIdx.x; s < nv; s += ST) {
         const uint64_t kk = sm.keys[s];
-        const uint32_t dd = SRC == 0 ? (uint32_t)((kk >> shift) & 0xFF) : (uint32_t)sm.his[s];
+        const uint32_t dd = digit_of<SRC>(kk, has_hi ? sm.his[s] : 0u, shift);
         const uint64_t g = sm.gbase[dd] + (s - sm.tstart[dd]);
         if (g >= n) continue;  // only after a failed look-back (err is set)
         out_lo[g] = kk;
@@ -278,6 +289,317 @@ int radix_sort(SortBufs &b, uint64_t n, bool has_hi, DeviceArena &arena, cudaStr
     cudaEventDestroy(e1);
     arena.free_scratch(status);
     if (herr) return set_error(MP_EDEVICE, "radix sort look-back gave up (device error flags 0x%x)", herr);
+    return 0;
+}
+
+// ---------------------------------------------------------------------------
+// Sort by m-mer bucket, then within buckets.
+//
+// The tuples of a scan are sorted first by their m-mer bucket (the top 20 bits of the
+// k-mer) with onesweep passes over the bucket's bytes only -- the per-bucket counts are the
+// .kmerHist the scan was planned from, so the digit offsets need no histogram pass -- and
+// then each unit of consecutive buckets (at most SS_CAP tuples) is sorted in shared memory
+// by the rest of the key: (bucket - first bucket of the unit) << lowbits | the low k-mer
+// bits and the adjacency byte.  Buckets larger than a unit are gathered, sorted together
+// by the device-wide sort and put back.  Both steps are stable, so the result equals the
+// stable (k-mer, adjacency) order of the enumeration (metapart.c:1496, 2169-2195).
+
+constexpr int SS_THREADS = 1024;
+constexpr int SS_ITEMS = 12;
+constexpr int SS_CAP = SS_THREADS * SS_ITEMS;  // 12288 tuples per unit (about 180 KB of shared memory)
+constexpr int SS_WARPS = SS_THREADS / 32;
+constexpr uint32_t SS_MAXB = 4096;             // buckets per unit
+
+struct SegSmem {
+    uint64_t key[SS_CAP];
+    uint16_t perm[2][SS_CAP];
+    uint32_t whist[SS_WARPS][256];
+    uint32_t dstart[256];
+    uint32_t wsum[SS_WARPS];
+    unsigned long long kor, kand;
+};
+
+__global__ void __launch_bounds__(SS_THREADS) k_segsort(const uint64_t *__restrict__ ustart, const uint32_t *__restrict__ ucount,
+                                                         const uint32_t *__restrict__ ubucket, const uint64_t *__restrict__ lo_in,
+                                                         const uint8_t *__restrict__ hi_in, const uint32_t *__restrict__ id_in,
+                                                         uint64_t *__restrict__ lo_out, uint32_t *__restrict__ id_out, int bsh,
+                                                         int lowbits)
+{
+    extern __shared__ __align__(16) unsigned char smraw[];
+    SegSmem &sm = *reinterpret_cast<SegSmem *>(smraw);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint64_t start = ustart[blockIdx.x];
+    const uint32_t cnt = ucount[blockIdx.x], b0 = ubucket[blockIdx.x];
+    const uint64_t lowmask = (1ull << lowbits) - 1;
+    if (threadIdx.x == 0) { sm.kor = 0; sm.kand = ~0ull; }
+    __syncthreads();
+    unsigned long long kor = 0, kand = ~0ull;
+    for (uint32_t e = threadIdx.x; e < cnt; e += SS_THREADS) {
+        const uint64_t l = lo_in[start + e];
+        const uint64_t km = (l >> 8) | (hi_in ? ((uint64_t)hi_in[start + e] << 56) : 0ull);
+        const uint64_t key = ((uint64_t)((uint32_t)(km >> bsh) - b0) << lowbits) | (l & lowmask);
+        sm.key[e] = key;
+        sm.perm[0][e] = (uint16_t)e;
+        kor |= key;
+        kand &= key;
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+        kor |= __shfl_xor_sync(FULLM, kor, o);
+        kand &= __shfl_xor_sync(FULLM, kand, o);
+    }
+    if (lane == 0) { atomicOr(&sm.kor, kor); atomicAnd(&sm.kand, kand); }
+    __syncthreads();
+    const uint64_t varying = sm.kor ^ sm.kand;
+    int cur = 0;
+    const uint32_t lt = (1u << lane) - 1;
+    for (int dgt = 0; dgt < 8; dgt++) {
+        if (!((varying >> (8 * dgt)) & 0xFF)) continue;  // constant digit in this unit
+        for (int i = threadIdx.x; i < SS_WARPS * 256; i += SS_THREADS) (&sm.whist[0][0])[i] = 0;
+        __syncthreads();
+        uint32_t src[SS_ITEMS], dg[SS_ITEMS], rank[SS_ITEMS];
+#pragma unroll
+        for (int j = 0; j < SS_ITEMS; j++) {
+            const uint32_t e = warp * (32 * SS_ITEMS) + j * 32 + lane;
+            src[j] = e < cnt ? sm.perm[cur][e] : 0;
+            dg[j] = e < cnt ? (uint32_t)((sm.key[src[j]] >> (8 * dgt)) & 0xFF) : 256u;
+        }
+#pragma unroll
+        for (int j = 0; j < SS_ITEMS; j++) {
+            const uint32_t d = dg[j];
+            const uint32_t peers = __match_any_sync(FULLM, d);
+            uint32_t pre = 0;
+            if (d < 256) pre = sm.whist[warp][d];
+            __syncwarp();
+            if (d < 256) {
+                rank[j] = pre + __popc(peers & lt);
+                if ((peers & lt) == 0) sm.whist[warp][d] = pre + __popc(peers);
+            }
+            __syncwarp();
+        }
+        __syncthreads();
+        if (threadIdx.x < 256) {
+            const uint32_t d = threadIdx.x;
+            uint32_t r = 0;
+#pragma unroll
+            for (int w = 0; w < SS_WARPS; w++) {
+                const uint32_t t = sm.whist[w][d];
+                sm.whist[w][d] = r;
+                r += t;
+            }
+            // exclusive scan of the 256 digit totals over 8 warps
+            uint32_t x = r;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(FULLM, x, o);
+                if (lane >= o) x += y;
+            }
+            if (lane == 31) sm.wsum[warp] = x;
+            sm.dstart[d] = x - r;  // warp-local exclusive part; warp offsets added below
+        }
+        __syncthreads();
+        if (threadIdx.x < 256) {
+            uint32_t before = 0;
+            for (int w = 0; w < warp; w++) before += sm.wsum[w];
+            sm.dstart[threadIdx.x] += before;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int j = 0; j < SS_ITEMS; j++)
+            if (dg[j] < 256) sm.perm[cur ^ 1][sm.dstart[dg[j]] + sm.whist[warp][dg[j]] + rank[j]] = (uint16_t)src[j];
+        __syncthreads();
+        cur ^= 1;
+    }
+    for (uint32_t e = threadIdx.x; e < cnt; e += SS_THREADS) {
+        const uint32_t sidx = sm.perm[cur][e];
+        const uint64_t key = sm.key[sidx];
+        const uint64_t bucket = b0 + (key >> lowbits);
+        lo_out[start + e] = (bucket << lowbits) | (key & lowmask);
+        id_out[start + e] = id_in[start + sidx];
+    }
+}
+
+// Big buckets: gather with key (big-bucket index << lowbits | low bits), sort, put back.
+__global__ void k_big_gather(const uint64_t *__restrict__ bstart, const uint32_t *__restrict__ bcount,
+                             const uint64_t *__restrict__ boff, const uint64_t *__restrict__ lo_in,
+                             const uint32_t *__restrict__ id_in, uint64_t *__restrict__ tk, uint32_t *__restrict__ tid,
+                             int lowbits)
+{
+    const uint32_t b = blockIdx.x;
+    const uint64_t lowmask = (1ull << lowbits) - 1, s = bstart[b], o = boff[b];
+    for (uint32_t e = threadIdx.x; e < bcount[b]; e += blockDim.x) {
+        tk[o + e] = ((uint64_t)b << lowbits) | (lo_in[s + e] & lowmask);
+        tid[o + e] = id_in[s + e];
+    }
+}
+
+__global__ void k_big_scatter(const uint64_t *__restrict__ bstart, const uint32_t *__restrict__ bcount,
+                              const uint32_t *__restrict__ bbucket, const uint64_t *__restrict__ boff,
+                              const uint64_t *__restrict__ tk, const uint32_t *__restrict__ tid, uint64_t *__restrict__ lo_out,
+                              uint32_t *__restrict__ id_out, int lowbits)
+{
+    const uint32_t b = blockIdx.x;
+    const uint64_t lowmask = (1ull << lowbits) - 1, s = bstart[b], o = boff[b];
+    const uint64_t hibits = (uint64_t)bbucket[b] << lowbits;
+    for (uint32_t e = threadIdx.x; e < bcount[b]; e += blockDim.x) {
+        lo_out[s + e] = hibits | (tk[o + e] & lowmask);
+        id_out[s + e] = tid[o + e];
+    }
+}
+
+int bucket_sort(SortBufs &b, uint64_t n, bool has_hi, int k, const uint64_t *hist, uint64_t scan_lo, uint64_t scan_hi,
+                DeviceArena &arena, cudaStream_t st, SortStats *stats, int *out_lo_buf, int *out_hi_buf)
+{
+    if (stats) *stats = SortStats{};
+    *out_lo_buf = *out_hi_buf = b.cur;
+    if (n <= 1) return 0;
+    const int bsh = 2 * (k - 10), lowbits = 2 * (k - 10) + 8;
+    // bucket digit offsets from the histogram: digit d = byte d of the bucket
+    std::vector<uint64_t> base(3 * 256, 0), cnt(3 * 256, 0);
+    for (uint64_t bk = scan_lo; bk < scan_hi; bk++) {
+        const uint64_t c = hist[bk + 1] - hist[bk];
+        for (int d = 0; d < 3; d++) cnt[d * 256 + ((bk >> (8 * d)) & 0xFF)] += c;
+    }
+    std::vector<int> passes;
+    for (int d = 0; d < 3; d++) {
+        uint64_t acc = 0;
+        bool constant = false;
+        for (int v = 0; v < 256; v++) {
+            base[d * 256 + v] = acc;
+            if (cnt[d * 256 + v] == n) constant = true;
+            acc += cnt[d * 256 + v];
+        }
+        if (acc != n) return set_error(MP_EFMT, "the histogram does not match the scan's tuples");
+        if (!constant) passes.push_back(d);
+    }
+    const uint64_t tiles = (n + STILE - 1) / STILE;
+    uint64_t *dbase = arena.alloc<uint64_t>(3 * 256);
+    uint32_t *ctr = arena.alloc<uint32_t>(8), *err = arena.alloc<uint32_t>(1);
+    unsigned long long *status = passes.empty() ? nullptr : arena.alloc<unsigned long long>(tiles * 256);
+    if (!dbase || !ctr || !err || (!passes.empty() && !status)) return set_error(MP_ENOMEM, "device memory for the bucket sort");
+    MP_CUDA(cudaMemcpyAsync(dbase, base.data(), base.size() * 8, cudaMemcpyHostToDevice, st));
+    MP_CUDA(cudaMemsetAsync(ctr, 0, 8 * sizeof(uint32_t), st));
+    MP_CUDA(cudaMemsetAsync(err, 0, sizeof(uint32_t), st));
+    if (status) MP_CUDA(cudaMemsetAsync(status, 0, tiles * 256 * sizeof(unsigned long long), st));
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(k_onesweep<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SortSmem));
+        cudaFuncSetAttribute(k_segsort, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SegSmem));
+        attr = true;
+    }
+    cudaEvent_t ev[5];
+    for (auto &e : ev) cudaEventCreate(&e);
+    cudaEventRecord(ev[0], st);
+    for (size_t pi = 0; pi < passes.size(); pi++) {
+        const int d = passes[pi];
+        const int src = b.cur, dst = b.cur ^ 1;
+        (mp::count_launch(), k_onesweep<2><<<(unsigned)tiles, ST, sizeof(SortSmem), st>>>(
+            b.lo[src], has_hi ? b.hi[src] : nullptr, b.id[src], b.lo[dst], has_hi ? b.hi[dst] : nullptr, b.id[dst], n,
+            bsh + 8 * d, dbase + d * 256, status, ctr + pi, (uint32_t)(pi + 1), err));
+        b.cur = dst;
+    }
+    cudaEventRecord(ev[1], st);
+    // units of consecutive buckets, and the big buckets
+    std::vector<uint64_t> us, bs, bo;
+    std::vector<uint32_t> uc, ub, bc, bb;
+    {
+        uint64_t pos = 0, u_start = 0, u_cnt = 0, off = 0;
+        uint32_t u_b0 = (uint32_t)scan_lo;
+        bool have = false;
+        for (uint64_t bk = scan_lo; bk < scan_hi; bk++) {
+            const uint64_t c = hist[bk + 1] - hist[bk];
+            if (c == 0) continue;
+            if (c > (uint64_t)SS_CAP) {
+                if (have) { us.push_back(u_start); uc.push_back((uint32_t)u_cnt); ub.push_back(u_b0); have = false; }
+                bs.push_back(pos); bc.push_back((uint32_t)c); bb.push_back((uint32_t)bk); bo.push_back(off);
+                off += c;
+            } else {
+                if (have && (u_cnt + c > (uint64_t)SS_CAP || bk - u_b0 >= SS_MAXB)) {
+                    us.push_back(u_start); uc.push_back((uint32_t)u_cnt); ub.push_back(u_b0); have = false;
+                }
+                if (!have) { have = true; u_start = pos; u_cnt = 0; u_b0 = (uint32_t)bk; }
+                u_cnt += c;
+            }
+            pos += c;
+        }
+        if (have) { us.push_back(u_start); uc.push_back((uint32_t)u_cnt); ub.push_back(u_b0); }
+    }
+    const int in = b.cur, out = b.cur ^ 1;
+    const size_t nu = us.size(), nb = bs.size();
+    uint64_t *d_us = arena.alloc<uint64_t>(nu + 1), *d_bs = arena.alloc<uint64_t>(nb + 1), *d_bo = arena.alloc<uint64_t>(nb + 1);
+    uint32_t *d_uc = arena.alloc<uint32_t>(nu + 1), *d_ub = arena.alloc<uint32_t>(nu + 1);
+    uint32_t *d_bc = arena.alloc<uint32_t>(nb + 1), *d_bb = arena.alloc<uint32_t>(nb + 1);
+    if (!d_us || !d_bs || !d_bo || !d_uc || !d_ub || !d_bc || !d_bb) return set_error(MP_ENOMEM, "device memory for sort units");
+    if (nu) {
+        MP_CUDA(cudaMemcpyAsync(d_us, us.data(), nu * 8, cudaMemcpyHostToDevice, st));
+        MP_CUDA(cudaMemcpyAsync(d_uc, uc.data(), nu * 4, cudaMemcpyHostToDevice, st));
+        MP_CUDA(cudaMemcpyAsync(d_ub, ub.data(), nu * 4, cudaMemcpyHostToDevice, st));
+        (mp::count_launch(), k_segsort<<<(unsigned)nu, SS_THREADS, sizeof(SegSmem), st>>>(
+            d_us, d_uc, d_ub, b.lo[in], has_hi ? b.hi[in] : nullptr, b.id[in], b.lo[out], b.id[out], bsh, lowbits));
+    }
+    cudaEventRecord(ev[2], st);
+    uint64_t nbig = 0;
+    if (nb) {
+        MP_CUDA(cudaMemcpyAsync(d_bs, bs.data(), nb * 8, cudaMemcpyHostToDevice, st));
+        MP_CUDA(cudaMemcpyAsync(d_bc, bc.data(), nb * 4, cudaMemcpyHostToDevice, st));
+        MP_CUDA(cudaMemcpyAsync(d_bb, bb.data(), nb * 4, cudaMemcpyHostToDevice, st));
+        // batches of oversized buckets whose index fits above the low key bits
+        const size_t per_batch = lowbits >= 44 ? ((size_t)1 << (64 - lowbits)) : ((size_t)1 << 20);
+        uint64_t maxbatch = 0;
+        for (size_t b0 = 0; b0 < nb; b0 += per_batch) {
+            uint64_t t = 0;
+            for (size_t q = b0; q < nb && q < b0 + per_batch; q++) t += bc[q];
+            if (t > maxbatch) maxbatch = t;
+            nbig += t;
+        }
+        SortBufs t;
+        for (int q = 0; q < 2; q++) {
+            t.lo[q] = arena.alloc<uint64_t>(maxbatch + 1);
+            t.id[q] = arena.alloc<uint32_t>(maxbatch + 1);
+            if (!t.lo[q] || !t.id[q]) return set_error(MP_ENOMEM, "device memory for oversized buckets");
+        }
+        for (size_t b0 = 0; b0 < nb; b0 += per_batch) {
+            const size_t b1 = std::min(nb, b0 + per_batch);
+            uint64_t acc = 0;
+            for (size_t q = b0; q < b1; q++) { bo[q] = acc; acc += bc[q]; }
+            MP_CUDA(cudaMemcpyAsync(d_bo + b0, bo.data() + b0, (b1 - b0) * 8, cudaMemcpyHostToDevice, st));
+            t.cur = 0;
+            (mp::count_launch(), k_big_gather<<<(unsigned)(b1 - b0), 256, 0, st>>>(d_bs + b0, d_bc + b0, d_bo + b0, b.lo[in],
+                                                                                  b.id[in], t.lo[0], t.id[0], lowbits));
+            SortStats bst;
+            int rc = radix_sort(t, acc, false, arena, st, &bst);
+            if (rc) return rc;
+            (mp::count_launch(), k_big_scatter<<<(unsigned)(b1 - b0), 256, 0, st>>>(d_bs + b0, d_bc + b0, d_bb + b0, d_bo + b0,
+                                                                                   t.lo[t.cur], t.id[t.cur], b.lo[out],
+                                                                                   b.id[out], lowbits));
+        }
+    }
+    cudaEventRecord(ev[3], st);
+    uint32_t herr = 0;
+    MP_CUDA(cudaMemcpyAsync(&herr, err, sizeof herr, cudaMemcpyDeviceToHost, st));
+    MP_CUDA(cudaStreamSynchronize(st));
+    MP_CUDA(cudaGetLastError());
+    if (stats) {
+        float a = 0, bms = 0, c = 0;
+        cudaEventElapsedTime(&a, ev[0], ev[1]);
+        cudaEventElapsedTime(&bms, ev[1], ev[2]);
+        cudaEventElapsedTime(&c, ev[2], ev[3]);
+        stats->tuples = n;
+        stats->passes = (int)passes.size();
+        stats->pass_ms = a;
+        stats->bytes = (uint64_t)passes.size() * 2 * (12 + (has_hi ? 1 : 0)) * n;
+        stats->seg_ms = bms;
+        stats->big_ms = c;
+        stats->units = nu;
+        stats->big_buckets = nb;
+        stats->big_tuples = nbig;
+    }
+    for (auto &e : ev) cudaEventDestroy(e);
+    arena.free_scratch(status);
+    if (herr) return set_error(MP_EDEVICE, "radix sort look-back gave up (device error flags 0x%x)", herr);
+    *out_lo_buf = out;  // lo and id end in the other buffer; hi (constant within a bucket) stays in `in`
+    *out_hi_buf = in;
+    b.cur = out;
     return 0;
 }
 

@@ -18,9 +18,18 @@ struct SortStats {
     double pass_ms = 0;
     uint64_t bytes = 0;       // algorithmic bytes of the digit passes (read + write of every tuple per pass)
     uint64_t hist_bytes = 0;  // bytes read by the upfront histogram
+    double seg_ms = 0;        // shared-memory unit sort (bucket_sort)
+    double big_ms = 0;        // oversized buckets (bucket_sort)
+    uint64_t units = 0, big_buckets = 0, big_tuples = 0;
 };
 
 // Stable sort of b[cur][0, n) by (hi, lo); on return b.cur names the sorted buffer.
 int radix_sort(SortBufs &b, uint64_t n, bool has_hi, DeviceArena &arena, cudaStream_t st, SortStats *stats);
+
+// Stable sort of one scan's tuples by (k-mer, adjacency) using the scan's m-mer bucket counts
+// (hist, buckets [scan_lo, scan_hi)).  On return lo/id are in b.*[*out_lo_buf] and hi in
+// b.hi[*out_hi_buf].
+int bucket_sort(SortBufs &b, uint64_t n, bool has_hi, int k, const uint64_t *hist, uint64_t scan_lo, uint64_t scan_hi,
+                DeviceArena &arena, cudaStream_t st, SortStats *stats, int *out_lo_buf, int *out_hi_buf);
 
 }  // namespace mp

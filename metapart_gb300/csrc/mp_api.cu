@@ -76,6 +76,7 @@ struct mp_job {
     int sort_passes_total = 0;
     double sort_ms_total = 0;
     uint64_t sort_bytes_total = 0, sort_tuples_total = 0;
+    double seg_ms_total = 0;
     int pe_rounds = 0;
 };
 
@@ -449,6 +450,7 @@ int mp_job_partition(mp_job *j, const mp_part_params *p, const uint64_t *chunk_s
     j->sort_ms_total = 0;
     j->sort_bytes_total = 0;
     j->sort_tuples_total = 0;
+    j->seg_ms_total = 0;
     if (j->d_parent) { j->arena.free_persistent(j->d_parent); j->d_parent = nullptr; }
     if (j->d_size) { j->arena.free_persistent(j->d_size); j->d_size = nullptr; }
     if (j->d_filtered) { j->arena.free_persistent(j->d_filtered); j->d_filtered = nullptr; }
@@ -473,6 +475,7 @@ int mp_job_partition(mp_job *j, const mp_part_params *p, const uint64_t *chunk_s
         void *tmp = j->arena.alloc<uint8_t>(tb);
         if (!cnt || !off || !ntot || !tmp) return set_error(MP_ENOMEM, "device memory for enumeration offsets");
         SortBufs sb;
+        int lo_buf = 0, hi_buf = 0;
         uint64_t n = 0;
         {
             StageTimer tm(j->st, &j->stage_ms[2]);
@@ -513,17 +516,18 @@ int mp_job_partition(mp_job *j, const mp_part_params *p, const uint64_t *chunk_s
         {
             StageTimer tm(j->st, &j->stage_ms[3]);
             SortStats ss;
-            if ((rc = radix_sort(sb, n, has_hi, j->arena, j->st, &ss))) return rc;
+            if ((rc = bucket_sort(sb, n, has_hi, k, hist, lo, hi, j->arena, j->st, &ss, &lo_buf, &hi_buf))) return rc;
             j->sort_stats = ss;
             j->sort_passes_total += ss.passes;
             j->sort_ms_total += ss.pass_ms;
             j->sort_bytes_total += ss.bytes;
             j->sort_tuples_total += n;
+            j->seg_ms_total += ss.seg_ms + ss.big_ms;
         }
         Tuples tp;
-        tp.lo = sb.lo[sb.cur];
-        tp.hi = has_hi ? sb.hi[sb.cur] : nullptr;
-        tp.id = sb.id[sb.cur];
+        tp.lo = sb.lo[lo_buf];
+        tp.hi = has_hi ? sb.hi[hi_buf] : nullptr;
+        tp.id = sb.id[lo_buf];
         tp.n = n;
         snprintf(name, sizeof name, "scan%d_sorted.bin", s);
         if ((rc = dump_tuples(j, name, tp.lo, tp.hi, tp.id, n))) return rc;
@@ -531,7 +535,7 @@ int mp_job_partition(mp_job *j, const mp_part_params *p, const uint64_t *chunk_s
         if ((rc = range_bounds(hist, thrR.data() + (size_t)s * T, T, lo, hi, rb))) return rc;
         {
             StageTimer tm(j->st, &j->stage_ms[4]);
-            if ((rc = filter_scan(tp, rb, j->d_parent, j->d_filtered, j->arena, j->st))) return rc;
+            if ((rc = filter_scan(tp, rb, j->d_parent, j->d_filtered, j->arena, j->st, !j->dump_dir.empty()))) return rc;
         }
         snprintf(name, sizeof name, "scan%d_filtered.bin", s);
         if ((rc = dump_tuples(j, name, tp.lo, tp.hi, tp.id, n))) return rc;

@@ -137,6 +137,9 @@ def workload(name: str, n_reads: int | None = None, seed: int = 7) -> ReadSpec:
         return ReadSpec(n_reads=n_reads or 5_000_000, lengths=(250,), n_genomes=100, glen=(2e6, 2e6),
                         abundance=AB_ZIPF, ab_param=1.1, repeat_frac=0.3, repeat_len=5000, repeat_pool=200,
                         sub_rate=0.01, qual="I", seed=seed)
+    if name == "hotspot":       # one 200 bp genome at very high coverage: oversized m-mer buckets, long runs
+        return ReadSpec(n_reads=n_reads or 60_000, lengths=(100,), n_genomes=1, glen=(200, 200),
+                        sub_rate=0.002, qual="I", seed=seed)
     if name == "interleaved_small":
         return ReadSpec(n_reads=n_reads or 20_000, lengths=(100,), n_genomes=10, glen=(40_000, 40_000),
                         sub_rate=0.005, qual="#J", interleaved=True, insert_len=300, seed=seed)

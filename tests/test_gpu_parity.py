@@ -20,6 +20,8 @@ CASES = [
     ("plain_large", 30000, pu.Params(k=29, chunks=8, scans=1, threads=8)),
     ("min3", 8000, pu.Params(k=31, chunks=4, scans=1, threads=2, min3=True)),
     ("plain_small", 20000, pu.Params(k=21, chunks=4, scans=1, threads=2, min3=True)),
+    ("hotspot", 60000, pu.Params(k=31, chunks=4, scans=1, threads=2)),
+    ("hotspot", 40000, pu.Params(k=25, chunks=6, scans=2, threads=3)),
     ("interleaved_small", 20000, pu.Params(k=27, chunks=4, scans=1, threads=2, interleaved=True)),
     ("interleaved_small", 20000, pu.Params(k=25, chunks=8, scans=2, threads=2, interleaved=True)),
 ]
