@@ -51,6 +51,16 @@ def parse_args():
     ap.add_argument("--chunks", type=int, default=64)
     ap.add_argument("--cpu-reads", type=int, default=0, help="reads in the CPU sample (0: auto)")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--mode", default="plain", choices=["plain", "serve", "batch"],
+                    help="plain: one read set per step; serve: Poisson request loop (p50/p99 latency); "
+                         "batch: many samples, back to back vs queued together")
+    ap.add_argument("--duration", type=float, default=60.0, help="serve: seconds of arrivals")
+    ap.add_argument("--rate", type=float, default=20.0, help="serve: mean arrivals per second")
+    ap.add_argument("--slots", type=int, default=8, help="serve/batch: jobs in flight at most")
+    ap.add_argument("--budget-gb", type=float, default=160.0, help="serve/batch: HBM admission budget")
+    ap.add_argument("--pool", type=int, default=48, help="serve: distinct synthetic requests cycled")
+    ap.add_argument("--samples", type=int, default=64, help="batch: samples")
+    ap.add_argument("--sample-scale", type=float, default=1.0, help="batch: read-count scale")
     return ap.parse_args()
 
 
@@ -166,6 +176,10 @@ def main():
     dist = Replicas()
     if args.impl == "reference":
         return reference_arm(args, dist)
+    if args.mode == "serve":
+        return serve_mode(args, dist)
+    if args.mode == "batch":
+        return batch_mode(args, dist)
 
     import numpy as np
     import torch
@@ -218,6 +232,7 @@ def main():
     sort_bytes = sort_ms = 0.0
     sort_passes = sort_tuples = 0
     stage = {}
+    split = {}
     l0 = native.launch_count()
     dist.barrier()
     torch.cuda.synchronize(dev)
@@ -234,6 +249,13 @@ def main():
             sort_tuples += s["tuples"]
             for kk, v in job.stage_ms().items():
                 stage[kk] = stage.get(kk, 0.0) + v
+            for kk, v in job.sort_split().items():
+                if isinstance(v, dict):
+                    d = split.setdefault(kk, {})
+                    for k2, v2 in v.items():
+                        d[k2] = d.get(k2, 0) + v2
+                else:
+                    split[kk] = split.get(kk, 0.0) + v
         ev1.record(stream)
         ev1.synchronize()
     torch.cuda.synchronize(dev)
@@ -293,6 +315,9 @@ def main():
                      "traffic": (round(traffic) if traffic else None)},
         "gpu_launches": int(launches),
         "stage_ms": {kk: round(v / args.steps, 3) for kk, v in stage.items()},
+        "sort_split": {kk: ({k2: int(v2 / args.steps) for k2, v2 in v.items()} if isinstance(v, dict) else
+                             round(v / args.steps, 3) if kk.endswith("_ms") else int(v / args.steps))
+                       for kk, v in split.items()},
         "tuples_sorted_per_s": round(sort_tuples / args.steps / (ms / 1e3), 1),
         "clocks": clk.summary(),
     }
@@ -302,6 +327,210 @@ def main():
     ctx.close()
     if dist.rank == 0:
         print(json.dumps(line), flush=True)
+    dist.close()
+
+
+# ------------------------------------------------- request loop and batches
+
+def _pinned(n: int):
+    import torch
+    t = torch.empty(n, dtype=torch.uint8, pin_memory=True)
+    return t, t.data_ptr()
+
+
+def _request_params(args, spec, chunks=None):
+    from metapart_gb300 import serve
+    return serve.RequestParams(args.k, 0, 1, args.threads, chunks or args.chunks, 0)
+
+
+def serve_mode(args, dist):
+    """Poisson arrivals of partition requests into the request loop; p50/p99 latency and bases/s."""
+    import random
+
+    import numpy as np
+    import torch
+    from metapart_gb300 import native, serve, synth
+    if dist.rank != 0:
+        dist.close()
+        return
+    torch.cuda.set_device(dist.local)
+    specs = synth.serving_mix(args.pool, seed=11)
+    pool = []
+    for sp in specs:
+        t = synth.fastq_to(sp, _pinned)
+        out = torch.empty(t.numel() + 64, dtype=torch.uint8, pin_memory=True)
+        pool.append((sp, t, out, sp.n_reads * sp.lengths[0]))
+    budget = int(args.budget_gb * (1 << 30))
+    ctx = native.Context(dist.local, hbm_budget=budget)
+    srv = serve.Server(ctx, slots=args.slots, hbm_budget=budget)
+    params = [_request_params(args, sp) for sp, *_ in pool]
+    # warm-up: every slot once
+    wt = [srv.submit(t.data_ptr(), t.numel(), params[i], o.data_ptr(), o.numel())
+          for i, (sp, t, o, b) in enumerate(pool[:args.slots])]
+    for x in wt:
+        r = srv.result(x)
+        if r.status:
+            raise RuntimeError(f"warm-up request failed: {r.error}")
+    rng = random.Random(3)
+    arrivals, at = [], 0.0
+    while True:
+        at += rng.expovariate(args.rate)
+        if at >= args.duration:
+            break
+        arrivals.append(at)
+    free = list(range(len(pool)))
+    rng.shuffle(free)
+    inflight, results, stalls = {}, [], 0
+
+    def reap(block_one=False):
+        done = []
+        for tk, i in inflight.items():
+            r = srv.result(tk, wait=False)
+            if r is not None:
+                done.append((tk, i, r))
+        if not done and block_one and inflight:
+            tk = next(iter(inflight))
+            done.append((tk, inflight[tk], srv.result(tk)))
+        for tk, i, r in done:
+            del inflight[tk]
+            free.append(i)
+            results.append((i, r))
+
+    with ClockSampler(dist.local) as clk:
+        t0 = time.perf_counter()
+        for at in arrivals:
+            while True:
+                reap()
+                now = time.perf_counter() - t0
+                if now >= at:
+                    break
+                time.sleep(min(0.002, at - now))
+            if not free:
+                stalls += 1
+                reap(block_one=True)
+            i = free.pop(0)
+            sp, t, o, b = pool[i]
+            tk = srv.submit(t.data_ptr(), t.numel(), params[i], o.data_ptr(), o.numel())
+            inflight[tk] = i
+        while inflight:
+            reap(block_one=True)
+    st = srv.stats()
+    srv.close()
+    ctx.close()
+    bad = [r for _, r in results if r.status]
+    if bad:
+        raise RuntimeError(f"{len(bad)} requests failed, first: {bad[0].error}")
+    lat = np.array([r.latency_ms for _, r in results])
+    qms = np.array([r.queue_ms for _, r in results])
+    bases = sum(pool[i][3] for i, _ in results)
+    span = (max(r.t_done_ms for _, r in results) - min(r.t_submit_ms for _, r in results)) / 1e3
+    dev_ms = sum(r.device_ms for _, r in results)
+    line = {
+        "metric": METRIC, "mode": "serve", "value": round(bases / span, 1), "unit": "bases/s", "n_gpus": 1,
+        "steps": len(results), "warmup": len(wt), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "u64", "data": "synthetic (seeded generator, no real reads)",
+        "config": {"workload": f"Poisson arrivals, mean {args.rate}/s for {args.duration:.0f} s; requests of "
+                               f"10k-2M SE x 150 bp reads (log-uniform) from 5-50 genomes, 1% subs; "
+                               f"{len(pool)} distinct requests cycled",
+                   "k": args.k, "m": 10, "num_scans": 1, "num_threads": args.threads, "chunks": args.chunks,
+                   "slots": args.slots, "hbm_budget_gb": args.budget_gb},
+        "p50_ms": round(float(np.percentile(lat, 50)), 2), "p99_ms": round(float(np.percentile(lat, 99)), 2),
+        "mean_ms": round(float(lat.mean()), 2), "queue_p50_ms": round(float(np.percentile(qms, 50)), 2),
+        "queue_p99_ms": round(float(np.percentile(qms, 99)), 2), "jobs": len(results),
+        "jobs_per_s": round(len(results) / span, 2), "device_busy": round(dev_ms / 1e3 / span, 3),
+        "peak_running": st["peak_running"], "peak_reserved_gb": round(st["peak_reserved"] / (1 << 30), 2),
+        "pool_stalls": stalls, "clocks": clk.summary(),
+    }
+    print(json.dumps(line), flush=True)
+    dist.close()
+
+
+def _checksum(t, n: int) -> tuple:
+    """Order-sensitive checksum of the first n bytes of a host tensor (sums of the 8-byte words and of the words
+    times their index parity), enough to tell two runs' partition files apart."""
+    import numpy as np
+    a = t[:n].numpy()
+    w = np.frombuffer(a[: n - n % 8].tobytes() if n % 8 else a, dtype=np.uint64) if n >= 8 else np.zeros(0, np.uint64)
+    tail = bytes(a[n - n % 8:n]) if n % 8 else b""
+    return int(w.sum()), int(w[::2].sum()), int(w[1::3].sum()), tail
+
+
+def batch_mode(args, dist):
+    """Independent samples partitioned one after another through one job (plain) and queued together in the
+    request loop (batched); both from pinned host FASTQ to partition files on the host."""
+    import numpy as np
+    import torch
+    from metapart_gb300 import native, serve, synth
+    if dist.rank != 0:
+        dist.close()
+        return
+    torch.cuda.set_device(dist.local)
+    specs = synth.batch_mix(args.samples, seed=5, scale=args.sample_scale)
+    ins = [synth.fastq_to(sp, _pinned) for sp in specs]
+    outs = [torch.empty(t.numel() + 64, dtype=torch.uint8, pin_memory=True) for t in ins]
+    bases = sum(sp.n_reads * sp.lengths[0] for sp in specs)
+    budget = int(args.budget_gb * (1 << 30))
+    ctx = native.Context(dist.local, hbm_budget=budget)
+    params = [_request_params(args, sp) for sp in specs]
+
+    def plain_all():
+        job = native.Job(ctx)
+        sizes = []
+        try:
+            for t, o, p in zip(ins, outs, params):
+                job.reset()
+                f, ofs = native.fastq_index_ptr(p.num_chunks, t.data_ptr(), t.numel())
+                st = native.chunk_starts_of(f, ofs, [t.numel()])
+                job.load_ptr(t.data_ptr(), t.numel())
+                cnt = job.count(p.k, st)
+                bnd = job.partition(p.k, p.num_scans, p.num_threads, st, cnt.chunk_first_read, cnt.hist)
+                job.prepare_output()
+                sizes.append((job.output_to(o.data_ptr(), o.numel()), bnd.tolist()))
+        finally:
+            job.close()
+        return sizes
+
+    def batched_all(srv):
+        tks = [srv.submit(t.data_ptr(), t.numel(), p, o.data_ptr(), o.numel()) for t, o, p in zip(ins, outs, params)]
+        res = [srv.result(x) for x in tks]
+        bad = [r for r in res if r.status]
+        if bad:
+            raise RuntimeError(f"batched sample failed: {bad[0].error}")
+        return [(r.out_total, r.bounds) for r in res]
+
+    with ClockSampler(dist.local) as clk:
+        plain_all()  # warm-up
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        want = plain_all()
+        torch.cuda.synchronize()
+        plain_s = time.perf_counter() - t0
+        digest_plain = [_checksum(o, n) for o, (n, _) in zip(outs, want)]
+        with serve.Server(ctx, slots=args.slots, hbm_budget=budget) as srv:
+            batched_all(srv)  # warm-up
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            got = batched_all(srv)
+            torch.cuda.synchronize()
+            batched_s = time.perf_counter() - t0
+            st = srv.stats()
+    digest_batched = [_checksum(o, n) for o, (n, _) in zip(outs, got)]
+    same = want == got and digest_plain == digest_batched
+    ctx.close()
+    line = {
+        "metric": METRIC, "mode": "batch", "value": round(bases / batched_s, 1), "unit": "bases/s", "n_gpus": 1,
+        "steps": 1, "warmup": 1, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
+        "data": "synthetic (seeded generator, no real reads)",
+        "config": {"workload": f"{len(specs)} samples, reads log-uniform 50k-5M x {args.sample_scale} (even), "
+                               f"lengths in {{100,150,250}}, 10-100 genomes of 0.5-3 Mb, 1% subs",
+                   "k": args.k, "m": 10, "num_scans": 1, "num_threads": args.threads, "chunks": args.chunks,
+                   "slots": args.slots, "bases": bases, "reads": sum(sp.n_reads for sp in specs)},
+        "plain_bases_per_s": round(bases / plain_s, 1), "batched_bases_per_s": round(bases / batched_s, 1),
+        "batched_over_plain": round(plain_s / batched_s, 3), "plain_s": round(plain_s, 3),
+        "batched_s": round(batched_s, 3), "identical_results": bool(same), "peak_running": st["peak_running"],
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line), flush=True)
     dist.close()
 
 

@@ -135,6 +135,60 @@ int mp_sort_tuples(mp_ctx *ctx, const uint64_t *lo_in, const uint8_t *hi_in, con
 int mp_sort_tuples_noalloc(const uint64_t *lo_in, const uint8_t *hi_in, const uint32_t *id_in, uint64_t *lo_out,
                            uint8_t *hi_out, uint32_t *id_out, uint64_t n, void *stream);
 
+/* ---- Request loop: continuous admission of partition jobs on one context.
+ * The reference runs one input per MPI launch; this loop has no counterpart there.  Worker threads
+ * each own one job (one CUDA stream); a request is admitted in arrival order when a worker is free
+ * and its estimated HBM footprint fits in what the server budget has left, so the stages of
+ * different jobs overlap on the GPU.  A job that runs out of device memory beside others is run
+ * again alone.  Each admitted request runs the whole chain: chunk index (genFastqIdx), upload,
+ * m-mer histogram (genHistograms), partition (metapart) and the partition FASTQ download. */
+typedef struct mp_server mp_server;
+
+typedef struct {
+    int k, min3, num_scans, num_threads;  /* as mp_part_params */
+    int num_chunks;                       /* genFastqIdx chunks; a multiple of num_threads */
+    int interleaved;                      /* 1: interleaved pairs, 0: single end */
+} mp_request_params;
+
+typedef struct {
+    int status;            /* 0 or a negative MP_E* code */
+    char error[256];       /* message when status != 0 */
+    uint64_t n_reads;
+    uint64_t out_total;    /* partition FASTQ bytes written to the request's out buffer */
+    uint64_t bounds[17];   /* the 16 work partitions' read-id bounds */
+    uint64_t footprint;    /* HBM bytes reserved at admission */
+    double t_submit_ms, t_admit_ms, t_done_ms;  /* since the server was created */
+    double device_ms;      /* sum of the job's stage times on the GPU */
+} mp_result;
+
+typedef struct {
+    uint64_t queued, admitted, completed, reserved, peak_reserved, budget;
+    int running, peak_running;
+} mp_server_stats_t;
+
+/* Estimated device bytes of one request (FASTQ, read table, forest, the largest scan's tuple
+ * buffers, output), from the request size and its first records. */
+uint64_t mp_request_footprint(const char *fastq, uint64_t nbytes, const mp_request_params *p);
+
+/* slots: worker threads (jobs in flight at most); hbm_budget: bytes the admitted footprints may add
+ * up to (0 = unlimited; the context's own budget still bounds the real allocations). */
+int mp_server_create(mp_ctx *ctx, int slots, uint64_t hbm_budget, mp_server **out);
+
+/* Queues one request.  fastq (one single-end or interleaved FASTQ) and the output buffers stay
+ * owned by the caller and must stay valid until the request is done; out receives the partition
+ * files grouped as in mp_job_output, file_sizes (nullable) 16 x num_threads sizes, labels (nullable,
+ * labels_cap entries) the component label of every read. */
+int mp_server_submit(mp_server *s, const char *fastq, uint64_t nbytes, const mp_request_params *p, char *out,
+                     uint64_t out_cap, uint64_t *file_sizes, uint32_t *labels, uint64_t labels_cap, uint64_t *ticket);
+
+/* 1 and *res when the request is done (its result is then released), 0 while it is pending; with
+ * wait != 0 blocks until done. */
+int mp_server_poll(mp_server *s, uint64_t ticket, int wait, mp_result *res);
+int mp_server_stats(mp_server *s, mp_server_stats_t *st);
+
+/* Runs the queued requests to completion, then stops the workers. */
+void mp_server_destroy(mp_server *s);
+
 /* Optional stage dumps in the reference's formats (the files oracle/ref_hooks.c writes),
  * for parity testing.  NULL disables. */
 int mp_job_set_dump_dir(mp_job *job, const char *dir);
@@ -145,6 +199,15 @@ int mp_job_stage_ms(const mp_job *job, double *ms, int n);
 
 /* Algorithmic bytes and device time of the last sort's digit passes (roofline reporting). */
 int mp_job_sort_stats(const mp_job *job, uint64_t *tuples, int *passes, double *pass_ms, uint64_t *bytes);
+
+/* Where the last partition's sort time went, summed over its scans: the m-mer bucket digit passes, the
+ * shared-memory sort of bucket units, and the buckets too large for a unit (ms, and their counts);
+ * unit_counters (nullable, 8 entries): units sorted by the full shared-memory LSD fallback, groups
+ * of interleaved distinct k-mers finished by a warp, tuples those warps moved, then the unit sort's
+ * SM cycles summed over units in its load, digit passes, group marking, group finishing (and
+ * fallback) and store phases.  Tracing only; no counterpart in the reference. */
+int mp_job_sort_split(const mp_job *job, double *pass_ms, double *unit_ms, double *big_ms, uint64_t *units,
+                      uint64_t *big_buckets, uint64_t *big_tuples, uint64_t *unit_counters);
 
 #ifdef __cplusplus
 }

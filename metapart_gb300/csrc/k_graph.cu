@@ -104,10 +104,13 @@ __device__ __forceinline__ void mark_tuple(uint32_t J, uint64_t q, uint32_t adj,
 }
 
 // One warp per SEG tuples: the runs whose first tuple lies in the warp's segment.  In each
-// window of 32 tuples a lane finds whether its tuple starts a run (one shuffle), and 14
-// ballots give every run its before/after adjacency-code counts by popcount.  A run still
-// open at the end of a window is carried (its counts held by every lane); when a run spans
-// windows its marks are applied by one more pass over it after it is judged.
+// window of 32 tuples a lane finds whether its tuple starts a run (one shuffle) and whether its
+// adjacency byte differs from the previous tuple of its run.  A run whose tuples all share one
+// adjacency byte has at most one before- and one after-code, so markMischiefKmers leaves it alone;
+// a window holding only such runs costs a few ballots.  Otherwise 14 ballots give every run its
+// before/after adjacency-code counts by popcount.  A run still open at the end of a window is
+// carried: while it is uniform its counts follow from its length and byte; when it spans windows
+// its marks are applied by one more pass over it after it is judged.
 __global__ void __launch_bounds__(256) k_filter_warp(const uint64_t *lo, const uint8_t *hi, const uint32_t *id,
                                                      uint64_t n, const uint64_t *range_ends, int T, uint32_t *parent,
                                                      uint8_t *filtered, uint32_t *z)
@@ -120,12 +123,18 @@ __global__ void __launch_bounds__(256) k_filter_warp(const uint64_t *lo, const u
     if (c0 >= n) return;
     const uint64_t c1 = min(n, c0 + SEG);
     const uint32_t le = (lane == 31) ? FULLW : ((2u << lane) - 1);  // lanes <= lane
-    bool open = false;
+    bool open = false, ohom = true;  // a run carried into the next window; all its bytes equal so far
     uint64_t rs = 0;
-    uint32_t cb[7], ca[7], deg = 0;
+    uint32_t cb[7], ca[7], deg = 0;  // its counts (kept while it is not uniform)
 #pragma unroll
     for (int c = 0; c < 7; c++) cb[c] = ca[c] = 0;
-    uint64_t prev_km = c0 ? kmer_of(lo, hi, c0 - 1) : 0;
+    uint64_t prev_km = 0;
+    uint32_t prev_adj = 0;
+    if (c0) {
+        const uint64_t l = lo[c0 - 1];
+        prev_km = (l >> 8) | (hi ? ((uint64_t)hi[c0 - 1] << 56) : 0ull);
+        prev_adj = (uint32_t)(l & 0xFF);
+    }
     uint64_t nlv = c0 + lane < n ? lo[c0 + lane] : 0;  // next window's words, loaded one window ahead
     uint8_t nhv = (hi && c0 + lane < n) ? hi[c0 + lane] : 0;
     for (uint64_t p = c0;; p += 32) {
@@ -139,20 +148,48 @@ __global__ void __launch_bounds__(256) k_filter_warp(const uint64_t *lo, const u
             nlv = lo[i + 32];
             if (hi) nhv = hi[i + 32];
         }
+        const uint32_t adj = (uint32_t)(lv & 0xFF);
         uint64_t pk = __shfl_up_sync(FULLW, km, 1);
-        if (lane == 0) pk = prev_km;
+        uint32_t pa = __shfl_up_sync(FULLW, adj, 1);
+        if (lane == 0) {
+            pk = prev_km;
+            pa = prev_adj;
+        }
         const bool head = valid && (i == 0 || km != pk);
         const uint32_t H = __ballot_sync(FULLW, head), V = __ballot_sync(FULLW, valid);
+        const uint32_t D = __ballot_sync(FULLW, valid && !head && adj != pa);
+        const uint32_t run_adj = prev_adj;  // byte of a uniform carried run
         prev_km = __shfl_sync(FULLW, km, 31);
-        const uint32_t adj = (uint32_t)(lv & 0xFF);
+        prev_adj = __shfl_sync(FULLW, adj, 31);
+        const int fh = H ? __ffs(H) - 1 : 32;
+        const bool arr_end = p + 32 >= n;
+        const int lh = H ? 31 - __clz(H) : -1;
+        if (D == 0 && !(open && !ohom)) {
+            // every run that ends in this window is uniform: no marks
+            if (open && (fh < 32 || arr_end)) open = false;
+            if (!owned) continue;
+            if (lh >= 0 && !arr_end) {
+                open = true;
+                ohom = true;
+                rs = p + lh;
+            }
+            continue;
+        }
+        if (open && ohom) {  // counts of the uniform part carried in
+            const uint32_t len = (uint32_t)(p - rs);
+#pragma unroll
+            for (int c = 0; c < 7; c++) cb[c] = ca[c] = 0;
+            if ((run_adj & 7) < 7) cb[run_adj & 7] = len;
+            if (((run_adj >> 3) & 7) < 7) ca[(run_adj >> 3) & 7] = len;
+            deg = len;
+            ohom = false;
+        }
         uint32_t Bm[7], Am[7];
 #pragma unroll
         for (int c = 0; c < 7; c++) {
             Bm[c] = __ballot_sync(FULLW, valid && (adj & 7) == (uint32_t)c);
             Am[c] = __ballot_sync(FULLW, valid && ((adj >> 3) & 7) == (uint32_t)c);
         }
-        const int fh = H ? __ffs(H) - 1 : 32;
-        const bool arr_end = p + 32 >= n;
         // the run carried into this window occupies lanes [0, fh)
         if (open) {
             const uint32_t m = lane_range(0, fh) & V;
@@ -178,23 +215,27 @@ __global__ void __launch_bounds__(256) k_filter_warp(const uint64_t *lo, const u
         const int nh = later ? __ffs(later) - 1 : 32;
         if (head && (nh < 32 || arr_end)) {
             const uint32_t m = lane_range(lane, nh) & V;
-            uint32_t b[7], a[7];
+            if (D & m) {  // a uniform run needs no judgement
+                uint32_t b[7], a[7];
 #pragma unroll
-            for (int c = 0; c < 7; c++) { b[c] = __popc(Bm[c] & m); a[c] = __popc(Am[c] & m); }
-            const uint64_t re = nh < 32 ? p + nh : n;
-            if (!at_range_end(ends, T, re)) J = judge_run(b, a, __popc(m));
+                for (int c = 0; c < 7; c++) { b[c] = __popc(Bm[c] & m); a[c] = __popc(Am[c] & m); }
+                const uint64_t re = nh < 32 ? p + nh : n;
+                if (!at_range_end(ends, T, re)) J = judge_run(b, a, __popc(m));
+            }
         }
         const uint32_t Js = __shfl_sync(FULLW, J, s < 0 ? 0 : s);
         if (s >= 0 && valid) mark_tuple(Js, i, adj, id, parent, filtered, z);  // J == 0 for the still-open run
         // the last run of the window stays open when the array continues past it
-        const int lh = H ? 31 - __clz(H) : -1;
         if (lh >= 0 && !arr_end) {
             const uint32_t m = lane_range(lh, 32) & V;
-#pragma unroll
-            for (int c = 0; c < 7; c++) { cb[c] = __popc(Bm[c] & m); ca[c] = __popc(Am[c] & m); }
-            deg = __popc(m);
             rs = p + lh;
             open = true;
+            ohom = (D & m) == 0;
+            if (!ohom) {
+#pragma unroll
+                for (int c = 0; c < 7; c++) { cb[c] = __popc(Bm[c] & m); ca[c] = __popc(Am[c] & m); }
+                deg = __popc(m);
+            }
         }
     }
 }

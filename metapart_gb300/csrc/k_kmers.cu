@@ -18,12 +18,11 @@ namespace mp {
 constexpr unsigned FULL = 0xFFFFFFFFu;
 
 struct Round {
-    uint64_t W;     // codes of positions 32t..32t+31, position 32t in bits 63..62
-    uint32_t N;     // bit j: position 32t+j is 'N'
-    uint32_t A[5];  // bit b of a5 (char bits 1..5) per position
+    uint64_t W;  // codes of positions 32t..32t+31, position 32t in bits 63..62
+    uint32_t N;  // bit j: position 32t+j is 'N'
+    uint32_t c;  // this lane's character (position 32t+lane); the adjacency bytes take neighbours by shuffle
 };
 
-template <bool ADJ>
 __device__ __forceinline__ void load_round(const uint8_t *s, uint32_t L, int t, int lane, Round &r)
 {
     const uint32_t p = 32u * (uint32_t)t + (uint32_t)lane;
@@ -32,19 +31,7 @@ __device__ __forceinline__ void load_round(const uint8_t *s, uint32_t L, int t, 
     const uint32_t P1 = __ballot_sync(FULL, f & 2), P0 = __ballot_sync(FULL, f & 1);
     r.W = (spread32(__brev(P1)) << 1) | spread32(__brev(P0));
     r.N = __ballot_sync(FULL, p < L && c == 'N');
-    if (ADJ) {
-        const uint32_t a = a5_of(c);
-#pragma unroll
-        for (int b = 0; b < 5; b++) r.A[b] = __ballot_sync(FULL, (a >> b) & 1);
-    }
-}
-
-__device__ __forceinline__ uint32_t a5_at(const uint32_t *A, int bit)
-{
-    uint32_t v = 0;
-#pragma unroll
-    for (int b = 0; b < 5; b++) v |= ((A[b] >> bit) & 1u) << b;
-    return v;
+    r.c = c;
 }
 
 // Forward code, validity (no N in the window) of the k-mer at lane's position of round t.
@@ -86,8 +73,8 @@ __global__ void __launch_bounds__(256) k_count_plain(const uint8_t *fq, const ui
         uint32_t *ccc = cc ? cc + (size_t)chunk_of(chunk_rec, nchunks, r) * NB : nullptr;
         const int last = (int)L - k;
         Round cur, nxt;
-        load_round<false>(s, L, 0, lane, cur);
-        load_round<false>(s, L, 1, lane, nxt);
+        load_round(s, L, 0, lane, cur);
+        load_round(s, L, 1, lane, nxt);
         for (int t = 0; 32 * t <= last; t++) {
             const int i = 32 * t + lane;
             uint64_t fwd;
@@ -103,7 +90,7 @@ __global__ void __launch_bounds__(256) k_count_plain(const uint8_t *fq, const ui
                 }
             }
             cur = nxt;
-            load_round<false>(s, L, t + 2, lane, nxt);
+            load_round(s, L, t + 2, lane, nxt);
         }
     }
 }
@@ -225,8 +212,8 @@ __global__ void __launch_bounds__(256) k_enum_plain(const uint8_t *fq, const uin
             id = (p == BAD) ? (uint32_t)r : p;  // findRoot after full compression (metapart.c:543-568)
         }
         Round prv, cur, nxt;
-        load_round<WRITE>(s, L, 0, lane, cur);
-        load_round<WRITE>(s, L, 1, lane, nxt);
+        load_round(s, L, 0, lane, cur);
+        load_round(s, L, 1, lane, nxt);
         prv = cur;
         uint32_t total = 0;
         for (int t = 0; 32 * t <= last; t++) {
@@ -239,13 +226,17 @@ __global__ void __launch_bounds__(256) k_enum_plain(const uint8_t *fq, const uin
             const uint32_t b = (uint32_t)(canon >> sh);
             const bool v = v0 && b >= lo && b < hi;
             const uint32_t bal = __ballot_sync(FULL, v);
+            uint32_t pc = 0, nc = 0;  // characters before and after this lane's k-mer
+            if (WRITE) {
+                const uint32_t x = __shfl_sync(FULL, cur.c, (lane + 31) & 31), y = __shfl_sync(FULL, prv.c, 31);
+                pc = lane ? x : y;
+                const int q = lane + k;
+                const uint32_t u = __shfl_sync(FULL, cur.c, q & 31), w = __shfl_sync(FULL, nxt.c, q & 31);
+                nc = q < 32 ? u : w;
+            }
             if (WRITE && v) {
-                uint32_t pa = 7u, na = 7u;  // 'N' at the read ends (enumerateKmers.c:177, 252-255)
-                if (i > 0) pa = lane ? a5_at(cur.A, lane - 1) : a5_at(prv.A, 31);
-                if (i < last) {
-                    const int q = lane + k;
-                    na = q < 32 ? a5_at(cur.A, q) : a5_at(nxt.A, q - 32);
-                }
+                // 'N' at the read ends (enumerateKmers.c:177, 252-255)
+                const uint32_t pa = i > 0 ? a5_of(pc) : 7u, na = i < last ? a5_of(nc) : 7u;
                 const uint32_t adj = f ? adj_fwd(pa, na) : adj_rc(pa, na);
                 const uint64_t pos = base + __popc(bal & ((1u << lane) - 1));
                 o_lo[pos] = (canon << 8) | adj;
@@ -256,11 +247,69 @@ __global__ void __launch_bounds__(256) k_enum_plain(const uint8_t *fq, const uin
             total += __popc(bal);
             prv = cur;
             cur = nxt;
-            load_round<WRITE>(s, L, t + 2, lane, nxt);
+            load_round(s, L, t + 2, lane, nxt);
         }
         if (!WRITE && lane == 0) {
             cnt[r] = total;
             if (total > 255) atomicOr(err, DERR_TOO_MANY);  // the reference's per-read counter is a uint8_t
+        }
+    }
+}
+
+// Tuples per read of every scan in one pass: scan s holds buckets [bounds[s], bounds[s+1]).
+// cnt[s * stride + r]; S <= MAX_SCAN_COUNT.
+constexpr int MAX_SCAN_COUNT = 8;
+
+__global__ void __launch_bounds__(256) k_enum_count_scans(const uint8_t *fq, const uint64_t *seq_off,
+                                                          const uint32_t *seq_len, uint64_t n_reads, int k,
+                                                          const uint32_t *bounds, int S, uint32_t *cnt, uint64_t stride,
+                                                          uint32_t *err)
+{
+    __shared__ uint32_t sb[MAX_SCAN_COUNT + 1];
+    if (threadIdx.x <= (unsigned)S) sb[threadIdx.x] = bounds[threadIdx.x];
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    const int sh = 2 * (k - 10);
+    const uint32_t b_lo = sb[0], b_hi = sb[S];
+    for (uint64_t r = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < n_reads; r += nw) {
+        const uint32_t L = seq_len[r];
+        uint32_t c[MAX_SCAN_COUNT];
+#pragma unroll
+        for (int q = 0; q < MAX_SCAN_COUNT; q++) c[q] = 0;
+        if (L > (uint32_t)k && (L > 32u * MAX_ROUNDS_ENUM || L - (uint32_t)k >= 300u)) {
+            if (lane == 0) atomicOr(err, DERR_LONG_READ);
+        } else if (L > (uint32_t)k) {
+            const uint8_t *s = fq + seq_off[r];
+            const int last = (int)L - k;
+            Round cur, nxt;
+            load_round(s, L, 0, lane, cur);
+            load_round(s, L, 1, lane, nxt);
+            for (int t = 0; 32 * t <= last; t++) {
+                const int i = 32 * t + lane;
+                uint64_t fwd;
+                const bool v0 = kmer_at(lane, k, cur, nxt, fwd) && i <= last;
+                const uint64_t rc = revcomp(fwd, k);
+                const uint32_t b = (uint32_t)((fwd < rc ? fwd : rc) >> sh);
+                if (v0 && b >= b_lo && b < b_hi) {
+                    int sc = 0;
+#pragma unroll
+                    for (int q = 1; q < MAX_SCAN_COUNT; q++) sc += (q < S && b >= sb[q]) ? 1 : 0;
+#pragma unroll
+                    for (int q = 0; q < MAX_SCAN_COUNT; q++) c[q] += (sc == q) ? 1u : 0u;
+                }
+                cur = nxt;
+                load_round(s, L, t + 2, lane, nxt);
+            }
+        }
+        for (int q = 0; q < S; q++) {
+            uint32_t x = c[q];
+#pragma unroll
+            for (int o = 16; o; o >>= 1) x += __shfl_xor_sync(FULL, x, o);
+            if (lane == 0) {
+                cnt[(uint64_t)q * stride + r] = x;
+                if (x > 255) atomicOr(err, DERR_TOO_MANY);  // the reference's per-read counter is a uint8_t
+            }
         }
     }
 }
@@ -336,6 +385,15 @@ void launch_enum_count(const uint8_t *fq, const ParsedReads &pr, int k, int min3
     else
         (mp::count_launch(), k_enum_plain<false><<<grid_for(pr.n_reads, 8), 256, 0, st>>>(fq, pr.seq_off, pr.seq_len, pr.n_reads, k, lo, hi,
                                                                      nullptr, nullptr, cnt, nullptr, nullptr, nullptr, err));
+}
+
+int launch_enum_count_scans(const uint8_t *fq, const ParsedReads &pr, int k, const uint32_t *bounds, int S,
+                            uint32_t *cnt, uint64_t stride, uint32_t *err, cudaStream_t st)
+{
+    if (S < 1 || S > MAX_SCAN_COUNT) return -1;
+    (mp::count_launch(), k_enum_count_scans<<<grid_for(pr.n_reads, 8), 256, 0, st>>>(
+        fq, pr.seq_off, pr.seq_len, pr.n_reads, k, bounds, S, cnt, stride, err));
+    return 0;
 }
 
 void launch_enum_write(const uint8_t *fq, const ParsedReads &pr, int k, int min3, uint32_t lo, uint32_t hi,

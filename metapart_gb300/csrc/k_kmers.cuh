@@ -12,6 +12,11 @@ void launch_count(const uint8_t *fq, const ParsedReads &pr, int k, int min3, con
 void launch_enum_count(const uint8_t *fq, const ParsedReads &pr, int k, int min3, uint32_t lo, uint32_t hi,
                        uint32_t *cnt, uint32_t *err, cudaStream_t st);
 
+// K2a for all scans at once (plain variant, at most 8 scans): cnt[s * stride + read] for the buckets
+// [bounds[s], bounds[s+1]) (bounds: S + 1 device words).  Returns -1 (nothing launched) for other S.
+int launch_enum_count_scans(const uint8_t *fq, const ParsedReads &pr, int k, const uint32_t *bounds, int S,
+                            uint32_t *cnt, uint64_t stride, uint32_t *err, cudaStream_t st);
+
 // K2b: tuples at off[read]: o_lo = kmer << 8 | adj, o_hi = kmer >> 56 (nullable when k <= 28),
 // o_id = read id (scan 0, label == nullptr) or its component label.
 void launch_enum_write(const uint8_t *fq, const ParsedReads &pr, int k, int min3, uint32_t lo, uint32_t hi,

@@ -1,5 +1,6 @@
 // Device memory arena, the parsed-read table and the host-side stage entry points.
 #pragma once
+#include <atomic>
 #include <vector>
 
 #include "mp_common.cuh"
@@ -8,11 +9,11 @@ namespace mp {
 
 // Stream-ordered device allocations of one job.  Scratch allocations live until
 // release_scratch(); persistent ones until release_all().  Sizes are charged
-// against the context's HBM budget.
+// against the context's HBM budget, which jobs running on other host threads share.
 struct DeviceArena {
     cudaStream_t st = nullptr;
     std::vector<std::pair<void *, size_t>> persistent, scratch;
-    uint64_t *budget_used = nullptr;  // shared with the context
+    std::atomic<uint64_t> *budget_used = nullptr;  // shared with the context
     uint64_t budget_limit = ~0ull;
     uint64_t peak = 0, live = 0;
 
@@ -20,14 +21,19 @@ struct DeviceArena {
     {
         bytes = (bytes + 255) & ~(size_t)255;
         if (bytes == 0) bytes = 256;
-        if (budget_used && *budget_used + bytes > budget_limit) return nullptr;
+        if (budget_used) {  // reserve first, so concurrent jobs never overshoot the budget together
+            uint64_t cur = budget_used->load();
+            do {
+                if (cur + bytes > budget_limit) return nullptr;
+            } while (!budget_used->compare_exchange_weak(cur, cur + bytes));
+        }
         void *p = nullptr;
         if (cudaMallocAsync(&p, bytes, st) != cudaSuccess) {
             cudaGetLastError();
+            if (budget_used) budget_used->fetch_sub(bytes);
             return nullptr;
         }
         (keep ? persistent : scratch).push_back({p, bytes});
-        if (budget_used) *budget_used += bytes;
         live += bytes;
         if (live > peak) peak = live;
         return p;
@@ -39,7 +45,7 @@ struct DeviceArena {
         for (size_t i = 0; i < v.size(); i++)
             if (v[i].first == p) {
                 cudaFreeAsync(p, st);
-                if (budget_used) *budget_used -= v[i].second;
+                if (budget_used) budget_used->fetch_sub(v[i].second);
                 live -= v[i].second;
                 v.erase(v.begin() + (long)i);
                 return;
@@ -51,7 +57,7 @@ struct DeviceArena {
     {
         for (auto &x : scratch) {
             cudaFreeAsync(x.first, st);
-            if (budget_used) *budget_used -= x.second;
+            if (budget_used) budget_used->fetch_sub(x.second);
             live -= x.second;
         }
         scratch.clear();
@@ -61,7 +67,7 @@ struct DeviceArena {
         release_scratch();
         for (auto &x : persistent) {
             cudaFreeAsync(x.first, st);
-            if (budget_used) *budget_used -= x.second;
+            if (budget_used) budget_used->fetch_sub(x.second);
             live -= x.second;
         }
         persistent.clear();

@@ -11,6 +11,7 @@
 // counts, looks back over earlier tiles for its global offsets, reorders the tile in
 // shared memory and writes each digit's run contiguously.
 #include <algorithm>
+#include <cstdlib>
 #include <cstdio>
 #include <mutex>
 #include <vector>
@@ -19,7 +20,7 @@
 
 namespace mp {
 
-constexpr int ST = 256;
+constexpr int ST = 256;  // threads per tile (two resident tiles per SM)
 constexpr int SI = 16;
 constexpr int STILE = ST * SI;
 constexpr int SW = ST / 32;
@@ -71,6 +72,9 @@ __global__ void __launch_bounds__(256) k_hist_upfront(const uint64_t *__restrict
 
 // Digit of a tuple for one pass: SRC 0 = byte of lo at `shift`, 1 = the hi byte,
 // 2 = byte of the k-mer value (lo >> 8 | hi << 56) at `shift` (the m-mer bucket digits).
+// Opt-in shared memory sizes of the sort kernels, set once per device (thread-safe).
+static void sort_kernel_attrs();
+
 template <int SRC>
 __device__ __forceinline__ uint32_t digit_of(uint64_t lo, uint32_t hi, int shift)
 {
@@ -80,12 +84,12 @@ __device__ __forceinline__ uint32_t digit_of(uint64_t lo, uint32_t hi, int shift
 }
 
 template <int SRC>
-__global__ void __launch_bounds__(ST) k_onesweep(const uint64_t *__restrict__ in_lo, const uint8_t *__restrict__ in_hi,
-                                                 const uint32_t *__restrict__ in_id, uint64_t *__restrict__ out_lo,
-                                                 uint8_t *__restrict__ out_hi, uint32_t *__restrict__ out_id, uint64_t n,
-                                                 int shift, const uint64_t *__restrict__ dbase,
-                                                 unsigned long long *status, uint32_t *tile_ctr, uint32_t epoch,
-                                                 uint32_t *err)
+__global__ void __launch_bounds__(ST, 2) k_onesweep(const uint64_t *__restrict__ in_lo, const uint8_t *__restrict__ in_hi,
+                                                    const uint32_t *__restrict__ in_id, uint64_t *__restrict__ out_lo,
+                                                    uint8_t *__restrict__ out_hi, uint32_t *__restrict__ out_id, uint64_t n,
+                                                    int shift, const uint64_t *__restrict__ dbase,
+                                                    unsigned long long *status, uint32_t *tile_ctr, uint32_t epoch,
+                                                    uint32_t *err)
 {
     extern __shared__ __align__(16) unsigned char smraw[];
     SortSmem &sm = *reinterpret_cast<SortSmem *>(smraw);
@@ -98,90 +102,96 @@ __global__ void __launch_bounds__(ST) k_onesweep(const uint64_t *__restrict__ in
     const bool has_hi = in_hi != nullptr;
 
     uint64_t key[SI];
-    uint32_t val[SI], rank[SI], dg[SI];
-    uint8_t hv[SI];
+    uint32_t val[SI], rd[SI];  // rd: rank within the warp's digit (bits 0-15) | digit (bits 16-24, 256 = none)
+    uint32_t hv[(SI + 3) / 4];
+#pragma unroll
+    for (int j = 0; j < (SI + 3) / 4; j++) hv[j] = 0;
 #pragma unroll
     for (int j = 0; j < SI; j++) {
         const uint64_t idx = base + (uint64_t)warp * (32 * SI) + (uint64_t)j * 32 + lane;
         const bool v = idx < n;
         key[j] = v ? in_lo[idx] : 0ull;
         val[j] = v ? in_id[idx] : 0u;
-        hv[j] = (has_hi && v) ? in_hi[idx] : (uint8_t)0;
-        dg[j] = v ? digit_of<SRC>(key[j], hv[j], shift) : 256u;
+        const uint32_t h = (has_hi && v) ? (uint32_t)in_hi[idx] : 0u;
+        hv[j >> 2] |= h << (8 * (j & 3));
+        rd[j] = (v ? digit_of<SRC>(key[j], h, shift) : 256u) << 16;
     }
     // warp-level multi-split: stable rank of each tuple among equal digits of its warp
     const uint32_t lt = (1u << lane) - 1;
 #pragma unroll
     for (int j = 0; j < SI; j++) {
-        const uint32_t d = dg[j];
+        const uint32_t d = rd[j] >> 16;
         const uint32_t peers = __match_any_sync(FULLM, d);
         uint32_t pre = 0;
         if (d < 256) pre = sm.whist[warp][d];
         __syncwarp();
         if (d < 256) {
-            rank[j] = pre + __popc(peers & lt);
+            rd[j] |= pre + __popc(peers & lt);
             if ((peers & lt) == 0) sm.whist[warp][d] = pre + __popc(peers);
         }
         __syncwarp();
     }
     __syncthreads();
-    // thread d: warp prefixes and tile count of digit d
+    // threads 0..255 own one digit each: warp prefixes, the tile count, its look-back
     const uint32_t d = threadIdx.x;
-    uint32_t run = 0;
+    const bool dig = d < 256;
+    uint32_t cnt = 0, x = 0;
+    if (dig) {
 #pragma unroll
-    for (int w = 0; w < SW; w++) {
-        const uint32_t t = sm.whist[w][d];
-        sm.whist[w][d] = run;
-        run += t;
-    }
-    const uint32_t cnt = run;
-    const unsigned long long E = (unsigned long long)epoch << 60, PF = 1ull << 59, CM = PF - 1;
-    unsigned long long *me = status + tile * 256 + d;
-    st_relaxed(me, tile == 0 ? (E | PF | cnt) : (E | cnt));
-    // tile-local exclusive scan of digit counts
-    {
-        uint32_t x = cnt;
+        for (int w = 0; w < SW; w++) {
+            const uint32_t t = sm.whist[w][d];
+            sm.whist[w][d] = cnt;
+            cnt += t;
+        }
+        const unsigned long long E = (unsigned long long)epoch << 60, PF = 1ull << 59;
+        st_relaxed(status + tile * 256 + d, tile == 0 ? (E | PF | cnt) : (E | cnt));
+        // tile-local exclusive scan of the digit counts (warps 0..7 are all digit owners)
+        x = cnt;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
-            uint32_t y = __shfl_up_sync(FULLM, x, o);
+            const uint32_t y = __shfl_up_sync(FULLM, x, o);
             if (lane >= o) x += y;
         }
         if (lane == 31) sm.wsum[warp] = x;
-        __syncthreads();
+    }
+    __syncthreads();
+    if (dig) {
         uint32_t before = 0;
         for (int w = 0; w < warp; w++) before += sm.wsum[w];
         sm.tstart[d] = before + x - cnt;
-    }
-    // decoupled look-back for digit d
-    unsigned long long excl = 0;
-    if (tile > 0) {
-        int64_t p = (int64_t)tile - 1;
-        uint32_t spins = 0;
-        while (p >= 0) {
-            const unsigned long long v = ld_relaxed(status + (uint64_t)p * 256 + d);
-            if ((v >> 60) != epoch) {
-                if (++spins > SPIN_CAP) {
-                    atomicOr(err, DERR_SPIN);
-                    break;
+        // decoupled look-back for digit d
+        const unsigned long long E = (unsigned long long)epoch << 60, PF = 1ull << 59, CM = PF - 1;
+        unsigned long long excl = 0;
+        if (tile > 0) {
+            int64_t p = (int64_t)tile - 1;
+            uint32_t spins = 0;
+            while (p >= 0) {
+                const unsigned long long v = ld_relaxed(status + (uint64_t)p * 256 + d);
+                if ((v >> 60) != epoch) {
+                    if (++spins > SPIN_CAP) {
+                        atomicOr(err, DERR_SPIN);
+                        break;
+                    }
+                    continue;
                 }
-                continue;
+                excl += v & CM;
+                if (v & PF) break;
+                p--;
             }
-            excl += v & CM;
-            if (v & PF) break;
-            p--;
+            st_relaxed(status + tile * 256 + d, E | PF | (excl + cnt));
         }
-        st_relaxed(me, E | PF | (excl + cnt));
+        sm.gbase[d] = dbase[d] + excl;
     }
-    sm.gbase[d] = dbase[d] + excl;
     if (threadIdx.x == 0) sm.nvalid = (uint32_t)min((uint64_t)STILE, n - base);
     __syncthreads();
 #pragma unroll
     for (int j = 0; j < SI; j++) {
-        if (dg[j] < 256) {
-            const uint32_t s = sm.tstart[dg[j]] + sm.whist[warp][dg[j]] + rank[j];
+        const uint32_t dd = rd[j] >> 16;
+        if (dd < 256) {
+            const uint32_t s = sm.tstart[dd] + sm.whist[warp][dd] + (rd[j] & 0xFFFF);
             sm.keys[s] = key[j];
             sm.vals[s] = val[j];
-            if (has_hi) sm.his[s] = hv[j];
+            if (has_hi) sm.his[s] = (uint8_t)(hv[j >> 2] >> (8 * (j & 3)));
         }
     }
     __syncthreads();
@@ -242,12 +252,7 @@ int radix_sort(SortBufs &b, uint64_t n, bool has_hi, DeviceArena &arena, cudaStr
         if (!constant) passes.push_back(dgt);
     }
     MP_CUDA(cudaMemcpyAsync(dbase, base.data(), base.size() * sizeof(uint64_t), cudaMemcpyHostToDevice, st));
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaFuncSetAttribute(k_onesweep<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SortSmem));
-        cudaFuncSetAttribute(k_onesweep<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SortSmem));
-        attr_set = true;
-    }
+    sort_kernel_attrs();
     std::vector<cudaEvent_t> ev(passes.size() + 1);
     for (auto &e : ev) cudaEventCreate(&e);
     cudaEventRecord(ev[0], st);
@@ -310,20 +315,104 @@ constexpr int SS_CAP = SS_THREADS * SS_ITEMS;  // 12288 tuples per unit (about 1
 constexpr int SS_WARPS = SS_THREADS / 32;
 constexpr uint32_t SS_MAXB = 4096;             // buckets per unit
 
+constexpr int SS_GBITS = 8;             // bits per grouping pass: three passes group a unit by its top 24 varying bits
+constexpr int SS_GPASSES = 3;
+constexpr int SS_WORDS = SS_CAP / 32;
+
+constexpr int SS_LIST = 4096;           // out-of-order groups a unit may queue for the warps
+constexpr int SS_MAX_KMERS = 64;        // distinct k-mers a warp separates in one out-of-order group
+
 struct SegSmem {
     uint64_t key[SS_CAP];
     uint16_t perm[2][SS_CAP];
     uint32_t whist[SS_WARPS][256];
-    uint32_t dstart[256];
     uint32_t wsum[SS_WARPS];
+    uint32_t gstart[SS_WORDS];  // bit p: position p starts a group
+    uint32_t dirty[SS_WORDS];   // bit p: position p is out of order within its group
+    uint32_t list[SS_LIST];     // out-of-order groups: start | end << 16
     unsigned long long kor, kand;
+    uint32_t fallback, nlist;
 };
 
+// One stable counting-sort pass over a unit: perm[cur] (or the identity) -> perm[cur ^ 1] by the
+// digit (key >> sh) & (2^BITS - 1).  Items are ranked in warp-blocked order; a warp finds the lanes
+// holding its digit with match_any, so equal digits keep their order.
+template <int BITS>
+__device__ void seg_pass(SegSmem &sm, int cur, uint32_t cnt, int sh, bool identity)
+{
+    constexpr uint32_t NBIN = 1u << BITS, MASK = NBIN - 1;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t lt = (1u << lane) - 1;
+    for (uint32_t i = threadIdx.x; i < SS_WARPS * NBIN; i += SS_THREADS) sm.whist[i / NBIN][i % NBIN] = 0;
+    __syncthreads();
+    uint32_t src[SS_ITEMS], dg[SS_ITEMS], rank[SS_ITEMS];
+#pragma unroll
+    for (int j = 0; j < SS_ITEMS; j++) {
+        const uint32_t e = warp * (32 * SS_ITEMS) + j * 32 + lane;
+        const bool v = e < cnt;
+        src[j] = v ? (identity ? e : (uint32_t)sm.perm[cur][e]) : 0u;
+        dg[j] = v ? (uint32_t)((sm.key[src[j]] >> sh) & MASK) : NBIN;
+    }
+#pragma unroll
+    for (int j = 0; j < SS_ITEMS; j++) {
+        const uint32_t d = dg[j];
+        const uint32_t peers = __match_any_sync(FULLM, d);
+        uint32_t pre = 0;
+        if (d < NBIN) pre = sm.whist[warp][d];
+        __syncwarp();
+        if (d < NBIN) {
+            rank[j] = pre + __popc(peers & lt);
+            if ((peers & lt) == 0) sm.whist[warp][d] = pre + __popc(peers);
+        }
+        __syncwarp();
+    }
+    __syncthreads();
+    // thread d: exclusive prefix of digit d over the warps, then over the digits; whist ends up
+    // holding each (warp, digit)'s first output position
+    uint32_t colsum = 0;
+    if (threadIdx.x < NBIN) {  // NBIN is a multiple of 32: whole warps take part in the shuffles
+        const uint32_t d = threadIdx.x;
+        for (int w = 0; w < SS_WARPS; w++) {
+            const uint32_t t = sm.whist[w][d];
+            sm.whist[w][d] = colsum;
+            colsum += t;
+        }
+        uint32_t x = colsum;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(FULLM, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) sm.wsum[warp] = x;
+        colsum = x - colsum;  // exclusive within this warp's 32 digits
+    }
+    __syncthreads();
+    if (threadIdx.x < NBIN) {
+        uint32_t before = colsum;
+        for (int w = 0; w < (int)(threadIdx.x >> 5); w++) before += sm.wsum[w];
+        for (int w = 0; w < SS_WARPS; w++) sm.whist[w][threadIdx.x] += before;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < SS_ITEMS; j++)
+        if (dg[j] < NBIN) sm.perm[cur ^ 1][sm.whist[warp][dg[j]] + rank[j]] = (uint16_t)src[j];
+    __syncthreads();
+}
+
+// Sort of one unit: key = (bucket - first bucket of the unit) << lowbits | low k-mer bits and adjacency.
+// Four stable passes -- the adjacency byte, then three bytes of the top 24 varying key bits --
+// leave every group of equal top bits ordered by (adjacency, input order).  A group holding one
+// k-mer (a single item, or the run of an abundant k-mer) is then in its final order.  Groups where
+// distinct k-mers interleave -- mostly a k-mer and its sequencing-error variants, which differ in
+// one low base -- are found in parallel, queued, and each finished by a warp that moves out its
+// k-mers in increasing order, each with its tuples in (adjacency, input order).  A unit with too
+// many such groups, or a group with too many distinct k-mers, goes through the full LSD sort over
+// its varying bytes instead.
 __global__ void __launch_bounds__(SS_THREADS) k_segsort(const uint64_t *__restrict__ ustart, const uint32_t *__restrict__ ucount,
                                                          const uint32_t *__restrict__ ubucket, const uint64_t *__restrict__ lo_in,
                                                          const uint8_t *__restrict__ hi_in, const uint32_t *__restrict__ id_in,
                                                          uint64_t *__restrict__ lo_out, uint32_t *__restrict__ id_out, int bsh,
-                                                         int lowbits)
+                                                         int lowbits, uint32_t force_full, unsigned long long *trace)
 {
     extern __shared__ __align__(16) unsigned char smraw[];
     SegSmem &sm = *reinterpret_cast<SegSmem *>(smraw);
@@ -331,91 +420,200 @@ __global__ void __launch_bounds__(SS_THREADS) k_segsort(const uint64_t *__restri
     const uint64_t start = ustart[blockIdx.x];
     const uint32_t cnt = ucount[blockIdx.x], b0 = ubucket[blockIdx.x];
     const uint64_t lowmask = (1ull << lowbits) - 1;
-    if (threadIdx.x == 0) { sm.kor = 0; sm.kand = ~0ull; }
+    long long tph[6] = {clock64(), 0, 0, 0, 0, 0};  // phase stamps (thread 0): start, loaded, passes, marks, groups, sorted
+    if (threadIdx.x == 0) {
+        sm.kor = 0;
+        sm.kand = ~0ull;
+        sm.fallback = 0;
+        sm.nlist = 0;
+    }
+    // all loads of the unit in flight at once
+    uint64_t lr[SS_ITEMS];
+    uint32_t hr[SS_ITEMS];
+#pragma unroll
+    for (int j = 0; j < SS_ITEMS; j++) {
+        const uint32_t e = threadIdx.x + j * SS_THREADS;
+        lr[j] = e < cnt ? lo_in[start + e] : 0ull;
+        hr[j] = (hi_in && e < cnt) ? (uint32_t)hi_in[start + e] : 0u;
+    }
     __syncthreads();
     unsigned long long kor = 0, kand = ~0ull;
-    for (uint32_t e = threadIdx.x; e < cnt; e += SS_THREADS) {
-        const uint64_t l = lo_in[start + e];
-        const uint64_t km = (l >> 8) | (hi_in ? ((uint64_t)hi_in[start + e] << 56) : 0ull);
-        const uint64_t key = ((uint64_t)((uint32_t)(km >> bsh) - b0) << lowbits) | (l & lowmask);
-        sm.key[e] = key;
-        sm.perm[0][e] = (uint16_t)e;
-        kor |= key;
-        kand &= key;
+#pragma unroll
+    for (int j = 0; j < SS_ITEMS; j++) {
+        const uint32_t e = threadIdx.x + j * SS_THREADS;
+        if (e < cnt) {
+            const uint64_t km = (lr[j] >> 8) | ((uint64_t)hr[j] << 56);
+            const uint64_t key = ((uint64_t)((uint32_t)(km >> bsh) - b0) << lowbits) | (lr[j] & lowmask);
+            sm.key[e] = key;
+            kor |= key;
+            kand &= key;
+        }
     }
 #pragma unroll
     for (int o = 16; o; o >>= 1) {
         kor |= __shfl_xor_sync(FULLM, kor, o);
         kand &= __shfl_xor_sync(FULLM, kand, o);
     }
-    if (lane == 0) { atomicOr(&sm.kor, kor); atomicAnd(&sm.kand, kand); }
-    __syncthreads();
-    const uint64_t varying = sm.kor ^ sm.kand;
-    int cur = 0;
-    const uint32_t lt = (1u << lane) - 1;
-    for (int dgt = 0; dgt < 8; dgt++) {
-        if (!((varying >> (8 * dgt)) & 0xFF)) continue;  // constant digit in this unit
-        for (int i = threadIdx.x; i < SS_WARPS * 256; i += SS_THREADS) (&sm.whist[0][0])[i] = 0;
-        __syncthreads();
-        uint32_t src[SS_ITEMS], dg[SS_ITEMS], rank[SS_ITEMS];
-#pragma unroll
-        for (int j = 0; j < SS_ITEMS; j++) {
-            const uint32_t e = warp * (32 * SS_ITEMS) + j * 32 + lane;
-            src[j] = e < cnt ? sm.perm[cur][e] : 0;
-            dg[j] = e < cnt ? (uint32_t)((sm.key[src[j]] >> (8 * dgt)) & 0xFF) : 256u;
-        }
-#pragma unroll
-        for (int j = 0; j < SS_ITEMS; j++) {
-            const uint32_t d = dg[j];
-            const uint32_t peers = __match_any_sync(FULLM, d);
-            uint32_t pre = 0;
-            if (d < 256) pre = sm.whist[warp][d];
-            __syncwarp();
-            if (d < 256) {
-                rank[j] = pre + __popc(peers & lt);
-                if ((peers & lt) == 0) sm.whist[warp][d] = pre + __popc(peers);
-            }
-            __syncwarp();
-        }
-        __syncthreads();
-        if (threadIdx.x < 256) {
-            const uint32_t d = threadIdx.x;
-            uint32_t r = 0;
-#pragma unroll
-            for (int w = 0; w < SS_WARPS; w++) {
-                const uint32_t t = sm.whist[w][d];
-                sm.whist[w][d] = r;
-                r += t;
-            }
-            // exclusive scan of the 256 digit totals over 8 warps
-            uint32_t x = r;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const uint32_t y = __shfl_up_sync(FULLM, x, o);
-                if (lane >= o) x += y;
-            }
-            if (lane == 31) sm.wsum[warp] = x;
-            sm.dstart[d] = x - r;  // warp-local exclusive part; warp offsets added below
-        }
-        __syncthreads();
-        if (threadIdx.x < 256) {
-            uint32_t before = 0;
-            for (int w = 0; w < warp; w++) before += sm.wsum[w];
-            sm.dstart[threadIdx.x] += before;
-        }
-        __syncthreads();
-#pragma unroll
-        for (int j = 0; j < SS_ITEMS; j++)
-            if (dg[j] < 256) sm.perm[cur ^ 1][sm.dstart[dg[j]] + sm.whist[warp][dg[j]] + rank[j]] = (uint16_t)src[j];
-        __syncthreads();
-        cur ^= 1;
+    if (lane == 0) {
+        atomicOr(&sm.kor, kor);
+        atomicAnd(&sm.kand, kand);
     }
+    __syncthreads();
+    tph[1] = tph[2] = tph[3] = tph[4] = clock64();
+    const uint64_t varying = sm.kor ^ sm.kand;
+    int cur = -1;  // -1: the identity order
+    if (varying) {
+        const int hb = 63 - __clzll((long long)varying);
+        // gl: lowest group bit.  With hb < 32 the passes cover every varying bit.
+        const int gl = hb >= 8 + SS_GPASSES * SS_GBITS ? hb + 1 - SS_GPASSES * SS_GBITS : 8;
+        int c = 0;
+        for (int ps = 0; ps <= SS_GPASSES; ps++) {
+            const int sh = ps == 0 ? 0 : gl + (ps - 1) * SS_GBITS;
+            const uint64_t bits = ps == 0 ? 0xFFull : ((1ull << SS_GBITS) - 1) << sh;
+            if (!(varying & bits)) continue;  // constant digit in this unit
+            if (ps == 0) seg_pass<8>(sm, c, cnt, 0, cur < 0);
+            else seg_pass<SS_GBITS>(sm, c, cnt, sh, cur < 0);
+            c ^= 1;
+            cur = c;
+        }
+        tph[2] = tph[3] = tph[4] = clock64();
+        if (gl > 8 && cur >= 0) {
+            const uint16_t *P = sm.perm[cur];
+            // group starts and out-of-order positions, one ballot word per warp and round
+#pragma unroll
+            for (int j = 0; j < SS_ITEMS; j++) {
+                const uint32_t p = (uint32_t)j * SS_THREADS + threadIdx.x;
+                bool gs = false, dt = false;
+                if (p < cnt) {
+                    const uint64_t kp = sm.key[P[p]];
+                    if (p == 0) {
+                        gs = true;
+                    } else {
+                        const uint64_t kq = sm.key[P[p - 1]];
+                        gs = (kq >> gl) != (kp >> gl);
+                        dt = !gs && kq > kp;
+                    }
+                }
+                const uint32_t wg = __ballot_sync(FULLM, gs), wd = __ballot_sync(FULLM, dt);
+                if (lane == 0) {
+                    sm.gstart[(j * SS_THREADS + warp * 32) >> 5] = wg;
+                    sm.dirty[(j * SS_THREADS + warp * 32) >> 5] = wd;
+                }
+            }
+            __syncthreads();
+            // queue the out-of-order groups whose start this thread holds
+            uint32_t ndirty = 0;
+            for (int j = 0; j < SS_ITEMS; j++) {
+                const uint32_t p = (uint32_t)j * SS_THREADS + threadIdx.x;
+                if (p >= cnt || !((sm.gstart[p >> 5] >> (p & 31)) & 1u)) continue;
+                // q: the next group start (or cnt); dirty: any out-of-order position in (p, q)
+                uint32_t q = cnt;
+                bool dirty = false;
+                uint32_t w = p >> 5;
+                uint32_t gm = sm.gstart[w] & ~((2u << (p & 31)) - 1);  // starts above p in its word
+                uint32_t dm = sm.dirty[w] & ~((2u << (p & 31)) - 1);
+                for (;;) {
+                    if (gm) {
+                        const uint32_t qq = (w << 5) + (uint32_t)(__ffs(gm) - 1);
+                        q = qq < cnt ? qq : cnt;
+                        dirty |= (dm & ((1u << (qq & 31)) - 1)) != 0;
+                        break;
+                    }
+                    dirty |= dm != 0;
+                    if (++w >= (uint32_t)SS_WORDS || (w << 5) >= cnt) break;
+                    gm = sm.gstart[w];
+                    dm = sm.dirty[w];
+                }
+                if (!dirty) continue;
+                ndirty++;
+                const uint32_t slot = atomicAdd(&sm.nlist, 1u);
+                if (slot < (uint32_t)SS_LIST) sm.list[slot] = p | (q << 16);
+                else sm.fallback = 1;
+            }
+            if (trace && ndirty) atomicAdd(&trace[1], (unsigned long long)ndirty);
+            if (force_full && threadIdx.x == 0) sm.fallback = 1;
+            __syncthreads();
+            tph[3] = clock64();
+            // a warp per queued group: repeatedly take the smallest k-mer above the last one and move
+            // its tuples out in their current order (the other perm buffer is the scratch)
+            const uint32_t nl = sm.fallback ? 0u : min(sm.nlist, (uint32_t)SS_LIST);
+            uint16_t *Pw = sm.perm[cur], *Tw = sm.perm[cur ^ 1];
+            uint32_t nmoves = 0;
+            for (uint32_t g = warp; g < nl; g += SS_WARPS) {
+                const uint32_t p = sm.list[g] & 0xFFFF, q = sm.list[g] >> 16;
+                uint32_t out = p;
+                uint64_t last = 0;
+                bool first = true, ok = false;
+                for (int round = 0; round < SS_MAX_KMERS; round++) {
+                    uint64_t mn = ~0ull;
+                    for (uint32_t i = p + lane; i < q; i += 32) {
+                        const uint64_t km = sm.key[Pw[i]] >> 8;
+                        if ((first || km > last) && km < mn) mn = km;
+                    }
+#pragma unroll
+                    for (int o = 16; o; o >>= 1) {
+                        const uint64_t y = __shfl_xor_sync(FULLM, mn, o);
+                        mn = y < mn ? y : mn;
+                    }
+                    if (mn == ~0ull) {
+                        ok = true;
+                        break;
+                    }
+                    for (uint32_t b = p; b < q; b += 32) {
+                        const uint32_t i = b + lane;
+                        uint16_t x = 0;
+                        bool sel = false;
+                        if (i < q) {
+                            x = Pw[i];
+                            sel = (sm.key[x] >> 8) == mn;
+                        }
+                        const uint32_t bal = __ballot_sync(FULLM, sel);
+                        if (sel) Tw[out + __popc(bal & ((1u << lane) - 1))] = x;
+                        out += __popc(bal);
+                    }
+                    last = mn;
+                    first = false;
+                    nmoves += q - p;
+                }
+                if (!ok) {
+                    if (lane == 0) sm.fallback = 1;
+                    continue;
+                }
+                __syncwarp();
+                for (uint32_t i = p + lane; i < q; i += 32) Pw[i] = Tw[i];
+                __syncwarp();
+            }
+            if (trace && lane == 0 && nmoves) atomicAdd(&trace[2], (unsigned long long)nmoves);
+            __syncthreads();
+            tph[4] = clock64();
+            if (sm.fallback) {  // uniform across the block
+                if (trace && threadIdx.x == 0) atomicAdd(&trace[0], 1ull);
+                cur = -1;
+                c = 0;
+                for (int dgt = 0; dgt < 8; dgt++) {
+                    if (!((varying >> (8 * dgt)) & 0xFF)) continue;
+                    seg_pass<8>(sm, c, cnt, 8 * dgt, cur < 0);
+                    c ^= 1;
+                    cur = c;
+                }
+            }
+        }
+    }
+    __syncthreads();
+    tph[5] = clock64();
     for (uint32_t e = threadIdx.x; e < cnt; e += SS_THREADS) {
-        const uint32_t sidx = sm.perm[cur][e];
+        const uint32_t sidx = cur < 0 ? e : (uint32_t)sm.perm[cur][e];
         const uint64_t key = sm.key[sidx];
         const uint64_t bucket = b0 + (key >> lowbits);
         lo_out[start + e] = (bucket << lowbits) | (key & lowmask);
         id_out[start + e] = id_in[start + sidx];
+    }
+    if (trace && threadIdx.x == 0) {  // cycles per phase, summed over units (the fallback counts with the groups)
+        atomicAdd(&trace[3], (unsigned long long)(tph[1] - tph[0]));
+        atomicAdd(&trace[4], (unsigned long long)(tph[2] - tph[1]));
+        atomicAdd(&trace[5], (unsigned long long)(tph[3] - tph[2]));
+        atomicAdd(&trace[6], (unsigned long long)(tph[5] - tph[3]));
+        atomicAdd(&trace[7], (unsigned long long)(clock64() - tph[5]));
     }
 }
 
@@ -447,6 +645,27 @@ __global__ void k_big_scatter(const uint64_t *__restrict__ bstart, const uint32_
     }
 }
 
+// MP_UNIT_SORT_FULL=1 sends every unit that has groups through the full shared-memory LSD sort
+// (used by the tests to cover that path on ordinary inputs).
+static uint32_t unit_sort_force_full()
+{
+    const char *e = getenv("MP_UNIT_SORT_FULL");
+    return e && *e && *e != '0' ? 1u : 0u;
+}
+
+static void sort_kernel_attrs()
+{
+    static std::once_flag once[64];
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::call_once(once[dev & 63], [] {
+        cudaFuncSetAttribute(k_onesweep<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SortSmem));
+        cudaFuncSetAttribute(k_onesweep<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SortSmem));
+        cudaFuncSetAttribute(k_onesweep<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SortSmem));
+        cudaFuncSetAttribute(k_segsort, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SegSmem));
+    });
+}
+
 int bucket_sort(SortBufs &b, uint64_t n, bool has_hi, int k, const uint64_t *hist, uint64_t scan_lo, uint64_t scan_hi,
                 DeviceArena &arena, cudaStream_t st, SortStats *stats, int *out_lo_buf, int *out_hi_buf)
 {
@@ -475,18 +694,16 @@ int bucket_sort(SortBufs &b, uint64_t n, bool has_hi, int k, const uint64_t *his
     const uint64_t tiles = (n + STILE - 1) / STILE;
     uint64_t *dbase = arena.alloc<uint64_t>(3 * 256);
     uint32_t *ctr = arena.alloc<uint32_t>(8), *err = arena.alloc<uint32_t>(1);
+    unsigned long long *trace = arena.alloc<unsigned long long>(8);
+    if (!trace) return set_error(MP_ENOMEM, "device memory for the bucket sort");
+    MP_CUDA(cudaMemsetAsync(trace, 0, 8 * sizeof(unsigned long long), st));
     unsigned long long *status = passes.empty() ? nullptr : arena.alloc<unsigned long long>(tiles * 256);
     if (!dbase || !ctr || !err || (!passes.empty() && !status)) return set_error(MP_ENOMEM, "device memory for the bucket sort");
     MP_CUDA(cudaMemcpyAsync(dbase, base.data(), base.size() * 8, cudaMemcpyHostToDevice, st));
     MP_CUDA(cudaMemsetAsync(ctr, 0, 8 * sizeof(uint32_t), st));
     MP_CUDA(cudaMemsetAsync(err, 0, sizeof(uint32_t), st));
     if (status) MP_CUDA(cudaMemsetAsync(status, 0, tiles * 256 * sizeof(unsigned long long), st));
-    static bool attr = false;
-    if (!attr) {
-        cudaFuncSetAttribute(k_onesweep<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SortSmem));
-        cudaFuncSetAttribute(k_segsort, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SegSmem));
-        attr = true;
-    }
+    sort_kernel_attrs();
     cudaEvent_t ev[5];
     for (auto &e : ev) cudaEventCreate(&e);
     cudaEventRecord(ev[0], st);
@@ -535,7 +752,8 @@ int bucket_sort(SortBufs &b, uint64_t n, bool has_hi, int k, const uint64_t *his
         MP_CUDA(cudaMemcpyAsync(d_uc, uc.data(), nu * 4, cudaMemcpyHostToDevice, st));
         MP_CUDA(cudaMemcpyAsync(d_ub, ub.data(), nu * 4, cudaMemcpyHostToDevice, st));
         (mp::count_launch(), k_segsort<<<(unsigned)nu, SS_THREADS, sizeof(SegSmem), st>>>(
-            d_us, d_uc, d_ub, b.lo[in], has_hi ? b.hi[in] : nullptr, b.id[in], b.lo[out], b.id[out], bsh, lowbits));
+            d_us, d_uc, d_ub, b.lo[in], has_hi ? b.hi[in] : nullptr, b.id[in], b.lo[out], b.id[out], bsh, lowbits,
+            unit_sort_force_full(), trace));
     }
     cudaEventRecord(ev[2], st);
     uint64_t nbig = 0;
@@ -575,6 +793,8 @@ int bucket_sort(SortBufs &b, uint64_t n, bool has_hi, int k, const uint64_t *his
         }
     }
     cudaEventRecord(ev[3], st);
+    unsigned long long ht[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    MP_CUDA(cudaMemcpyAsync(ht, trace, sizeof ht, cudaMemcpyDeviceToHost, st));
     uint32_t herr = 0;
     MP_CUDA(cudaMemcpyAsync(&herr, err, sizeof herr, cudaMemcpyDeviceToHost, st));
     MP_CUDA(cudaStreamSynchronize(st));
@@ -593,6 +813,10 @@ int bucket_sort(SortBufs &b, uint64_t n, bool has_hi, int k, const uint64_t *his
         stats->units = nu;
         stats->big_buckets = nb;
         stats->big_tuples = nbig;
+        stats->fallback_units = ht[0];
+        stats->dirty_groups = ht[1];
+        stats->moves = ht[2];
+        for (int q = 0; q < 5; q++) stats->phase_cycles[q] = ht[3 + q];
     }
     for (auto &e : ev) cudaEventDestroy(e);
     arena.free_scratch(status);
@@ -695,12 +919,7 @@ int sort_tuples_noalloc(const uint64_t *lo_in, const uint8_t *hi_in, const uint3
         return 0;
     }
     MP_CUDA(cudaMemcpyAsync(S->dbase, base, sizeof base, cudaMemcpyHostToDevice, st));
-    static bool attr = false;
-    if (!attr) {
-        MP_CUDA(cudaFuncSetAttribute(k_onesweep<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SortSmem)));
-        MP_CUDA(cudaFuncSetAttribute(k_onesweep<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SortSmem)));
-        attr = true;
-    }
+    sort_kernel_attrs();
     // pass i writes the caller's output when (np - 1 - i) is even, the scratch otherwise,
     // so the last pass always lands in the output
     const uint64_t *src_lo = lo_in;

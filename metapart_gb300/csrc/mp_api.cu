@@ -45,7 +45,7 @@ using namespace mp;
 struct mp_ctx {
     int device = 0;
     uint64_t budget = ~0ull;
-    uint64_t used = 0;
+    std::atomic<uint64_t> used{0};
     std::mutex mu;
 };
 
@@ -76,7 +76,9 @@ struct mp_job {
     int sort_passes_total = 0;
     double sort_ms_total = 0;
     uint64_t sort_bytes_total = 0, sort_tuples_total = 0;
-    double seg_ms_total = 0;
+    double seg_ms_total = 0, big_ms_total = 0;
+    uint64_t units_total = 0, big_buckets_total = 0, big_tuples_total = 0;
+    uint64_t fallback_total = 0, dirty_total = 0, moves_total = 0, phase_total[5] = {0, 0, 0, 0, 0};
     int pe_rounds = 0;
 };
 
@@ -211,14 +213,16 @@ int range_bounds(const uint64_t *hist, const uint64_t *ltr, int T, uint64_t scan
                  std::vector<uint64_t> &bounds)
 {
     std::vector<uint64_t> cnt(T, 0);
+    // cb + 1 is the first range start above b; it only moves forward as b grows
+    int cb = 0;
     for (uint64_t b = scan_lo; b < scan_hi; b++) {
         const uint64_t c = hist[b + 1] - hist[b];
         if (!c) continue;
-        int cb = 0;
         while (cb <= T && b >= ltr[cb]) cb++;
         cb--;
         if (cb < 0 || cb >= T) return set_error(MP_EUNSUP, "thread k-mer ranges do not cover bucket %llu", (unsigned long long)b);
         cnt[cb] += c;
+        cb++;
     }
     bounds.assign(T + 1, 0);
     for (int t = 0; t < T; t++) {
@@ -272,7 +276,7 @@ int mp_ctx_create(int device, uint64_t hbm_budget_bytes, mp_ctx **out)
 
 void mp_ctx_destroy(mp_ctx *ctx) { delete ctx; }
 
-uint64_t mp_ctx_hbm_in_use(const mp_ctx *ctx) { return ctx ? ctx->used : 0; }
+uint64_t mp_ctx_hbm_in_use(const mp_ctx *ctx) { return ctx ? ctx->used.load() : 0; }
 
 int mp_job_create(mp_ctx *ctx, mp_job **out)
 {
@@ -451,6 +455,10 @@ int mp_job_partition(mp_job *j, const mp_part_params *p, const uint64_t *chunk_s
     j->sort_bytes_total = 0;
     j->sort_tuples_total = 0;
     j->seg_ms_total = 0;
+    j->big_ms_total = 0;
+    j->units_total = j->big_buckets_total = j->big_tuples_total = 0;
+    j->fallback_total = j->dirty_total = j->moves_total = 0;
+    for (auto &v : j->phase_total) v = 0;
     if (j->d_parent) { j->arena.free_persistent(j->d_parent); j->d_parent = nullptr; }
     if (j->d_size) { j->arena.free_persistent(j->d_size); j->d_size = nullptr; }
     if (j->d_filtered) { j->arena.free_persistent(j->d_filtered); j->d_filtered = nullptr; }
@@ -466,10 +474,27 @@ int mp_job_partition(mp_job *j, const mp_part_params *p, const uint64_t *chunk_s
     MP_CUDA(cudaMemsetAsync(err, 0, 4, j->st));
     const bool has_hi = 2 * k + 8 > 64;
     char name[64], name2[64];
+    // tuples per read of every scan in one pass (plain variant, monotone scan bounds)
+    uint32_t *cnt_all = nullptr, *d_b = nullptr;
+    {
+        bool mono = !p->min3 && S <= 8;
+        for (int s = 0; s < S && mono; s++) mono = scanR[s] <= scanR[s + 1];
+        if (mono) {
+            cnt_all = j->arena.alloc_persistent<uint32_t>((size_t)S * (N + 1));
+            d_b = j->arena.alloc_persistent<uint32_t>(S + 1);
+            if (!cnt_all || !d_b) return set_error(MP_ENOMEM, "device memory for enumeration counts");
+            std::vector<uint32_t> hb(scanR.begin(), scanR.end());
+            StageTimer tm(j->st, &j->stage_ms[2]);
+            MP_CUDA(cudaMemcpyAsync(d_b, hb.data(), (S + 1) * 4, cudaMemcpyHostToDevice, j->st));
+            if (launch_enum_count_scans(j->d_fq, j->pr, k, d_b, S, cnt_all, N + 1, err, j->st))
+                return set_error(MP_EARG, "enumeration count over %d scans", S);
+            for (int s = 0; s < S; s++) MP_CUDA(cudaMemsetAsync(cnt_all + (size_t)s * (N + 1) + N, 0, 4, j->st));
+        }
+    }
     for (int s = 0; s < S; s++) {
         const uint64_t lo = scanR[s], hi = scanR[s + 1];
         const uint64_t expect = hist[hi] - hist[lo];
-        uint32_t *cnt = j->arena.alloc<uint32_t>(N + 1);
+        uint32_t *cnt = cnt_all ? cnt_all + (size_t)s * (N + 1) : j->arena.alloc<uint32_t>(N + 1);
         uint64_t *off = j->arena.alloc<uint64_t>(N + 2), *ntot = j->arena.alloc<uint64_t>(1);
         size_t tb = scan_tmp_bytes(N + 1);
         void *tmp = j->arena.alloc<uint8_t>(tb);
@@ -479,8 +504,10 @@ int mp_job_partition(mp_job *j, const mp_part_params *p, const uint64_t *chunk_s
         uint64_t n = 0;
         {
             StageTimer tm(j->st, &j->stage_ms[2]);
-            launch_enum_count(j->d_fq, j->pr, k, p->min3, (uint32_t)lo, (uint32_t)hi, cnt, err, j->st);
-            MP_CUDA(cudaMemsetAsync(cnt + N, 0, 4, j->st));
+            if (!cnt_all) {
+                launch_enum_count(j->d_fq, j->pr, k, p->min3, (uint32_t)lo, (uint32_t)hi, cnt, err, j->st);
+                MP_CUDA(cudaMemsetAsync(cnt + N, 0, 4, j->st));
+            }
             scan_u32_to_u64(cnt, off, N + 1, ntot, tmp, tb, j->st);
             uint32_t cerr = 0;
             MP_CUDA(cudaMemcpyAsync(&n, ntot, 8, cudaMemcpyDeviceToHost, j->st));
@@ -522,7 +549,15 @@ int mp_job_partition(mp_job *j, const mp_part_params *p, const uint64_t *chunk_s
             j->sort_ms_total += ss.pass_ms;
             j->sort_bytes_total += ss.bytes;
             j->sort_tuples_total += n;
-            j->seg_ms_total += ss.seg_ms + ss.big_ms;
+            j->seg_ms_total += ss.seg_ms;
+            j->big_ms_total += ss.big_ms;
+            j->units_total += ss.units;
+            j->big_buckets_total += ss.big_buckets;
+            j->big_tuples_total += ss.big_tuples;
+            j->fallback_total += ss.fallback_units;
+            j->dirty_total += ss.dirty_groups;
+            j->moves_total += ss.moves;
+            for (int q = 0; q < 5; q++) j->phase_total[q] += ss.phase_cycles[q];
         }
         Tuples tp;
         tp.lo = sb.lo[lo_buf];
@@ -554,6 +589,8 @@ int mp_job_partition(mp_job *j, const mp_part_params *p, const uint64_t *chunk_s
         snprintf(name, sizeof name, "stats%d_parent.bin", s);
         if ((rc = dump_state(j, name, nullptr))) return rc;
     }
+    j->arena.free_persistent(cnt_all);
+    j->arena.free_persistent(d_b);
     {
         StageTimer tm(j->st, &j->stage_ms[6]);
         if (!j->dump_dir.empty()) {
@@ -626,6 +663,25 @@ int mp_job_sort_stats(const mp_job *j, uint64_t *tuples, int *passes, double *pa
     if (passes) *passes = j->sort_passes_total;
     if (pass_ms) *pass_ms = j->sort_ms_total;
     if (bytes) *bytes = j->sort_bytes_total;
+    return 0;
+}
+
+int mp_job_sort_split(const mp_job *j, double *pass_ms, double *unit_ms, double *big_ms, uint64_t *units,
+                      uint64_t *big_buckets, uint64_t *big_tuples, uint64_t *unit_counters)
+{
+    if (!j) return set_error(MP_EARG, "null job");
+    if (unit_counters) {
+        unit_counters[0] = j->fallback_total;
+        unit_counters[1] = j->dirty_total;
+        unit_counters[2] = j->moves_total;
+        for (int q = 0; q < 5; q++) unit_counters[3 + q] = j->phase_total[q];
+    }
+    if (pass_ms) *pass_ms = j->sort_ms_total;
+    if (unit_ms) *unit_ms = j->seg_ms_total;
+    if (big_ms) *big_ms = j->big_ms_total;
+    if (units) *units = j->units_total;
+    if (big_buckets) *big_buckets = j->big_buckets_total;
+    if (big_tuples) *big_tuples = j->big_tuples_total;
     return 0;
 }
 

@@ -57,6 +57,8 @@ def lib():
         L.mp_job_set_dump_dir.argtypes = [C.c_void_p, C.c_char_p]
         L.mp_job_stage_ms.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.c_int]
         L.mp_job_sort_stats.argtypes = [C.c_void_p, u64p, C.POINTER(C.c_int), C.POINTER(C.c_double), u64p]
+        L.mp_job_sort_split.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                        C.POINTER(C.c_double), u64p, u64p, u64p, u64p]
         L.mp_sort_tuples.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                      C.c_void_p, C.c_uint64, C.c_void_p]
         _lib = L
@@ -232,6 +234,17 @@ class Job:
         p, ms = C.c_int(), C.c_double()
         _check(lib().mp_job_sort_stats(self.h, C.byref(t), C.byref(p), C.byref(ms), C.byref(b)), "sort_stats")
         return {"tuples": t.value, "passes": p.value, "pass_ms": ms.value, "bytes": b.value}
+
+    def sort_split(self) -> dict:
+        a, u, g = C.c_double(), C.c_double(), C.c_double()
+        nu, nb, nt = C.c_uint64(), C.c_uint64(), C.c_uint64()
+        uc = (C.c_uint64 * 8)()
+        _check(lib().mp_job_sort_split(self.h, C.byref(a), C.byref(u), C.byref(g), C.byref(nu), C.byref(nb),
+                                       C.byref(nt), uc), "sort_split")
+        return {"digit_pass_ms": a.value, "unit_sort_ms": u.value, "big_bucket_ms": g.value, "units": nu.value,
+                "big_buckets": nb.value, "big_tuples": nt.value, "fallback_units": uc[0], "mixed_groups": uc[1],
+                "mixed_group_moves": uc[2], "unit_cycles": {"load": uc[3], "passes": uc[4], "mark": uc[5],
+                                                              "groups": uc[6], "store": uc[7]}}
 
 
 def fastq_index_ptr(num_chunks: int, host_ptr: int, nbytes: int, interleaved: bool = False):

@@ -115,6 +115,21 @@ def fastq_bytes(spec: ReadSpec) -> bytes:
         lib.mp_synth_free(p)
 
 
+def fastq_to(spec: ReadSpec, alloc):
+    """Generates into a caller buffer: alloc(nbytes) returns (buffer object, host address)."""
+    lib = _load()
+    p, n = C.c_void_p(), C.c_size_t()
+    rc = lib.mp_synth_fastq(C.byref(spec._c()), C.byref(p), C.byref(n))
+    if rc:
+        raise RuntimeError(f"mp_synth_fastq failed: {rc}")
+    try:
+        obj, addr = alloc(n.value)
+        C.memmove(addr, p.value, n.value)
+        return obj
+    finally:
+        lib.mp_synth_free(p)
+
+
 def write_fastq(spec: ReadSpec, path: str | Path) -> int:
     lib = _load()
     n = C.c_size_t()
@@ -144,3 +159,35 @@ def workload(name: str, n_reads: int | None = None, seed: int = 7) -> ReadSpec:
         return ReadSpec(n_reads=n_reads or 20_000, lengths=(100,), n_genomes=10, glen=(40_000, 40_000),
                         sub_rate=0.005, qual="#J", interleaved=True, insert_len=300, seed=seed)
     raise KeyError(name)
+
+
+def _loguniform_even(rng, lo: int, hi: int) -> int:
+    import math
+    n = int(math.exp(rng.uniform(math.log(lo), math.log(hi))))
+    return max(2, n - (n % 2))
+
+
+def serving_mix(n_jobs: int, seed: int = 11, min_reads: int = 10_000, max_reads: int = 2_000_000) -> list:
+    """Partition requests: read counts log-uniform in [min_reads, max_reads] (even), 150 bp, 5-50 genomes of
+    0.5-3 Mb each, log-normal abundance sigma 1.5, 1 % substitutions."""
+    import random
+    rng = random.Random(seed)
+    return [ReadSpec(n_reads=_loguniform_even(rng, min_reads, max_reads), lengths=(150,),
+                     n_genomes=rng.randint(5, 50), glen=(5e5, 3e6), gc=(0.35, 0.65), abundance=AB_LOGNORMAL,
+                     ab_param=1.5, sub_rate=0.01, qual="I", seed=seed * 1000 + i) for i in range(n_jobs)]
+
+
+def batch_mix(n_samples: int = 64, seed: int = 5, min_reads: int = 50_000, max_reads: int = 5_000_000,
+              scale: float = 1.0) -> list:
+    """Independent samples: read counts log-uniform in [min_reads, max_reads] (even; times scale), read
+    length one of 100/150/250, 10-100 genomes of 0.5-3 Mb, log-normal abundance sigma 1.5, 1 % substitutions."""
+    import random
+    rng = random.Random(seed)
+    out = []
+    for i in range(n_samples):
+        n = _loguniform_even(rng, min_reads, max_reads)
+        n = max(2, int(n * scale) // 2 * 2)
+        out.append(ReadSpec(n_reads=n, lengths=(rng.choice((100, 150, 250)),), n_genomes=rng.randint(10, 100),
+                            glen=(5e5, 3e6), gc=(0.35, 0.65), abundance=AB_LOGNORMAL, ab_param=1.5, sub_rate=0.01,
+                            qual="I", seed=seed * 1000 + i))
+    return out

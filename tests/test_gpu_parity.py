@@ -22,6 +22,8 @@ CASES = [
     ("plain_small", 20000, pu.Params(k=21, chunks=4, scans=1, threads=2, min3=True)),
     ("hotspot", 60000, pu.Params(k=31, chunks=4, scans=1, threads=2)),
     ("hotspot", 40000, pu.Params(k=25, chunks=6, scans=2, threads=3)),
+    ("plain_small", 20000, pu.Params(k=11, chunks=4, scans=2, threads=2)),
+    ("plain_small", 20000, pu.Params(k=13, chunks=4, scans=1, threads=4)),
     ("interleaved_small", 20000, pu.Params(k=27, chunks=4, scans=1, threads=2, interleaved=True)),
     ("interleaved_small", 20000, pu.Params(k=25, chunks=8, scans=2, threads=2, interleaved=True)),
 ]
@@ -43,15 +45,31 @@ def _keys(res, p):
     return ks
 
 
-@pytest.mark.parametrize("name,n,p", CASES, ids=[f"{c[0]}-k{c[2].k}-s{c[2].scans}-t{c[2].threads}" for c in CASES])
-def test_gpu_matches_oracle(tmp_path, built_gpu, name, n, p):
+def _compare(tmp_path, name, n, p, env_extra=None):
     fq = tmp_path / "in.fastq"
     synth.write_fastq(synth.workload(name, n, seed=11), fq)
     do = pu.run("oracle", tmp_path, [fq], p)
-    dg = pu.run("gpu", tmp_path, [fq], p)
+    dg = pu.run("gpu", tmp_path, [fq], p, env_extra=env_extra)
     a, b = pu.outputs(do, p, "in.fastq"), pu.outputs(dg, p, "in.fastq")
     keys = _keys(a, p)
     missing = [k for k in keys if k not in b]
     assert not missing, f"GPU run did not produce {missing}"
     diff = pu.diff_keys(a, b, keys)
     assert not diff, f"GPU output differs from the oracle in {diff}"
+
+
+@pytest.mark.parametrize("name,n,p", CASES, ids=[f"{c[0]}-k{c[2].k}-s{c[2].scans}-t{c[2].threads}" for c in CASES])
+def test_gpu_matches_oracle(tmp_path, built_gpu, name, n, p):
+    _compare(tmp_path, name, n, p)
+
+
+# Every bucket unit with groups goes through the full shared-memory LSD sort instead of the group passes.
+FALLBACK = [
+    ("plain_large", 30000, pu.Params(k=31, chunks=4, scans=2, threads=2)),
+    ("hotspot", 40000, pu.Params(k=27, chunks=4, scans=1, threads=2)),
+]
+
+
+@pytest.mark.parametrize("name,n,p", FALLBACK, ids=[f"{c[0]}-k{c[2].k}" for c in FALLBACK])
+def test_gpu_unit_sort_fallback(tmp_path, built_gpu, name, n, p):
+    _compare(tmp_path, name, n, p, env_extra={"MP_UNIT_SORT_FULL": "1"})
