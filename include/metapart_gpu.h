@@ -202,10 +202,8 @@ int mp_job_sort_stats(const mp_job *job, uint64_t *tuples, int *passes, double *
 
 /* Where the last partition's sort time went, summed over its scans: the m-mer bucket digit passes, the
  * shared-memory sort of bucket units, and the buckets too large for a unit (ms, and their counts);
- * unit_counters (nullable, 8 entries): units sorted by the full shared-memory LSD fallback, groups
- * of interleaved distinct k-mers finished by a warp, tuples those warps moved, then the unit sort's
- * SM cycles summed over units in its load, digit passes, group marking, group finishing (and
- * fallback) and store phases.  Tracing only; no counterpart in the reference. */
+ * unit_counters (nullable, 4 entries): the unit sort's digit passes and its SM cycles in the load,
+ * digit-pass and store phases, each summed over units.  Tracing only; no counterpart in the reference. */
 int mp_job_sort_split(const mp_job *job, double *pass_ms, double *unit_ms, double *big_ms, uint64_t *units,
                       uint64_t *big_buckets, uint64_t *big_tuples, uint64_t *unit_counters);
 

@@ -39,6 +39,15 @@ struct SortSmem {
     uint32_t nvalid;
 };
 
+__device__ __forceinline__ void prefetch_l2(const void *p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
+
+// One 128-byte-line prefetch per line of [p, p + bytes), spread over a block of `threads`.
+__device__ __forceinline__ void prefetch_range(const void *p, uint64_t bytes, int threads)
+{
+    for (uint64_t off = (uint64_t)threadIdx.x * 128; off < bytes; off += (uint64_t)threads * 128)
+        prefetch_l2((const char *)p + off);
+}
+
 __device__ __forceinline__ unsigned long long ld_relaxed(const unsigned long long *p)
 {
     unsigned long long v;
@@ -74,6 +83,7 @@ __global__ void __launch_bounds__(256) k_hist_upfront(const uint64_t *__restrict
 // 2 = byte of the k-mer value (lo >> 8 | hi << 56) at `shift` (the m-mer bucket digits).
 // Opt-in shared memory sizes of the sort kernels, set once per device (thread-safe).
 static void sort_kernel_attrs();
+static int sm_count();
 
 template <int SRC>
 __device__ __forceinline__ uint32_t digit_of(uint64_t lo, uint32_t hi, int shift)
@@ -89,7 +99,7 @@ __global__ void __launch_bounds__(ST, 2) k_onesweep(const uint64_t *__restrict__
                                                     uint8_t *__restrict__ out_hi, uint32_t *__restrict__ out_id, uint64_t n,
                                                     int shift, const uint64_t *__restrict__ dbase,
                                                     unsigned long long *status, uint32_t *tile_ctr, uint32_t epoch,
-                                                    uint32_t *err)
+                                                    uint32_t *err, uint32_t pf_tiles)
 {
     extern __shared__ __align__(16) unsigned char smraw[];
     SortSmem &sm = *reinterpret_cast<SortSmem *>(smraw);
@@ -100,6 +110,15 @@ __global__ void __launch_bounds__(ST, 2) k_onesweep(const uint64_t *__restrict__
     const uint64_t tile = sm.tile_id;
     const uint64_t base = tile * STILE;
     const bool has_hi = in_hi != nullptr;
+    if (pf_tiles) {  // the tile that starts pf_tiles later (about one wave of resident tiles) into L2
+        const uint64_t pb = base + (uint64_t)pf_tiles * STILE;
+        if (pb < n) {
+            const uint64_t pn = min((uint64_t)STILE, n - pb);
+            prefetch_range(in_lo + pb, pn * 8, ST);
+            prefetch_range(in_id + pb, pn * 4, ST);
+            if (has_hi) prefetch_range(in_hi + pb, pn, ST);
+        }
+    }
 
     uint64_t key[SI];
     uint32_t val[SI], rd[SI];  // rd: rank within the warp's digit (bits 0-15) | digit (bits 16-24, 256 = none)
@@ -159,6 +178,21 @@ __global__ void __launch_bounds__(ST, 2) k_onesweep(const uint64_t *__restrict__
         uint32_t before = 0;
         for (int w = 0; w < warp; w++) before += sm.wsum[w];
         sm.tstart[d] = before + x - cnt;
+    }
+    if (threadIdx.x == 0) sm.nvalid = (uint32_t)min((uint64_t)STILE, n - base);
+    __syncthreads();
+    // tile order in shared memory first: the look-back below then finds more predecessors done
+#pragma unroll
+    for (int j = 0; j < SI; j++) {
+        const uint32_t dd = rd[j] >> 16;
+        if (dd < 256) {
+            const uint32_t s = sm.tstart[dd] + sm.whist[warp][dd] + (rd[j] & 0xFFFF);
+            sm.keys[s] = key[j];
+            sm.vals[s] = val[j];
+            if (has_hi) sm.his[s] = (uint8_t)(hv[j >> 2] >> (8 * (j & 3)));
+        }
+    }
+    if (dig) {
         // decoupled look-back for digit d
         const unsigned long long E = (unsigned long long)epoch << 60, PF = 1ull << 59, CM = PF - 1;
         unsigned long long excl = 0;
@@ -181,18 +215,6 @@ __global__ void __launch_bounds__(ST, 2) k_onesweep(const uint64_t *__restrict__
             st_relaxed(status + tile * 256 + d, E | PF | (excl + cnt));
         }
         sm.gbase[d] = dbase[d] + excl;
-    }
-    if (threadIdx.x == 0) sm.nvalid = (uint32_t)min((uint64_t)STILE, n - base);
-    __syncthreads();
-#pragma unroll
-    for (int j = 0; j < SI; j++) {
-        const uint32_t dd = rd[j] >> 16;
-        if (dd < 256) {
-            const uint32_t s = sm.tstart[dd] + sm.whist[warp][dd] + (rd[j] & 0xFFFF);
-            sm.keys[s] = key[j];
-            sm.vals[s] = val[j];
-            if (has_hi) sm.his[s] = (uint8_t)(hv[j >> 2] >> (8 * (j & 3)));
-        }
     }
     __syncthreads();
     const uint32_t nv = sm.nvalid;
@@ -253,6 +275,7 @@ int radix_sort(SortBufs &b, uint64_t n, bool has_hi, DeviceArena &arena, cudaStr
     }
     MP_CUDA(cudaMemcpyAsync(dbase, base.data(), base.size() * sizeof(uint64_t), cudaMemcpyHostToDevice, st));
     sort_kernel_attrs();
+    const uint32_t pf = 2u * (uint32_t)sm_count();  // resident tiles: the prefetch distance
     std::vector<cudaEvent_t> ev(passes.size() + 1);
     for (auto &e : ev) cudaEventCreate(&e);
     cudaEventRecord(ev[0], st);
@@ -264,11 +287,11 @@ int radix_sort(SortBufs &b, uint64_t n, bool has_hi, DeviceArena &arena, cudaStr
         if (dgt < 8)
             (mp::count_launch(), k_onesweep<0><<<(unsigned)tiles, ST, sizeof(SortSmem), st>>>(b.lo[src], ih, b.id[src], b.lo[dst], oh,
                                                                          b.id[dst], n, 8 * dgt, dbase + dgt * 256, status,
-                                                                         ctr + pi, (uint32_t)(pi + 1), err));
+                                                                         ctr + pi, (uint32_t)(pi + 1), err, pf));
         else
             (mp::count_launch(), k_onesweep<1><<<(unsigned)tiles, ST, sizeof(SortSmem), st>>>(b.lo[src], ih, b.id[src], b.lo[dst], oh,
                                                                          b.id[dst], n, 0, dbase + dgt * 256, status,
-                                                                         ctr + pi, (uint32_t)(pi + 1), err));
+                                                                         ctr + pi, (uint32_t)(pi + 1), err, pf));
         cudaEventRecord(ev[pi + 1], st);
         b.cur = dst;
     }
@@ -311,309 +334,190 @@ int radix_sort(SortBufs &b, uint64_t n, bool has_hi, DeviceArena &arena, cudaStr
 
 constexpr int SS_THREADS = 1024;
 constexpr int SS_ITEMS = 12;
-constexpr int SS_CAP = SS_THREADS * SS_ITEMS;  // 12288 tuples per unit (about 180 KB of shared memory)
+constexpr int SS_CAP = SS_THREADS * SS_ITEMS;  // 12288 tuples per unit
 constexpr int SS_WARPS = SS_THREADS / 32;
 constexpr uint32_t SS_MAXB = 4096;             // buckets per unit
-
-constexpr int SS_GBITS = 8;             // bits per grouping pass: three passes group a unit by its top 24 varying bits
-constexpr int SS_GPASSES = 3;
-constexpr int SS_WORDS = SS_CAP / 32;
-
-constexpr int SS_LIST = 4096;           // out-of-order groups a unit may queue for the warps
-constexpr int SS_MAX_KMERS = 64;        // distinct k-mers a warp separates in one out-of-order group
+constexpr int SS_MAXBITS = 10;                 // widest digit of the unit sort
+constexpr int SS_BINS = 1 << SS_MAXBITS;
 
 struct SegSmem {
-    uint64_t key[SS_CAP];
-    uint16_t perm[2][SS_CAP];
-    uint32_t whist[SS_WARPS][256];
+    uint64_t key[SS_CAP];                // 96 KB
+    uint16_t perm[2][SS_CAP];            // 48 KB
+    uint16_t whist[SS_WARPS][SS_BINS];   // 64 KB: digit counts per warp, then each (warp, digit)'s first position
     uint32_t wsum[SS_WARPS];
-    uint32_t gstart[SS_WORDS];  // bit p: position p starts a group
-    uint32_t dirty[SS_WORDS];   // bit p: position p is out of order within its group
-    uint32_t list[SS_LIST];     // out-of-order groups: start | end << 16
     unsigned long long kor, kand;
-    uint32_t fallback, nlist;
 };
 
 // One stable counting-sort pass over a unit: perm[cur] (or the identity) -> perm[cur ^ 1] by the
-// digit (key >> sh) & (2^BITS - 1).  Items are ranked in warp-blocked order; a warp finds the lanes
-// holding its digit with match_any, so equal digits keep their order.
-template <int BITS>
-__device__ void seg_pass(SegSmem &sm, int cur, uint32_t cnt, int sh, bool identity)
+// digit (key >> sh) & mask, nbins = a power of two >= 32 covering the mask.  Items are ranked in
+// warp-blocked order with match_any, so equal digits keep their order.
+__device__ void seg_pass(SegSmem &sm, int cur, uint32_t cnt, int sh, uint32_t mask, uint32_t nbins, bool identity)
 {
-    constexpr uint32_t NBIN = 1u << BITS, MASK = NBIN - 1;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t lt = (1u << lane) - 1;
-    for (uint32_t i = threadIdx.x; i < SS_WARPS * NBIN; i += SS_THREADS) sm.whist[i / NBIN][i % NBIN] = 0;
+    {
+        uint32_t *w32 = reinterpret_cast<uint32_t *>(&sm.whist[0][0]);
+        const uint32_t words = nbins / 2;  // per warp row
+        for (uint32_t i = threadIdx.x; i < SS_WARPS * words; i += SS_THREADS)
+            w32[(i / words) * (SS_BINS / 2) + (i % words)] = 0;
+    }
     __syncthreads();
-    uint32_t src[SS_ITEMS], dg[SS_ITEMS], rank[SS_ITEMS];
+    uint32_t src[SS_ITEMS], rd[SS_ITEMS];  // rd: rank (bits 0-15) | digit (bits 16-27; nbins = none)
 #pragma unroll
     for (int j = 0; j < SS_ITEMS; j++) {
         const uint32_t e = warp * (32 * SS_ITEMS) + j * 32 + lane;
         const bool v = e < cnt;
         src[j] = v ? (identity ? e : (uint32_t)sm.perm[cur][e]) : 0u;
-        dg[j] = v ? (uint32_t)((sm.key[src[j]] >> sh) & MASK) : NBIN;
+        rd[j] = (v ? (uint32_t)((sm.key[src[j]] >> sh) & mask) : nbins) << 16;
     }
 #pragma unroll
     for (int j = 0; j < SS_ITEMS; j++) {
-        const uint32_t d = dg[j];
+        const uint32_t d = rd[j] >> 16;
         const uint32_t peers = __match_any_sync(FULLM, d);
         uint32_t pre = 0;
-        if (d < NBIN) pre = sm.whist[warp][d];
+        if (d < nbins) pre = sm.whist[warp][d];
         __syncwarp();
-        if (d < NBIN) {
-            rank[j] = pre + __popc(peers & lt);
-            if ((peers & lt) == 0) sm.whist[warp][d] = pre + __popc(peers);
+        if (d < nbins) {
+            rd[j] |= pre + __popc(peers & lt);
+            if ((peers & lt) == 0) sm.whist[warp][d] = (uint16_t)(pre + __popc(peers));
         }
         __syncwarp();
     }
     __syncthreads();
-    // thread d: exclusive prefix of digit d over the warps, then over the digits; whist ends up
-    // holding each (warp, digit)'s first output position
-    uint32_t colsum = 0;
-    if (threadIdx.x < NBIN) {  // NBIN is a multiple of 32: whole warps take part in the shuffles
-        const uint32_t d = threadIdx.x;
-        for (int w = 0; w < SS_WARPS; w++) {
-            const uint32_t t = sm.whist[w][d];
-            sm.whist[w][d] = colsum;
-            colsum += t;
+    // thread d: exclusive prefix of digit d over the warps, then over the digits
+    uint32_t colsum = 0, x = 0;
+    const uint32_t d = threadIdx.x;
+    if (d < nbins) {  // nbins is a multiple of 32: whole warps take part in the shuffles
+#pragma unroll
+        for (int w0 = 0; w0 < SS_WARPS; w0 += 8) {
+            uint32_t t[8];
+#pragma unroll
+            for (int i = 0; i < 8; i++) t[i] = sm.whist[w0 + i][d];
+#pragma unroll
+            for (int i = 0; i < 8; i++) {
+                sm.whist[w0 + i][d] = (uint16_t)colsum;
+                colsum += t[i];
+            }
         }
-        uint32_t x = colsum;
+        x = colsum;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
             const uint32_t y = __shfl_up_sync(FULLM, x, o);
             if (lane >= o) x += y;
         }
         if (lane == 31) sm.wsum[warp] = x;
-        colsum = x - colsum;  // exclusive within this warp's 32 digits
     }
     __syncthreads();
-    if (threadIdx.x < NBIN) {
-        uint32_t before = colsum;
-        for (int w = 0; w < (int)(threadIdx.x >> 5); w++) before += sm.wsum[w];
-        for (int w = 0; w < SS_WARPS; w++) sm.whist[w][threadIdx.x] += before;
+    if (d < nbins) {
+        uint32_t before = x - colsum;
+        for (int w = 0; w < warp; w++) before += sm.wsum[w];
+#pragma unroll
+        for (int w = 0; w < SS_WARPS; w++) sm.whist[w][d] = (uint16_t)(sm.whist[w][d] + before);
     }
     __syncthreads();
 #pragma unroll
-    for (int j = 0; j < SS_ITEMS; j++)
-        if (dg[j] < NBIN) sm.perm[cur ^ 1][sm.whist[warp][dg[j]] + rank[j]] = (uint16_t)src[j];
+    for (int j = 0; j < SS_ITEMS; j++) {
+        const uint32_t dd = rd[j] >> 16;
+        if (dd < nbins) sm.perm[cur ^ 1][sm.whist[warp][dd] + (rd[j] & 0xFFFF)] = (uint16_t)src[j];
+    }
     __syncthreads();
 }
 
-// Sort of one unit: key = (bucket - first bucket of the unit) << lowbits | low k-mer bits and adjacency.
-// Four stable passes -- the adjacency byte, then three bytes of the top 24 varying key bits --
-// leave every group of equal top bits ordered by (adjacency, input order).  A group holding one
-// k-mer (a single item, or the run of an abundant k-mer) is then in its final order.  Groups where
-// distinct k-mers interleave -- mostly a k-mer and its sequencing-error variants, which differ in
-// one low base -- are found in parallel, queued, and each finished by a warp that moves out its
-// k-mers in increasing order, each with its tuples in (adjacency, input order).  A unit with too
-// many such groups, or a group with too many distinct k-mers, goes through the full LSD sort over
-// its varying bytes instead.
+// Sort of the units, one persistent block per SM: key = (bucket - first bucket of the unit) << lowbits |
+// low k-mer bits and adjacency, stable LSD over the key's varying bits in digits of at most max_bits
+// (equal widths, so 53 varying bits take six passes).  While a unit is sorted, the next unit of this
+// block is prefetched into L2.  trace (nullable): [0] digit passes, [1..3] SM cycles in load, passes, store.
 __global__ void __launch_bounds__(SS_THREADS) k_segsort(const uint64_t *__restrict__ ustart, const uint32_t *__restrict__ ucount,
-                                                         const uint32_t *__restrict__ ubucket, const uint64_t *__restrict__ lo_in,
-                                                         const uint8_t *__restrict__ hi_in, const uint32_t *__restrict__ id_in,
-                                                         uint64_t *__restrict__ lo_out, uint32_t *__restrict__ id_out, int bsh,
-                                                         int lowbits, uint32_t force_full, unsigned long long *trace)
+                                                         const uint32_t *__restrict__ ubucket, uint32_t nunits,
+                                                         const uint64_t *__restrict__ lo_in, const uint8_t *__restrict__ hi_in,
+                                                         const uint32_t *__restrict__ id_in, uint64_t *__restrict__ lo_out,
+                                                         uint32_t *__restrict__ id_out, int bsh, int lowbits, int max_bits,
+                                                         unsigned long long *trace)
 {
     extern __shared__ __align__(16) unsigned char smraw[];
     SegSmem &sm = *reinterpret_cast<SegSmem *>(smraw);
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const uint64_t start = ustart[blockIdx.x];
-    const uint32_t cnt = ucount[blockIdx.x], b0 = ubucket[blockIdx.x];
+    const int lane = threadIdx.x & 31;
     const uint64_t lowmask = (1ull << lowbits) - 1;
-    long long tph[6] = {clock64(), 0, 0, 0, 0, 0};  // phase stamps (thread 0): start, loaded, passes, marks, groups, sorted
-    if (threadIdx.x == 0) {
-        sm.kor = 0;
-        sm.kand = ~0ull;
-        sm.fallback = 0;
-        sm.nlist = 0;
-    }
-    // all loads of the unit in flight at once
-    uint64_t lr[SS_ITEMS];
-    uint32_t hr[SS_ITEMS];
-#pragma unroll
-    for (int j = 0; j < SS_ITEMS; j++) {
-        const uint32_t e = threadIdx.x + j * SS_THREADS;
-        lr[j] = e < cnt ? lo_in[start + e] : 0ull;
-        hr[j] = (hi_in && e < cnt) ? (uint32_t)hi_in[start + e] : 0u;
-    }
-    __syncthreads();
-    unsigned long long kor = 0, kand = ~0ull;
-#pragma unroll
-    for (int j = 0; j < SS_ITEMS; j++) {
-        const uint32_t e = threadIdx.x + j * SS_THREADS;
-        if (e < cnt) {
-            const uint64_t km = (lr[j] >> 8) | ((uint64_t)hr[j] << 56);
-            const uint64_t key = ((uint64_t)((uint32_t)(km >> bsh) - b0) << lowbits) | (lr[j] & lowmask);
-            sm.key[e] = key;
-            kor |= key;
-            kand &= key;
+    unsigned long long cyc[3] = {0, 0, 0}, npass = 0;
+    for (uint32_t u = blockIdx.x; u < nunits; u += gridDim.x) {
+        const long long t0 = clock64();
+        const uint64_t start = ustart[u];
+        const uint32_t cnt = ucount[u], b0 = ubucket[u];
+        if (u + gridDim.x < nunits) {
+            const uint64_t ns = ustart[u + gridDim.x], nc = ucount[u + gridDim.x];
+            prefetch_range(lo_in + ns, nc * 8, SS_THREADS);
+            prefetch_range(id_in + ns, nc * 4, SS_THREADS);
+            if (hi_in) prefetch_range(hi_in + ns, nc, SS_THREADS);
         }
-    }
-#pragma unroll
-    for (int o = 16; o; o >>= 1) {
-        kor |= __shfl_xor_sync(FULLM, kor, o);
-        kand &= __shfl_xor_sync(FULLM, kand, o);
-    }
-    if (lane == 0) {
-        atomicOr(&sm.kor, kor);
-        atomicAnd(&sm.kand, kand);
-    }
-    __syncthreads();
-    tph[1] = tph[2] = tph[3] = tph[4] = clock64();
-    const uint64_t varying = sm.kor ^ sm.kand;
-    int cur = -1;  // -1: the identity order
-    if (varying) {
-        const int hb = 63 - __clzll((long long)varying);
-        // gl: lowest group bit.  With hb < 32 the passes cover every varying bit.
-        const int gl = hb >= 8 + SS_GPASSES * SS_GBITS ? hb + 1 - SS_GPASSES * SS_GBITS : 8;
-        int c = 0;
-        for (int ps = 0; ps <= SS_GPASSES; ps++) {
-            const int sh = ps == 0 ? 0 : gl + (ps - 1) * SS_GBITS;
-            const uint64_t bits = ps == 0 ? 0xFFull : ((1ull << SS_GBITS) - 1) << sh;
-            if (!(varying & bits)) continue;  // constant digit in this unit
-            if (ps == 0) seg_pass<8>(sm, c, cnt, 0, cur < 0);
-            else seg_pass<SS_GBITS>(sm, c, cnt, sh, cur < 0);
-            c ^= 1;
-            cur = c;
+        if (threadIdx.x == 0) {
+            sm.kor = 0;
+            sm.kand = ~0ull;
         }
-        tph[2] = tph[3] = tph[4] = clock64();
-        if (gl > 8 && cur >= 0) {
-            const uint16_t *P = sm.perm[cur];
-            // group starts and out-of-order positions, one ballot word per warp and round
+        // all loads of the unit in flight at once
+        uint64_t lr[SS_ITEMS];
+        uint32_t hr[SS_ITEMS];
 #pragma unroll
-            for (int j = 0; j < SS_ITEMS; j++) {
-                const uint32_t p = (uint32_t)j * SS_THREADS + threadIdx.x;
-                bool gs = false, dt = false;
-                if (p < cnt) {
-                    const uint64_t kp = sm.key[P[p]];
-                    if (p == 0) {
-                        gs = true;
-                    } else {
-                        const uint64_t kq = sm.key[P[p - 1]];
-                        gs = (kq >> gl) != (kp >> gl);
-                        dt = !gs && kq > kp;
-                    }
-                }
-                const uint32_t wg = __ballot_sync(FULLM, gs), wd = __ballot_sync(FULLM, dt);
-                if (lane == 0) {
-                    sm.gstart[(j * SS_THREADS + warp * 32) >> 5] = wg;
-                    sm.dirty[(j * SS_THREADS + warp * 32) >> 5] = wd;
-                }
-            }
-            __syncthreads();
-            // queue the out-of-order groups whose start this thread holds
-            uint32_t ndirty = 0;
-            for (int j = 0; j < SS_ITEMS; j++) {
-                const uint32_t p = (uint32_t)j * SS_THREADS + threadIdx.x;
-                if (p >= cnt || !((sm.gstart[p >> 5] >> (p & 31)) & 1u)) continue;
-                // q: the next group start (or cnt); dirty: any out-of-order position in (p, q)
-                uint32_t q = cnt;
-                bool dirty = false;
-                uint32_t w = p >> 5;
-                uint32_t gm = sm.gstart[w] & ~((2u << (p & 31)) - 1);  // starts above p in its word
-                uint32_t dm = sm.dirty[w] & ~((2u << (p & 31)) - 1);
-                for (;;) {
-                    if (gm) {
-                        const uint32_t qq = (w << 5) + (uint32_t)(__ffs(gm) - 1);
-                        q = qq < cnt ? qq : cnt;
-                        dirty |= (dm & ((1u << (qq & 31)) - 1)) != 0;
-                        break;
-                    }
-                    dirty |= dm != 0;
-                    if (++w >= (uint32_t)SS_WORDS || (w << 5) >= cnt) break;
-                    gm = sm.gstart[w];
-                    dm = sm.dirty[w];
-                }
-                if (!dirty) continue;
-                ndirty++;
-                const uint32_t slot = atomicAdd(&sm.nlist, 1u);
-                if (slot < (uint32_t)SS_LIST) sm.list[slot] = p | (q << 16);
-                else sm.fallback = 1;
-            }
-            if (trace && ndirty) atomicAdd(&trace[1], (unsigned long long)ndirty);
-            if (force_full && threadIdx.x == 0) sm.fallback = 1;
-            __syncthreads();
-            tph[3] = clock64();
-            // a warp per queued group: repeatedly take the smallest k-mer above the last one and move
-            // its tuples out in their current order (the other perm buffer is the scratch)
-            const uint32_t nl = sm.fallback ? 0u : min(sm.nlist, (uint32_t)SS_LIST);
-            uint16_t *Pw = sm.perm[cur], *Tw = sm.perm[cur ^ 1];
-            uint32_t nmoves = 0;
-            for (uint32_t g = warp; g < nl; g += SS_WARPS) {
-                const uint32_t p = sm.list[g] & 0xFFFF, q = sm.list[g] >> 16;
-                uint32_t out = p;
-                uint64_t last = 0;
-                bool first = true, ok = false;
-                for (int round = 0; round < SS_MAX_KMERS; round++) {
-                    uint64_t mn = ~0ull;
-                    for (uint32_t i = p + lane; i < q; i += 32) {
-                        const uint64_t km = sm.key[Pw[i]] >> 8;
-                        if ((first || km > last) && km < mn) mn = km;
-                    }
+        for (int j = 0; j < SS_ITEMS; j++) {
+            const uint32_t e = threadIdx.x + j * SS_THREADS;
+            lr[j] = e < cnt ? lo_in[start + e] : 0ull;
+            hr[j] = (hi_in && e < cnt) ? (uint32_t)hi_in[start + e] : 0u;
+        }
+        __syncthreads();
+        unsigned long long kor = 0, kand = ~0ull;
 #pragma unroll
-                    for (int o = 16; o; o >>= 1) {
-                        const uint64_t y = __shfl_xor_sync(FULLM, mn, o);
-                        mn = y < mn ? y : mn;
-                    }
-                    if (mn == ~0ull) {
-                        ok = true;
-                        break;
-                    }
-                    for (uint32_t b = p; b < q; b += 32) {
-                        const uint32_t i = b + lane;
-                        uint16_t x = 0;
-                        bool sel = false;
-                        if (i < q) {
-                            x = Pw[i];
-                            sel = (sm.key[x] >> 8) == mn;
-                        }
-                        const uint32_t bal = __ballot_sync(FULLM, sel);
-                        if (sel) Tw[out + __popc(bal & ((1u << lane) - 1))] = x;
-                        out += __popc(bal);
-                    }
-                    last = mn;
-                    first = false;
-                    nmoves += q - p;
-                }
-                if (!ok) {
-                    if (lane == 0) sm.fallback = 1;
-                    continue;
-                }
-                __syncwarp();
-                for (uint32_t i = p + lane; i < q; i += 32) Pw[i] = Tw[i];
-                __syncwarp();
-            }
-            if (trace && lane == 0 && nmoves) atomicAdd(&trace[2], (unsigned long long)nmoves);
-            __syncthreads();
-            tph[4] = clock64();
-            if (sm.fallback) {  // uniform across the block
-                if (trace && threadIdx.x == 0) atomicAdd(&trace[0], 1ull);
-                cur = -1;
-                c = 0;
-                for (int dgt = 0; dgt < 8; dgt++) {
-                    if (!((varying >> (8 * dgt)) & 0xFF)) continue;
-                    seg_pass<8>(sm, c, cnt, 8 * dgt, cur < 0);
-                    c ^= 1;
-                    cur = c;
-                }
+        for (int j = 0; j < SS_ITEMS; j++) {
+            const uint32_t e = threadIdx.x + j * SS_THREADS;
+            if (e < cnt) {
+                const uint64_t km = (lr[j] >> 8) | ((uint64_t)hr[j] << 56);
+                const uint64_t key = ((uint64_t)((uint32_t)(km >> bsh) - b0) << lowbits) | (lr[j] & lowmask);
+                sm.key[e] = key;
+                kor |= key;
+                kand &= key;
             }
         }
+#pragma unroll
+        for (int o = 16; o; o >>= 1) {
+            kor |= __shfl_xor_sync(FULLM, kor, o);
+            kand &= __shfl_xor_sync(FULLM, kand, o);
+        }
+        if (lane == 0) {
+            atomicOr(&sm.kor, kor);
+            atomicAnd(&sm.kand, kand);
+        }
+        __syncthreads();
+        const long long t1 = clock64();
+        const uint64_t varying = sm.kor ^ sm.kand;
+        int cur = -1;  // -1: the identity order
+        if (varying) {
+            const int lb = __ffsll((long long)varying) - 1, hb = 63 - __clzll((long long)varying);
+            const int span = hb - lb + 1, np = (span + max_bits - 1) / max_bits, w = (span + np - 1) / np;
+            const uint32_t mask = (uint32_t)((1ull << w) - 1), nbins = (1u << w) < 32u ? 32u : (1u << w);
+            int c = 0;
+            for (int i = 0; i < np; i++) {
+                const int sh = lb + i * w;
+                if (!((varying >> sh) & mask)) continue;  // constant digit in this unit
+                seg_pass(sm, c, cnt, sh, mask, nbins, cur < 0);
+                c ^= 1;
+                cur = c;
+                npass++;
+            }
+        }
+        const long long t2 = clock64();
+        for (uint32_t e = threadIdx.x; e < cnt; e += SS_THREADS) {
+            const uint32_t sidx = cur < 0 ? e : (uint32_t)sm.perm[cur][e];
+            const uint64_t key = sm.key[sidx];
+            const uint64_t bucket = b0 + (key >> lowbits);
+            lo_out[start + e] = (bucket << lowbits) | (key & lowmask);
+            id_out[start + e] = id_in[start + sidx];
+        }
+        __syncthreads();  // the next unit reuses the shared arrays
+        cyc[0] += (unsigned long long)(t1 - t0);
+        cyc[1] += (unsigned long long)(t2 - t1);
+        cyc[2] += (unsigned long long)(clock64() - t2);
     }
-    __syncthreads();
-    tph[5] = clock64();
-    for (uint32_t e = threadIdx.x; e < cnt; e += SS_THREADS) {
-        const uint32_t sidx = cur < 0 ? e : (uint32_t)sm.perm[cur][e];
-        const uint64_t key = sm.key[sidx];
-        const uint64_t bucket = b0 + (key >> lowbits);
-        lo_out[start + e] = (bucket << lowbits) | (key & lowmask);
-        id_out[start + e] = id_in[start + sidx];
-    }
-    if (trace && threadIdx.x == 0) {  // cycles per phase, summed over units (the fallback counts with the groups)
-        atomicAdd(&trace[3], (unsigned long long)(tph[1] - tph[0]));
-        atomicAdd(&trace[4], (unsigned long long)(tph[2] - tph[1]));
-        atomicAdd(&trace[5], (unsigned long long)(tph[3] - tph[2]));
-        atomicAdd(&trace[6], (unsigned long long)(tph[5] - tph[3]));
-        atomicAdd(&trace[7], (unsigned long long)(clock64() - tph[5]));
+    if (trace && threadIdx.x == 0) {
+        atomicAdd(&trace[0], npass);
+        for (int q = 0; q < 3; q++) atomicAdd(&trace[1 + q], cyc[q]);
     }
 }
 
@@ -645,12 +549,21 @@ __global__ void k_big_scatter(const uint64_t *__restrict__ bstart, const uint32_
     }
 }
 
-// MP_UNIT_SORT_FULL=1 sends every unit that has groups through the full shared-memory LSD sort
-// (used by the tests to cover that path on ordinary inputs).
-static uint32_t unit_sort_force_full()
+// Widest digit of the unit sort (MP_UNIT_SORT_MAX_BITS, 5..10; default 10).  The tests also run
+// narrower digits, which change every unit's pass plan.
+static int unit_sort_max_bits()
 {
-    const char *e = getenv("MP_UNIT_SORT_FULL");
-    return e && *e && *e != '0' ? 1u : 0u;
+    const char *e = getenv("MP_UNIT_SORT_MAX_BITS");
+    const int v = e && *e ? atoi(e) : SS_MAXBITS;
+    return v < 5 ? 5 : (v > SS_MAXBITS ? SS_MAXBITS : v);
+}
+
+static int sm_count()
+{
+    int dev = 0, n = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    return n > 0 ? n : 1;
 }
 
 static void sort_kernel_attrs()
@@ -704,6 +617,7 @@ int bucket_sort(SortBufs &b, uint64_t n, bool has_hi, int k, const uint64_t *his
     MP_CUDA(cudaMemsetAsync(err, 0, sizeof(uint32_t), st));
     if (status) MP_CUDA(cudaMemsetAsync(status, 0, tiles * 256 * sizeof(unsigned long long), st));
     sort_kernel_attrs();
+    const uint32_t pf = 2u * (uint32_t)sm_count();  // resident tiles: the prefetch distance
     cudaEvent_t ev[5];
     for (auto &e : ev) cudaEventCreate(&e);
     cudaEventRecord(ev[0], st);
@@ -712,7 +626,7 @@ int bucket_sort(SortBufs &b, uint64_t n, bool has_hi, int k, const uint64_t *his
         const int src = b.cur, dst = b.cur ^ 1;
         (mp::count_launch(), k_onesweep<2><<<(unsigned)tiles, ST, sizeof(SortSmem), st>>>(
             b.lo[src], has_hi ? b.hi[src] : nullptr, b.id[src], b.lo[dst], has_hi ? b.hi[dst] : nullptr, b.id[dst], n,
-            bsh + 8 * d, dbase + d * 256, status, ctr + pi, (uint32_t)(pi + 1), err));
+            bsh + 8 * d, dbase + d * 256, status, ctr + pi, (uint32_t)(pi + 1), err, pf));
         b.cur = dst;
     }
     cudaEventRecord(ev[1], st);
@@ -751,9 +665,9 @@ int bucket_sort(SortBufs &b, uint64_t n, bool has_hi, int k, const uint64_t *his
         MP_CUDA(cudaMemcpyAsync(d_us, us.data(), nu * 8, cudaMemcpyHostToDevice, st));
         MP_CUDA(cudaMemcpyAsync(d_uc, uc.data(), nu * 4, cudaMemcpyHostToDevice, st));
         MP_CUDA(cudaMemcpyAsync(d_ub, ub.data(), nu * 4, cudaMemcpyHostToDevice, st));
-        (mp::count_launch(), k_segsort<<<(unsigned)nu, SS_THREADS, sizeof(SegSmem), st>>>(
-            d_us, d_uc, d_ub, b.lo[in], has_hi ? b.hi[in] : nullptr, b.id[in], b.lo[out], b.id[out], bsh, lowbits,
-            unit_sort_force_full(), trace));
+        (mp::count_launch(), k_segsort<<<(unsigned)std::min<size_t>(nu, (size_t)sm_count()), SS_THREADS, sizeof(SegSmem), st>>>(
+            d_us, d_uc, d_ub, (uint32_t)nu, b.lo[in], has_hi ? b.hi[in] : nullptr, b.id[in], b.lo[out], b.id[out], bsh,
+            lowbits, unit_sort_max_bits(), trace));
     }
     cudaEventRecord(ev[2], st);
     uint64_t nbig = 0;
@@ -813,10 +727,8 @@ int bucket_sort(SortBufs &b, uint64_t n, bool has_hi, int k, const uint64_t *his
         stats->units = nu;
         stats->big_buckets = nb;
         stats->big_tuples = nbig;
-        stats->fallback_units = ht[0];
-        stats->dirty_groups = ht[1];
-        stats->moves = ht[2];
-        for (int q = 0; q < 5; q++) stats->phase_cycles[q] = ht[3 + q];
+        stats->unit_passes = ht[0];
+        for (int q = 0; q < 3; q++) stats->phase_cycles[q] = ht[1 + q];
     }
     for (auto &e : ev) cudaEventDestroy(e);
     arena.free_scratch(status);
@@ -934,11 +846,11 @@ int sort_tuples_noalloc(const uint64_t *lo_in, const uint8_t *hi_in, const uint3
         if (dgt < 8)
             (mp::count_launch(), k_onesweep<0><<<(unsigned)tiles, ST, sizeof(SortSmem), st>>>(
                 src_lo, src_hi, src_id, d_lo, d_hi, d_id, n, 8 * dgt, S->dbase + dgt * 256, S->status, S->ctr + i,
-                (uint32_t)(i + 1), &S->err));
+                (uint32_t)(i + 1), &S->err, 0u));
         else
             (mp::count_launch(), k_onesweep<1><<<(unsigned)tiles, ST, sizeof(SortSmem), st>>>(
                 src_lo, src_hi, src_id, d_lo, d_hi, d_id, n, 0, S->dbase + dgt * 256, S->status, S->ctr + i,
-                (uint32_t)(i + 1), &S->err));
+                (uint32_t)(i + 1), &S->err, 0u));
         src_lo = d_lo;
         src_hi = d_hi;
         src_id = d_id;

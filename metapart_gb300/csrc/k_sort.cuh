@@ -21,8 +21,8 @@ struct SortStats {
     double seg_ms = 0;        // shared-memory unit sort (bucket_sort)
     double big_ms = 0;        // oversized buckets (bucket_sort)
     uint64_t units = 0, big_buckets = 0, big_tuples = 0;
-    uint64_t fallback_units = 0, dirty_groups = 0, moves = 0;  // unit sort: full-LSD units, mixed groups, tuples moved
-    uint64_t phase_cycles[5] = {0, 0, 0, 0, 0};                 // unit sort, summed over units: load, passes, marks, groups, store
+    uint64_t unit_passes = 0;                 // unit sort: digit passes, summed over units
+    uint64_t phase_cycles[3] = {0, 0, 0};     // unit sort: SM cycles summed over units in load, passes, store
 };
 
 // Stable sort of b[cur][0, n) by (hi, lo); on return b.cur names the sorted buffer.

@@ -78,7 +78,7 @@ struct mp_job {
     uint64_t sort_bytes_total = 0, sort_tuples_total = 0;
     double seg_ms_total = 0, big_ms_total = 0;
     uint64_t units_total = 0, big_buckets_total = 0, big_tuples_total = 0;
-    uint64_t fallback_total = 0, dirty_total = 0, moves_total = 0, phase_total[5] = {0, 0, 0, 0, 0};
+    uint64_t unit_passes_total = 0, phase_total[3] = {0, 0, 0};
     int pe_rounds = 0;
 };
 
@@ -457,7 +457,7 @@ int mp_job_partition(mp_job *j, const mp_part_params *p, const uint64_t *chunk_s
     j->seg_ms_total = 0;
     j->big_ms_total = 0;
     j->units_total = j->big_buckets_total = j->big_tuples_total = 0;
-    j->fallback_total = j->dirty_total = j->moves_total = 0;
+    j->unit_passes_total = 0;
     for (auto &v : j->phase_total) v = 0;
     if (j->d_parent) { j->arena.free_persistent(j->d_parent); j->d_parent = nullptr; }
     if (j->d_size) { j->arena.free_persistent(j->d_size); j->d_size = nullptr; }
@@ -554,10 +554,8 @@ int mp_job_partition(mp_job *j, const mp_part_params *p, const uint64_t *chunk_s
             j->units_total += ss.units;
             j->big_buckets_total += ss.big_buckets;
             j->big_tuples_total += ss.big_tuples;
-            j->fallback_total += ss.fallback_units;
-            j->dirty_total += ss.dirty_groups;
-            j->moves_total += ss.moves;
-            for (int q = 0; q < 5; q++) j->phase_total[q] += ss.phase_cycles[q];
+            j->unit_passes_total += ss.unit_passes;
+            for (int q = 0; q < 3; q++) j->phase_total[q] += ss.phase_cycles[q];
         }
         Tuples tp;
         tp.lo = sb.lo[lo_buf];
@@ -671,10 +669,8 @@ int mp_job_sort_split(const mp_job *j, double *pass_ms, double *unit_ms, double 
 {
     if (!j) return set_error(MP_EARG, "null job");
     if (unit_counters) {
-        unit_counters[0] = j->fallback_total;
-        unit_counters[1] = j->dirty_total;
-        unit_counters[2] = j->moves_total;
-        for (int q = 0; q < 5; q++) unit_counters[3 + q] = j->phase_total[q];
+        unit_counters[0] = j->unit_passes_total;
+        for (int q = 0; q < 3; q++) unit_counters[1 + q] = j->phase_total[q];
     }
     if (pass_ms) *pass_ms = j->sort_ms_total;
     if (unit_ms) *unit_ms = j->seg_ms_total;

@@ -238,13 +238,12 @@ class Job:
     def sort_split(self) -> dict:
         a, u, g = C.c_double(), C.c_double(), C.c_double()
         nu, nb, nt = C.c_uint64(), C.c_uint64(), C.c_uint64()
-        uc = (C.c_uint64 * 8)()
+        uc = (C.c_uint64 * 4)()
         _check(lib().mp_job_sort_split(self.h, C.byref(a), C.byref(u), C.byref(g), C.byref(nu), C.byref(nb),
                                        C.byref(nt), uc), "sort_split")
         return {"digit_pass_ms": a.value, "unit_sort_ms": u.value, "big_bucket_ms": g.value, "units": nu.value,
-                "big_buckets": nb.value, "big_tuples": nt.value, "fallback_units": uc[0], "mixed_groups": uc[1],
-                "mixed_group_moves": uc[2], "unit_cycles": {"load": uc[3], "passes": uc[4], "mark": uc[5],
-                                                              "groups": uc[6], "store": uc[7]}}
+                "big_buckets": nb.value, "big_tuples": nt.value, "unit_passes": uc[0],
+                "unit_cycles": {"load": uc[1], "passes": uc[2], "store": uc[3]}}
 
 
 def fastq_index_ptr(num_chunks: int, host_ptr: int, nbytes: int, interleaved: bool = False):

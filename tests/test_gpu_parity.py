@@ -63,13 +63,14 @@ def test_gpu_matches_oracle(tmp_path, built_gpu, name, n, p):
     _compare(tmp_path, name, n, p)
 
 
-# Every bucket unit with groups goes through the full shared-memory LSD sort instead of the group passes.
-FALLBACK = [
+# Narrower unit-sort digits: a different pass plan for every bucket unit.
+NARROW = [
     ("plain_large", 30000, pu.Params(k=31, chunks=4, scans=2, threads=2)),
     ("hotspot", 40000, pu.Params(k=27, chunks=4, scans=1, threads=2)),
 ]
 
 
-@pytest.mark.parametrize("name,n,p", FALLBACK, ids=[f"{c[0]}-k{c[2].k}" for c in FALLBACK])
-def test_gpu_unit_sort_fallback(tmp_path, built_gpu, name, n, p):
-    _compare(tmp_path, name, n, p, env_extra={"MP_UNIT_SORT_FULL": "1"})
+@pytest.mark.parametrize("bits", [5, 8])
+@pytest.mark.parametrize("name,n,p", NARROW, ids=[f"{c[0]}-k{c[2].k}" for c in NARROW])
+def test_gpu_unit_sort_digit_width(tmp_path, built_gpu, name, n, p, bits):
+    _compare(tmp_path, name, n, p, env_extra={"MP_UNIT_SORT_MAX_BITS": str(bits)})
