@@ -1,11 +1,11 @@
 // K1 (m-mer histogram) and K2 (tuple enumeration) kernels.
 //
 // Plain variant: one warp per read.  Each round of 32 bases is loaded with one
-// coalesced byte load per lane and turned into bit-planes with __ballot_sync: the
-// 2-bit base codes (packed most-significant-first into a 64-bit word), an N mask,
-// and the five character bits the adjacency byte uses.  Lane j of round t then
-// owns k-mer position 32t+j: its forward code is a funnel shift of two packed
-// words, its reverse complement a bit reversal (countMmers.c:83-217,
+// coalesced byte load per lane; two warp OR-reductions pack the 2-bit base codes
+// most-significant-first into a 64-bit word and a ballot gives the N mask.  Lane j
+// of round t then owns k-mer position 32t+j: its forward code is a funnel shift of
+// two packed words, its reverse complement a bit reversal, and the neighbouring
+// characters of the adjacency byte come by shuffle (countMmers.c:83-217,
 // enumerateKmers.c:127-371 compute the same codes with a rolling update).
 //
 // 3-minimizer variant: one thread per read running the reference's window logic
@@ -27,9 +27,10 @@ __device__ __forceinline__ void load_round(const uint8_t *s, uint32_t L, int t, 
 {
     const uint32_t p = 32u * (uint32_t)t + (uint32_t)lane;
     const uint32_t c = p < L ? (uint32_t)s[p] : 0x41u;
-    const uint32_t f = fcode(c);
-    const uint32_t P1 = __ballot_sync(FULL, f & 2), P0 = __ballot_sync(FULL, f & 1);
-    r.W = (spread32(__brev(P1)) << 1) | spread32(__brev(P0));
+    // lane j's code goes to bits 63-2j..62-2j of W: two warp OR-reductions build the halves
+    const uint32_t f = fcode(c) << (30 - 2 * (lane & 15));
+    const uint32_t hi = __reduce_or_sync(FULL, lane < 16 ? f : 0u), lo = __reduce_or_sync(FULL, lane < 16 ? 0u : f);
+    r.W = ((uint64_t)hi << 32) | lo;
     r.N = __ballot_sync(FULL, p < L && c == 'N');
     r.c = c;
 }

@@ -71,18 +71,37 @@ __global__ void k_out_entries(OutCtx c, const uint32_t *f1, const uint32_t *f2, 
     }
 }
 
+// Entry lengths; file sizes by one atomic per file and warp (entries are sorted by file, so a
+// warp's lanes of one file are contiguous: the last lane adds its segment of an inclusive scan).
 __global__ void k_out_len(OutCtx c, const uint32_t *val, uint64_t n, uint64_t *len, const uint64_t *key,
                           unsigned long long *file_bytes)
 {
     const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const uint64_t u = val[i];
-    const uint64_t r0 = c.interleaved ? 2 * u : u, r1 = c.interleaved ? 2 * u + 2 : u + 1;
-    const uint64_t l = c.rec_start[r1] - c.rec_start[r0];
-    len[i] = l;
-    atomicAdd(&file_bytes[key[i]], (unsigned long long)l);
+    const int lane = threadIdx.x & 31;
+    const bool v = i < n;
+    uint64_t l = 0, f = ~0ull;
+    if (v) {
+        const uint64_t u = val[i];
+        const uint64_t r0 = c.interleaved ? 2 * u : u, r1 = c.interleaved ? 2 * u + 2 : u + 1;
+        l = c.rec_start[r1] - c.rec_start[r0];
+        len[i] = l;
+        f = key[i];
+    }
+    uint64_t incl = l;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint64_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+        if (lane >= o) incl += y;
+    }
+    const uint32_t peers = __match_any_sync(0xFFFFFFFFu, f);
+    const int first = __ffs(peers) - 1, last = 31 - __clz(peers);
+    const uint64_t before = __shfl_sync(0xFFFFFFFFu, incl, first > 0 ? first - 1 : 0);
+    if (v && lane == last) atomicAdd(&file_bytes[f], (unsigned long long)(incl - (first > 0 ? before : 0)));
 }
 
+// A warp per record: bytes up to the first 4-byte boundary of the destination, then aligned 4-byte
+// words assembled from two aligned source words by a funnel shift, then the tail bytes.  Source
+// words may reach 3 bytes past the record; the FASTQ buffer carries 64 bytes of padding.
 __global__ void k_out_copy(OutCtx c, const uint8_t *fq, const uint32_t *val, const uint64_t *off, uint64_t n, uint8_t *out)
 {
     const uint64_t w = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -91,7 +110,16 @@ __global__ void k_out_copy(OutCtx c, const uint8_t *fq, const uint32_t *val, con
     const uint64_t u = val[w];
     const uint64_t r0 = c.interleaved ? 2 * u : u, r1 = c.interleaved ? 2 * u + 2 : u + 1;
     const uint64_t s = c.rec_start[r0], l = c.rec_start[r1] - s, o = off[w];
-    for (uint64_t q = lane; q < l; q += 32) out[o + q] = fq[s + q];
+    const uint64_t head = min(l, (uint64_t)((4 - (o & 3)) & 3));
+    if ((uint64_t)lane < head) out[o + lane] = fq[s + lane];
+    const uint64_t words = (l - head) >> 2;
+    const uint64_t sb = s + head;
+    const uint32_t a = (uint32_t)(sb & 3) * 8;
+    const uint32_t *src = reinterpret_cast<const uint32_t *>(fq + (sb & ~3ull));
+    uint32_t *dst = reinterpret_cast<uint32_t *>(out + o + head);
+    for (uint64_t j = lane; j < words; j += 32) dst[j] = __funnelshift_r(src[j], src[j + 1], a);
+    const uint64_t t0 = head + (words << 2);
+    if ((uint64_t)lane < l - t0) out[o + t0 + lane] = fq[s + t0 + lane];
 }
 
 int gather_output(const uint8_t *d_fq, const ParsedReads &pr, const uint32_t *d_label, const uint64_t *bounds_host,

@@ -62,18 +62,6 @@ __host__ __device__ __forceinline__ uint32_t adj_rc(uint32_t pa5, uint32_t na5)
     return ((a5_cmpl(na5) << 3) & 0xF8) | (a5_cmpl(pa5) & 7);
 }
 
-// Spread the 32 bits of x to the even bit positions of a 64-bit word.
-__device__ __forceinline__ uint64_t spread32(uint32_t v)
-{
-    uint64_t x = v;
-    x = (x | (x << 16)) & 0x0000FFFF0000FFFFull;
-    x = (x | (x << 8)) & 0x00FF00FF00FF00FFull;
-    x = (x | (x << 4)) & 0x0F0F0F0F0F0F0F0Full;
-    x = (x | (x << 2)) & 0x3333333333333333ull;
-    x = (x | (x << 1)) & 0x5555555555555555ull;
-    return x;
-}
-
 // Process-wide count of kernels this library launched (mp_launch_count).
 void count_launch();
 
