@@ -189,6 +189,14 @@ int mp_server_stats(mp_server *s, mp_server_stats_t *st);
 /* Runs the queued requests to completion, then stops the workers. */
 void mp_server_destroy(mp_server *s);
 
+/* k-mer cache (default on): mp_job_count of the plain variant keeps every read position's canonical
+ * k-mer and adjacency byte (9 bytes per position) in the job, and the next mp_job_partition with the
+ * same k filters it per scan instead of recomputing k-mers from the reads; the partition releases it.
+ * Skipped without error when device memory or the budget does not allow it.  Turn it off for a
+ * count-only job (the drop-in genHistograms).  No counterpart in the reference, whose stages are
+ * separate processes. */
+int mp_job_set_kmer_cache(mp_job *job, int enable);
+
 /* Optional stage dumps in the reference's formats (the files oracle/ref_hooks.c writes),
  * for parity testing.  NULL disables. */
 int mp_job_set_dump_dir(mp_job *job, const char *dir);

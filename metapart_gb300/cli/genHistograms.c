@@ -46,6 +46,7 @@ int main(int argc, char **argv)
     int rc = mp_ctx_create(env_device(), 0, &ctx);
     if (rc) cli_die(argv[0], "no GPU context", rc);
     if ((rc = mp_job_create(ctx, &job))) cli_die(argv[0], "job", rc);
+    mp_job_set_kmer_cache(job, 0); /* this process only counts */
     if ((rc = mp_job_load_fastq(job, buf, fs.total, fs.size, nfiles, nil > 0))) cli_die(argv[0], "loading reads", rc);
     uint64_t *hist = (uint64_t *)calloc(MP_NUM_BUCKETS + 1, sizeof(uint64_t));
     uint32_t *counts = (uint32_t *)calloc((size_t)nchunks * MP_NUM_BUCKETS, sizeof(uint32_t));

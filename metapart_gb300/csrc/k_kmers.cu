@@ -56,9 +56,15 @@ __device__ __forceinline__ uint32_t chunk_of(const uint64_t *chunk_rec, int nchu
 
 // ------------------------------------------------------------ K1 plain
 
+// KC: per position of every read, lo = canon << 8 | adj and hi = canon >> 56, or hi = KC_NONE
+// when the window holds an N.  Written by the count pass when kc_lo is given; the partition's
+// scans then filter this array instead of recomputing k-mers.
+constexpr uint8_t KC_NONE = 0xFF;
+
 __global__ void __launch_bounds__(256) k_count_plain(const uint8_t *fq, const uint64_t *seq_off, const uint32_t *seq_len,
                                                      uint64_t r0, uint64_t r1, int k, const uint64_t *chunk_rec,
-                                                     int nchunks, uint32_t *cc, unsigned long long *glob, uint32_t *err)
+                                                     int nchunks, uint32_t *cc, unsigned long long *glob, uint32_t *err,
+                                                     const uint64_t *kc_off, uint64_t *kc_lo, uint8_t *kc_hi)
 {
     const int lane = threadIdx.x & 31;
     const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
@@ -73,15 +79,31 @@ __global__ void __launch_bounds__(256) k_count_plain(const uint8_t *fq, const ui
         const uint8_t *s = fq + seq_off[r];
         uint32_t *ccc = cc ? cc + (size_t)chunk_of(chunk_rec, nchunks, r) * NB : nullptr;
         const int last = (int)L - k;
-        Round cur, nxt;
+        const uint64_t kbase = kc_lo ? kc_off[r] : 0;
+        Round prv, cur, nxt;
         load_round(s, L, 0, lane, cur);
         load_round(s, L, 1, lane, nxt);
+        prv = cur;
         for (int t = 0; 32 * t <= last; t++) {
             const int i = 32 * t + lane;
             uint64_t fwd;
             bool v = kmer_at(lane, k, cur, nxt, fwd) && i <= last;
             const uint64_t rc = revcomp(fwd, k);
-            const uint32_t b = (uint32_t)((fwd < rc ? fwd : rc) >> sh);
+            const bool f = fwd < rc;
+            const uint64_t canon = f ? fwd : rc;
+            const uint32_t b = (uint32_t)(canon >> sh);
+            if (kc_lo) {
+                const uint32_t x = __shfl_sync(FULL, cur.c, (lane + 31) & 31), y = __shfl_sync(FULL, prv.c, 31);
+                const int q = lane + k;
+                const uint32_t u = __shfl_sync(FULL, cur.c, q & 31), w = __shfl_sync(FULL, nxt.c, q & 31);
+                if (i <= last) {
+                    // 'N' at the read ends (enumerateKmers.c:177, 252-255)
+                    const uint32_t pa = i > 0 ? a5_of(lane ? x : y) : 7u, na = i < last ? a5_of(q < 32 ? u : w) : 7u;
+                    const uint32_t adj = f ? adj_fwd(pa, na) : adj_rc(pa, na);
+                    kc_lo[kbase + i] = (canon << 8) | adj;
+                    kc_hi[kbase + i] = v ? (uint8_t)(canon >> 56) : KC_NONE;
+                }
+            }
             const uint32_t act = __ballot_sync(FULL, v);
             if (v) {
                 const uint32_t peers = __match_any_sync(act, b);
@@ -90,10 +112,18 @@ __global__ void __launch_bounds__(256) k_count_plain(const uint8_t *fq, const ui
                     else atomicAdd(&glob[b], (unsigned long long)__popc(peers));
                 }
             }
+            prv = cur;
             cur = nxt;
             load_round(s, L, t + 2, lane, nxt);
         }
     }
+}
+
+// Positions per read (L - k + 1, or 0), for the k-mer cache offsets.
+__global__ void k_kc_positions(const uint32_t *seq_len, uint64_t n, int k, uint32_t *npos)
+{
+    const uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r < n) npos[r] = seq_len[r] > (uint32_t)k ? seq_len[r] - (uint32_t)k + 1 : 0u;
 }
 
 // ------------------------------------------------------- 3-minimizer core
@@ -315,6 +345,93 @@ __global__ void __launch_bounds__(256) k_enum_count_scans(const uint8_t *fq, con
     }
 }
 
+// K2a from the k-mer cache: tuples per read of every scan (S <= MAX_SCAN_COUNT), one warp per read.
+__global__ void __launch_bounds__(256) k_kc_count_scans(const uint64_t *kc_off, const uint64_t *kc_lo,
+                                                        const uint8_t *kc_hi, uint64_t n_reads, int k,
+                                                        const uint32_t *bounds, int S, uint32_t *cnt, uint64_t stride,
+                                                        uint32_t *err)
+{
+    __shared__ uint32_t sb[MAX_SCAN_COUNT + 1];
+    if (threadIdx.x <= (unsigned)S) sb[threadIdx.x] = bounds[threadIdx.x];
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    const int sh = 2 * (k - 10);
+    const uint32_t b_lo = sb[0], b_hi = sb[S];
+    for (uint64_t r = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < n_reads; r += nw) {
+        const uint64_t p0 = kc_off[r], np = kc_off[r + 1] - p0;
+        uint32_t c[MAX_SCAN_COUNT];
+#pragma unroll
+        for (int q = 0; q < MAX_SCAN_COUNT; q++) c[q] = 0;
+        if (np > 300) {  // L - k >= 300 (enumerateKmers.c:155)
+            if (lane == 0) atomicOr(err, DERR_LONG_READ);
+        } else {
+            for (uint64_t i = lane; i < np; i += 32) {
+                const uint8_t h = kc_hi[p0 + i];
+                if (h == KC_NONE) continue;
+                const uint64_t km = (kc_lo[p0 + i] >> 8) | ((uint64_t)h << 56);
+                const uint32_t b = (uint32_t)(km >> sh);
+                if (b < b_lo || b >= b_hi) continue;
+                int sc = 0;
+#pragma unroll
+                for (int q = 1; q < MAX_SCAN_COUNT; q++) sc += (q < S && b >= sb[q]) ? 1 : 0;
+#pragma unroll
+                for (int q = 0; q < MAX_SCAN_COUNT; q++) c[q] += (sc == q) ? 1u : 0u;
+            }
+        }
+        for (int q = 0; q < S; q++) {
+            uint32_t x = c[q];
+#pragma unroll
+            for (int o = 16; o; o >>= 1) x += __shfl_xor_sync(FULL, x, o);
+            if (lane == 0) {
+                cnt[(uint64_t)q * stride + r] = x;
+                if (x > 255) atomicOr(err, DERR_TOO_MANY);  // the reference's per-read counter is a uint8_t
+            }
+        }
+    }
+}
+
+// K2b from the k-mer cache: the tuples of buckets [lo, hi) at off[read], in position order.
+__global__ void __launch_bounds__(256) k_kc_write(const uint64_t *kc_off, const uint64_t *kc_lo, const uint8_t *kc_hi,
+                                                  uint64_t n_reads, int k, uint32_t lo, uint32_t hi,
+                                                  const uint32_t *label, const uint64_t *out_off, uint64_t *o_lo,
+                                                  uint8_t *o_hi, uint32_t *o_id)
+{
+    const int lane = threadIdx.x & 31;
+    const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    const int sh = 2 * (k - 10);
+    for (uint64_t r = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < n_reads; r += nw) {
+        const uint64_t p0 = kc_off[r], np = kc_off[r + 1] - p0;
+        if (np == 0 || np > 300) continue;
+        uint32_t id = (uint32_t)r;
+        if (label) {
+            const uint32_t p = label[r];
+            id = (p == BAD) ? (uint32_t)r : p;  // findRoot after full compression (metapart.c:543-568)
+        }
+        uint64_t base = out_off[r];
+        for (uint64_t i0 = 0; i0 < np; i0 += 32) {
+            const uint64_t i = i0 + lane;
+            uint64_t l = 0;
+            uint8_t h = KC_NONE;
+            if (i < np) {
+                l = kc_lo[p0 + i];
+                h = kc_hi[p0 + i];
+            }
+            const uint64_t km = (l >> 8) | ((uint64_t)h << 56);
+            const uint32_t b = (uint32_t)(km >> sh);
+            const bool v = h != KC_NONE && b >= lo && b < hi;
+            const uint32_t bal = __ballot_sync(FULL, v);
+            if (v) {
+                const uint64_t pos = base + __popc(bal & ((1u << lane) - 1));
+                o_lo[pos] = l;
+                if (o_hi) o_hi[pos] = h;
+                o_id[pos] = id;
+            }
+            base += __popc(bal);
+        }
+    }
+}
+
 // ------------------------------------------------------------- K2 3-min
 
 template <bool WRITE>
@@ -366,14 +483,15 @@ static unsigned grid_for(uint64_t work, int per_block, int max_blocks = 152 * 16
 }
 
 void launch_count(const uint8_t *fq, const ParsedReads &pr, int k, int min3, const uint64_t *chunk_rec, int nchunks,
-                  uint32_t *cc, unsigned long long *glob, uint32_t *err, cudaStream_t st)
+                  uint32_t *cc, unsigned long long *glob, uint32_t *err, cudaStream_t st, const uint64_t *kc_off,
+                  uint64_t *kc_lo, uint8_t *kc_hi)
 {
     if (min3)
         (mp::count_launch(), k_count_min3<<<grid_for(pr.n_reads, 128, 152 * 32), 128, 0, st>>>(fq, pr.seq_off, pr.seq_len, 0, pr.n_reads, k,
                                                                           chunk_rec, nchunks, cc, glob, err));
     else
         (mp::count_launch(), k_count_plain<<<grid_for(pr.n_reads, 8), 256, 0, st>>>(fq, pr.seq_off, pr.seq_len, 0, pr.n_reads, k, chunk_rec,
-                                                               nchunks, cc, glob, err));
+                                                               nchunks, cc, glob, err, kc_off, kc_lo, kc_hi));
     if (cc) (mp::count_launch(), k_sum_chunks<<<NB / 256, 256, 0, st>>>(cc, nchunks, glob));
 }
 
@@ -395,6 +513,28 @@ int launch_enum_count_scans(const uint8_t *fq, const ParsedReads &pr, int k, con
     (mp::count_launch(), k_enum_count_scans<<<grid_for(pr.n_reads, 8), 256, 0, st>>>(
         fq, pr.seq_off, pr.seq_len, pr.n_reads, k, bounds, S, cnt, stride, err));
     return 0;
+}
+
+void launch_kc_positions(const ParsedReads &pr, int k, uint32_t *npos, cudaStream_t st)
+{
+    (mp::count_launch(), k_kc_positions<<<(unsigned)((pr.n_reads + 255) / 256), 256, 0, st>>>(pr.seq_len, pr.n_reads, k, npos));
+}
+
+int launch_kc_count_scans(const uint64_t *kc_off, const uint64_t *kc_lo, const uint8_t *kc_hi, uint64_t n_reads, int k,
+                          const uint32_t *bounds, int S, uint32_t *cnt, uint64_t stride, uint32_t *err, cudaStream_t st)
+{
+    if (S < 1 || S > MAX_SCAN_COUNT) return -1;
+    (mp::count_launch(), k_kc_count_scans<<<grid_for(n_reads, 8), 256, 0, st>>>(kc_off, kc_lo, kc_hi, n_reads, k, bounds, S,
+                                                                             cnt, stride, err));
+    return 0;
+}
+
+void launch_kc_write(const uint64_t *kc_off, const uint64_t *kc_lo, const uint8_t *kc_hi, uint64_t n_reads, int k,
+                     uint32_t lo, uint32_t hi, const uint32_t *label, const uint64_t *off, uint64_t *o_lo, uint8_t *o_hi,
+                     uint32_t *o_id, cudaStream_t st)
+{
+    (mp::count_launch(), k_kc_write<<<grid_for(n_reads, 8), 256, 0, st>>>(kc_off, kc_lo, kc_hi, n_reads, k, lo, hi, label,
+                                                                       off, o_lo, o_hi, o_id));
 }
 
 void launch_enum_write(const uint8_t *fq, const ParsedReads &pr, int k, int min3, uint32_t lo, uint32_t hi,

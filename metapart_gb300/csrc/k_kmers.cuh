@@ -5,8 +5,18 @@ namespace mp {
 
 // K1: bucket counts.  cc (nullable): per-chunk u32 counts [nchunks][NB]; glob: u64 counts [NB]
 // (summed from cc when cc is given).
+// kc_off/kc_lo/kc_hi (nullable, plain variant only): the k-mer cache to fill (see k_kc_*).
 void launch_count(const uint8_t *fq, const ParsedReads &pr, int k, int min3, const uint64_t *chunk_rec, int nchunks,
-                  uint32_t *cc, unsigned long long *glob, uint32_t *err, cudaStream_t st);
+                  uint32_t *cc, unsigned long long *glob, uint32_t *err, cudaStream_t st, const uint64_t *kc_off = nullptr,
+                  uint64_t *kc_lo = nullptr, uint8_t *kc_hi = nullptr);
+
+// k-mer cache: positions per read (L - k + 1 or 0); per-read tuple counts of every scan; one scan's tuples.
+void launch_kc_positions(const ParsedReads &pr, int k, uint32_t *npos, cudaStream_t st);
+int launch_kc_count_scans(const uint64_t *kc_off, const uint64_t *kc_lo, const uint8_t *kc_hi, uint64_t n_reads, int k,
+                          const uint32_t *bounds, int S, uint32_t *cnt, uint64_t stride, uint32_t *err, cudaStream_t st);
+void launch_kc_write(const uint64_t *kc_off, const uint64_t *kc_lo, const uint8_t *kc_hi, uint64_t n_reads, int k,
+                     uint32_t lo, uint32_t hi, const uint32_t *label, const uint64_t *off, uint64_t *o_lo, uint8_t *o_hi,
+                     uint32_t *o_id, cudaStream_t st);
 
 // K2a: tuples per read in the bucket range [lo, hi).
 void launch_enum_count(const uint8_t *fq, const ParsedReads &pr, int k, int min3, uint32_t lo, uint32_t hi,

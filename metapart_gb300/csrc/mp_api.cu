@@ -61,6 +61,11 @@ struct mp_job {
     uint32_t *d_parent = nullptr;
     uint32_t *d_size = nullptr;
     uint8_t *d_filtered = nullptr;
+    // k-mer cache written by the count pass (plain variant): per-read position offsets, lo, hi
+    bool kc_on = true;
+    int kc_k = 0;
+    uint64_t *kc_off = nullptr, *kc_lo = nullptr;
+    uint8_t *kc_hi = nullptr;
     int T = 0, nchunks = 0;
     std::vector<uint64_t> chunk_rec;
     uint64_t bounds[17] = {0};
@@ -233,6 +238,48 @@ int range_bounds(const uint64_t *hist, const uint64_t *ltr, int T, uint64_t scan
     return 0;
 }
 
+void drop_kmer_cache(mp_job *j)
+{
+    j->arena.free_persistent(j->kc_off);
+    j->arena.free_persistent(j->kc_lo);
+    j->arena.free_persistent(j->kc_hi);
+    j->kc_off = j->kc_lo = nullptr;
+    j->kc_hi = nullptr;
+    j->kc_k = 0;
+}
+
+// Cache arrays for the plain variant's count pass; false (and no cache) when device memory or the
+// budget does not allow it -- the partition then computes its k-mers from the reads.
+bool make_kmer_cache(mp_job *j, int k)
+{
+    const uint64_t N = j->pr.n_reads;
+    uint32_t *npos = j->arena.alloc<uint32_t>(N + 1);
+    uint64_t *tot = j->arena.alloc<uint64_t>(1);
+    size_t tb = scan_tmp_bytes(N + 1);
+    void *tmp = j->arena.alloc<uint8_t>(tb);
+    j->kc_off = j->arena.alloc_persistent<uint64_t>(N + 2);
+    if (!npos || !tot || !tmp || !j->kc_off) {
+        drop_kmer_cache(j);
+        return false;
+    }
+    launch_kc_positions(j->pr, k, npos, j->st);
+    if (cudaMemsetAsync(npos + N, 0, 4, j->st) != cudaSuccess) return false;
+    scan_u32_to_u64(npos, j->kc_off, N + 1, tot, tmp, tb, j->st);
+    uint64_t P = 0;
+    if (cudaMemcpyAsync(&P, tot, 8, cudaMemcpyDeviceToHost, j->st) != cudaSuccess || cudaStreamSynchronize(j->st) != cudaSuccess) {
+        drop_kmer_cache(j);
+        return false;
+    }
+    j->kc_lo = j->arena.alloc_persistent<uint64_t>(P + 1);
+    j->kc_hi = j->arena.alloc_persistent<uint8_t>(P + 1);
+    if (!j->kc_lo || !j->kc_hi) {
+        drop_kmer_cache(j);
+        return false;
+    }
+    j->kc_k = k;
+    return true;
+}
+
 int chunk_records(mp_job *j, const uint64_t *chunk_starts, int nchunks, std::vector<uint64_t> &rec)
 {
     rec.assign(nchunks + 1, 0);
@@ -372,6 +419,9 @@ int mp_job_reset(mp_job *j)
     j->d_parent = j->d_size = nullptr;
     j->d_filtered = nullptr;
     j->d_out = nullptr;
+    j->kc_off = j->kc_lo = nullptr;
+    j->kc_hi = nullptr;
+    j->kc_k = 0;
     j->partitioned = j->output_ready = false;
     return 0;
 }
@@ -399,9 +449,12 @@ int mp_job_count(mp_job *j, int k, int min3, const uint64_t *chunk_starts, int n
     MP_CUDA(cudaMemsetAsync(glob, 0, NB * 8, j->st));
     MP_CUDA(cudaMemsetAsync(err, 0, 4, j->st));
     if (cc) MP_CUDA(cudaMemsetAsync(cc, 0, (size_t)nchunks * NB * 4, j->st));
+    drop_kmer_cache(j);
     {
         StageTimer tm(j->st, &j->stage_ms[1]);
-        launch_count(j->d_fq, j->pr, k, min3, d_rec, nchunks, cc, glob, err, j->st);
+        const bool kc = j->kc_on && !min3 && make_kmer_cache(j, k);
+        launch_count(j->d_fq, j->pr, k, min3, d_rec, nchunks, cc, glob, err, j->st, kc ? j->kc_off : nullptr,
+                     kc ? j->kc_lo : nullptr, kc ? j->kc_hi : nullptr);
     }
     std::vector<unsigned long long> g(NB);
     uint32_t herr = 0;
@@ -411,7 +464,10 @@ int mp_job_count(mp_job *j, int k, int min3, const uint64_t *chunk_starts, int n
     MP_CUDA(cudaStreamSynchronize(j->st));
     MP_CUDA(cudaGetLastError());
     j->arena.release_scratch();
-    if (herr & DERR_LONG_READ) return set_error(MP_EUNSUP, "a read is longer than %d bases", MAX_READ_COUNT);
+    if (herr & DERR_LONG_READ) {
+        drop_kmer_cache(j);
+        return set_error(MP_EUNSUP, "a read is longer than %d bases", MAX_READ_COUNT);
+    }
     hist_out[0] = 0;
     for (uint32_t b = 1; b <= NB; b++) hist_out[b] = hist_out[b - 1] + g[b - 1];
     if (chunk_reads_out)
@@ -476,6 +532,8 @@ int mp_job_partition(mp_job *j, const mp_part_params *p, const uint64_t *chunk_s
     char name[64], name2[64];
     // tuples per read of every scan in one pass (plain variant, monotone scan bounds)
     uint32_t *cnt_all = nullptr, *d_b = nullptr;
+    // the count pass's k-mer cache serves this partition when it holds the same k (plain variant)
+    const bool use_kc = j->kc_lo && j->kc_k == k && !p->min3 && S <= 8;
     {
         bool mono = !p->min3 && S <= 8;
         for (int s = 0; s < S && mono; s++) mono = scanR[s] <= scanR[s + 1];
@@ -486,8 +544,9 @@ int mp_job_partition(mp_job *j, const mp_part_params *p, const uint64_t *chunk_s
             std::vector<uint32_t> hb(scanR.begin(), scanR.end());
             StageTimer tm(j->st, &j->stage_ms[2]);
             MP_CUDA(cudaMemcpyAsync(d_b, hb.data(), (S + 1) * 4, cudaMemcpyHostToDevice, j->st));
-            if (launch_enum_count_scans(j->d_fq, j->pr, k, d_b, S, cnt_all, N + 1, err, j->st))
-                return set_error(MP_EARG, "enumeration count over %d scans", S);
+            const int lrc = use_kc ? launch_kc_count_scans(j->kc_off, j->kc_lo, j->kc_hi, N, k, d_b, S, cnt_all, N + 1, err, j->st)
+                                   : launch_enum_count_scans(j->d_fq, j->pr, k, d_b, S, cnt_all, N + 1, err, j->st);
+            if (lrc) return set_error(MP_EARG, "enumeration count over %d scans", S);
             for (int s = 0; s < S; s++) MP_CUDA(cudaMemsetAsync(cnt_all + (size_t)s * (N + 1) + N, 0, 4, j->st));
         }
     }
@@ -527,8 +586,12 @@ int mp_job_partition(mp_job *j, const mp_part_params *p, const uint64_t *chunk_s
                 if (!sb.lo[b] || !sb.id[b] || (has_hi && !sb.hi[b]))
                     return set_error(MP_ENOMEM, "device memory for %llu tuples", (unsigned long long)n);
             }
-            launch_enum_write(j->d_fq, j->pr, k, p->min3, (uint32_t)lo, (uint32_t)hi, s ? j->d_parent : nullptr, off,
-                              sb.lo[0], sb.hi[0], sb.id[0], err, j->st);
+            if (use_kc && cnt_all)
+                launch_kc_write(j->kc_off, j->kc_lo, j->kc_hi, N, k, (uint32_t)lo, (uint32_t)hi, s ? j->d_parent : nullptr,
+                                off, sb.lo[0], sb.hi[0], sb.id[0], j->st);
+            else
+                launch_enum_write(j->d_fq, j->pr, k, p->min3, (uint32_t)lo, (uint32_t)hi, s ? j->d_parent : nullptr, off,
+                                  sb.lo[0], sb.hi[0], sb.id[0], err, j->st);
         }
         uint32_t herr = 0;
         MP_CUDA(cudaMemcpyAsync(&herr, err, 4, cudaMemcpyDeviceToHost, j->st));
@@ -589,6 +652,7 @@ int mp_job_partition(mp_job *j, const mp_part_params *p, const uint64_t *chunk_s
     }
     j->arena.free_persistent(cnt_all);
     j->arena.free_persistent(d_b);
+    drop_kmer_cache(j);  // its HBM goes back before the mate union and the output
     {
         StageTimer tm(j->st, &j->stage_ms[6]);
         if (!j->dump_dir.empty()) {
@@ -637,6 +701,14 @@ int mp_job_output(mp_job *j, char *out, uint64_t capacity, uint64_t *file_sizes,
         MP_CUDA(cudaMemcpyAsync(out, j->d_out, j->out_total, cudaMemcpyDeviceToHost, j->st));
         MP_CUDA(cudaStreamSynchronize(j->st));
     }
+    return 0;
+}
+
+int mp_job_set_kmer_cache(mp_job *j, int enable)
+{
+    if (!j) return set_error(MP_EARG, "null job");
+    j->kc_on = enable != 0;
+    if (!j->kc_on) drop_kmer_cache(j);
     return 0;
 }
 

@@ -210,6 +210,7 @@ uint64_t mp_request_footprint(const char *fastq, uint64_t nbytes, const mp_reque
     f += tuples * 27.0;                                 // two tuple buffers of 13 B + look-back status
     f += (double)nbytes * (p->interleaved ? 2 : 1);     // partition FASTQ
     f += reads * 40.0;                                  // output entries and their sort
+    f += bases * 9.0;                                   // k-mer cache of the count pass
     f += 64.0 * (1 << 20);                              // histograms, scan scratch
     return (uint64_t)(f * 1.10);
 }

@@ -55,6 +55,7 @@ def lib():
         L.mp_job_labels.argtypes = [C.c_void_p, u32p]
         L.mp_job_output.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64, u64p, u64p]
         L.mp_job_set_dump_dir.argtypes = [C.c_void_p, C.c_char_p]
+        L.mp_job_set_kmer_cache.argtypes = [C.c_void_p, C.c_int]
         L.mp_job_stage_ms.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.c_int]
         L.mp_job_sort_stats.argtypes = [C.c_void_p, u64p, C.POINTER(C.c_int), C.POINTER(C.c_double), u64p]
         L.mp_job_sort_split.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double),
@@ -182,6 +183,10 @@ class Job:
     def num_reads(self) -> int:
         return lib().mp_job_num_reads(self.h)
 
+    def set_kmer_cache(self, enable: bool):
+        """Keep the count pass's k-mers for the next partition of the same k (default on)."""
+        _check(lib().mp_job_set_kmer_cache(self.h, int(enable)), "set_kmer_cache")
+
     def set_dump_dir(self, d: str | Path | None):
         _check(lib().mp_job_set_dump_dir(self.h, str(d).encode() if d else None), "set_dump_dir")
 
@@ -276,11 +281,12 @@ def chunk_starts_of(fno: np.ndarray, ofs: np.ndarray, file_sizes) -> np.ndarray:
 
 
 def run_pipeline(ctx: Context, fastq: bytes, k: int, num_chunks: int, num_scans: int, num_threads: int,
-                 min3: bool = False, interleaved: bool = False, dump_dir=None):
+                 min3: bool = False, interleaved: bool = False, dump_dir=None, kmer_cache: bool = True):
     """genFastqIdx -> genHistograms -> metapart on one in-memory FASTQ; returns (job, bounds, count)."""
     fno, ofs = fastq_index(num_chunks, [fastq], interleaved)
     starts = chunk_starts_of(fno, ofs, [len(fastq)])
     job = Job(ctx)
+    job.set_kmer_cache(kmer_cache)
     if dump_dir:
         job.set_dump_dir(dump_dir)
     job.load(fastq, interleaved=interleaved)
