@@ -5,6 +5,7 @@
 // 0xBADBADBAD (metapart.c:2330-2340).  Components hook the smaller root under the larger
 // one, so every component's root is its largest read id (metapart.c:2683-2716,
 // unionfind.h:58-66) regardless of the order unions run in.
+#include <algorithm>
 #include <vector>
 
 #include "k_graph.cuh"
@@ -437,36 +438,37 @@ __device__ __forceinline__ unsigned long long resv_key(uint32_t round, uint32_t 
     return ((unsigned long long)round << 32) | (0xFFFFFFFFu - j);
 }
 
-__global__ void k_pe_reserve(uint32_t *parent, const uint32_t *size, const uint32_t *act, uint32_t nact,
+// The round kernels read their list lengths from device memory (written by the previous kernel),
+// so the host launches several rounds between synchronisations; grid-stride loops cover any length.
+__global__ void k_pe_reserve(uint32_t *parent, const uint32_t *size, const uint32_t *act, const unsigned int *nact_p,
                              uint32_t *act2, unsigned int *nact2, uint32_t *pra, uint32_t *prb, uint32_t *psa,
                              uint32_t *psb, unsigned long long *resv, uint32_t round, uint32_t limit)
 {
-    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= nact) return;
-    const uint32_t j = act[t];
-    const uint32_t ra = uf_find(parent, 2 * j), rb = uf_find(parent, 2 * j + 1);
-    if (ra == rb) return;
-    const uint32_t za = size[ra], zb = size[rb];
-    const bool sa = za <= limit, sb = zb <= limit;
-    if (!sa && !sb) return;
-    pra[j] = ra;
-    prb[j] = rb;
-    psa[j] = za;  // sizes at the start of the round: the commit kernel changes sizes while it runs
-    psb[j] = zb;
-    act2[atomicAdd(nact2, 1u)] = j;
-    const unsigned long long key = resv_key(round, j);
-    if (sa) atomicMax(&resv[ra], key);
-    if (sb) atomicMax(&resv[rb], key);
+    const uint32_t nact = *nact_p;
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < nact; t += gridDim.x * blockDim.x) {
+        const uint32_t j = act[t];
+        const uint32_t ra = uf_find(parent, 2 * j), rb = uf_find(parent, 2 * j + 1);
+        if (ra == rb) continue;
+        const uint32_t za = size[ra], zb = size[rb];
+        const bool sa = za <= limit, sb = zb <= limit;
+        if (!sa && !sb) continue;
+        pra[j] = ra;
+        prb[j] = rb;
+        psa[j] = za;  // sizes at the start of the round: the commit kernel changes sizes while it runs
+        psb[j] = zb;
+        act2[atomicAdd(nact2, 1u)] = j;
+        const unsigned long long key = resv_key(round, j);
+        if (sa) atomicMax(&resv[ra], key);
+        if (sb) atomicMax(&resv[rb], key);
+    }
 }
 
-__global__ void k_pe_commit(uint32_t *parent, uint32_t *size, const uint32_t *act, uint32_t nact, uint32_t *next,
-                            unsigned int *nnext, uint32_t *pra, uint32_t *prb, const uint32_t *psa,
-                            const uint32_t *psb, const unsigned long long *resv, unsigned long long *gmax, unsigned long long *gadd,
-                            uint32_t *bigsmall, unsigned int *nbig, uint32_t round, uint32_t limit)
+__device__ __forceinline__ void pe_commit_one(uint32_t *parent, uint32_t *size, uint32_t j, uint32_t *next,
+                                              unsigned int *nnext, uint32_t *pra, uint32_t *prb, const uint32_t *psa,
+                                              const uint32_t *psb, const unsigned long long *resv, unsigned long long *gmax,
+                                              unsigned long long *gadd, uint32_t *bigsmall, unsigned int *nbig,
+                                              uint32_t round, uint32_t limit)
 {
-    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= nact) return;
-    const uint32_t j = act[t];
     const uint32_t ra = pra[j], rb = prb[j];
     const uint32_t za = psa[j], zb = psb[j];
     const bool sa = za <= limit, sb = zb <= limit;
@@ -491,12 +493,20 @@ __global__ void k_pe_commit(uint32_t *parent, uint32_t *size, const uint32_t *ac
     bigsmall[atomicAdd(nbig, 1u)] = j;
 }
 
-__global__ void k_pe_bigsmall(uint32_t *parent, uint32_t *size, const uint32_t *list, uint32_t nl, const uint32_t *pra,
-                              const uint32_t *prb, const unsigned long long *gmax, unsigned long long *gadd)
+__global__ void k_pe_commit(uint32_t *parent, uint32_t *size, const uint32_t *act, const unsigned int *nact_p, uint32_t *next,
+                            unsigned int *nnext, uint32_t *pra, uint32_t *prb, const uint32_t *psa,
+                            const uint32_t *psb, const unsigned long long *resv, unsigned long long *gmax, unsigned long long *gadd,
+                            uint32_t *bigsmall, unsigned int *nbig, uint32_t round, uint32_t limit)
 {
-    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= nl) return;
-    const uint32_t j = list[t];
+    const uint32_t nact = *nact_p;
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < nact; t += gridDim.x * blockDim.x)
+        pe_commit_one(parent, size, act[t], next, nnext, pra, prb, psa, psb, resv, gmax, gadd, bigsmall, nbig, round, limit);
+}
+
+__device__ __forceinline__ void pe_bigsmall_one(uint32_t *parent, uint32_t *size, uint32_t j, const uint32_t *pra,
+                                                const uint32_t *prb, const unsigned long long *gmax,
+                                                unsigned long long *gadd)
+{
     const uint32_t g = pra[j], x = prb[j];
     const uint32_t mx = (uint32_t)(gmax[g] & 0xFFFFFFFFu);
     const uint32_t R = mx > g ? mx : g;
@@ -516,6 +526,14 @@ __global__ void k_pe_bigsmall(uint32_t *parent, uint32_t *size, const uint32_t *
     }
     size[R] = tot;
     gadd[g] = 0;
+}
+
+__global__ void k_pe_bigsmall(uint32_t *parent, uint32_t *size, const uint32_t *list, const unsigned int *nl_p,
+                              const uint32_t *pra, const uint32_t *prb, const unsigned long long *gmax, unsigned long long *gadd)
+{
+    const uint32_t nl = *nl_p;
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < nl; t += gridDim.x * blockDim.x)
+        pe_bigsmall_one(parent, size, list[t], pra, prb, gmax, gadd);
 }
 
 // --------------------------------------------------------------- host side
@@ -599,7 +617,10 @@ int mate_union_and_plan(uint32_t *parent, uint64_t n_reads, uint32_t *size, uint
     unsigned long long *resv = arena.alloc<unsigned long long>(n_reads);
     unsigned long long *gmax = arena.alloc<unsigned long long>(n_reads);
     unsigned long long *gadd = arena.alloc<unsigned long long>(n_reads);
-    unsigned int *cnts = arena.alloc<unsigned int>(4);
+    constexpr int RB = 8;  // rounds launched between host synchronisations
+    // per round r of a batch: [4r] reserved pairs, [4r+1] pairs left for the next round, [4r+2] big-small merges;
+    // [4 RB + 1] the batch's first active count
+    unsigned int *cnts = arena.alloc<unsigned int>(4 * RB + 4);
     if (!act || !act2 || !pra || !prb || !big || !psa || !psb || !resv || !gmax || !gadd || !cnts)
         return set_error(MP_ENOMEM, "device memory for the mate union");
     MP_CUDA(cudaMemsetAsync(resv, 0, n_reads * sizeof(unsigned long long), st));
@@ -608,20 +629,32 @@ int mate_union_and_plan(uint32_t *parent, uint64_t n_reads, uint32_t *size, uint
     (mp::count_launch(), k_pe_prepare<<<blocks_for(n_reads, 256), 256, 0, st>>>(parent, n_reads, act, npairs));
     uint32_t nact = (uint32_t)npairs, round = 0;
     while (nact > 0) {
-        if (++round > 4000000u) return set_error(MP_EDEVICE, "mate union did not converge");
-        MP_CUDA(cudaMemsetAsync(cnts, 0, 4 * sizeof(unsigned int), st));
-        (mp::count_launch(), k_pe_reserve<<<blocks_for(nact, 256), 256, 0, st>>>(parent, size, act, nact, act2, cnts, pra, prb, psa, psb,
-                                                            resv, round, limit));
-        unsigned int h[3] = {0, 0, 0};
-        MP_CUDA(cudaMemcpyAsync(h, cnts, sizeof(unsigned int), cudaMemcpyDeviceToHost, st));
+        if (round + RB > 4000000u) return set_error(MP_EDEVICE, "mate union did not converge");
+        // counts only shrink, so nact bounds every list of the batch
+        const unsigned g = (unsigned)std::min<uint64_t>(blocks_for(nact, 256), 152u * 8u);
+        MP_CUDA(cudaMemsetAsync(cnts, 0, (4 * RB + 4) * sizeof(unsigned int), st));
+        MP_CUDA(cudaMemcpyAsync(cnts + 4 * RB + 1, &nact, sizeof(unsigned int), cudaMemcpyHostToDevice, st));
+        for (int r = 0; r < RB; r++) {
+            ++round;
+            const unsigned int *nin = r ? cnts + 4 * (r - 1) + 1 : cnts + 4 * RB + 1;
+            (mp::count_launch(), k_pe_reserve<<<g, 256, 0, st>>>(parent, size, act, nin, act2, cnts + 4 * r, pra, prb, psa,
+                                                                 psb, resv, round, limit));
+            (mp::count_launch(), k_pe_commit<<<g, 256, 0, st>>>(parent, size, act2, cnts + 4 * r, act, cnts + 4 * r + 1, pra,
+                                                                prb, psa, psb, resv, gmax, gadd, big, cnts + 4 * r + 2,
+                                                                round, limit));
+            (mp::count_launch(), k_pe_bigsmall<<<g, 256, 0, st>>>(parent, size, big, cnts + 4 * r + 2, pra, prb, gmax, gadd));
+        }
+        unsigned int h[4 * RB + 4];
+        MP_CUDA(cudaMemcpyAsync(h, cnts, sizeof h, cudaMemcpyDeviceToHost, st));
         MP_CUDA(cudaStreamSynchronize(st));
-        if (h[0] == 0) break;
-        (mp::count_launch(), k_pe_commit<<<blocks_for(h[0], 256), 256, 0, st>>>(parent, size, act2, h[0], act, cnts + 1, pra, prb, psa,
-                                                           psb, resv, gmax, gadd, big, cnts + 2, round, limit));
-        MP_CUDA(cudaMemcpyAsync(h, cnts, 3 * sizeof(unsigned int), cudaMemcpyDeviceToHost, st));
-        MP_CUDA(cudaStreamSynchronize(st));
-        if (h[2]) (mp::count_launch(), k_pe_bigsmall<<<blocks_for(h[2], 256), 256, 0, st>>>(parent, size, big, h[2], pra, prb, gmax, gadd));
-        nact = h[1];
+        nact = h[4 * (RB - 1) + 1];
+        // rounds that reserved nothing leave nothing active: stop counting at the first empty one
+        for (int r = 0; r < RB; r++)
+            if (h[4 * r] == 0) {
+                round -= (uint32_t)(RB - 1 - r);
+                nact = 0;
+                break;
+            }
     }
     if (rounds_out) *rounds_out = (int)round;
     // final printStats: compress and recount (metapart.c:4026-4030)

@@ -94,7 +94,7 @@ __device__ __forceinline__ uint32_t digit_of(uint64_t lo, uint32_t hi, int shift
 }
 
 template <int SRC>
-__global__ void __launch_bounds__(ST, 2) k_onesweep(const uint64_t *__restrict__ in_lo, const uint8_t *__restrict__ in_hi,
+__global__ void __launch_bounds__(ST, 3) k_onesweep(const uint64_t *__restrict__ in_lo, const uint8_t *__restrict__ in_hi,
                                                     const uint32_t *__restrict__ in_id, uint64_t *__restrict__ out_lo,
                                                     uint8_t *__restrict__ out_hi, uint32_t *__restrict__ out_id, uint64_t n,
                                                     int shift, const uint64_t *__restrict__ dbase,

@@ -359,6 +359,7 @@ static int load_common(mp_job *j, uint64_t nbytes, const uint64_t *file_sizes, i
     if (tot != nbytes) return set_error(MP_EARG, "file sizes do not add up to the input size");
     j->fq_bytes = nbytes;
     j->interleaved = interleaved;
+    j->stage_ms[0] = 0;
     {
         StageTimer tm(j->st, &j->stage_ms[0]);
         int rc = parse_fastq(j->d_fq, nbytes, &j->pr, j->arena, j->st);
