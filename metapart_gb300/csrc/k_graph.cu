@@ -302,6 +302,7 @@ struct EdgeCtx {
     uint32_t init_min;             // read id of the scan's first tuple (metapart.c:2543-2545)
     uint32_t init_min_ok;          // that read is not BAD
     uint32_t *parent;
+    const uint8_t *filtered;       // BAD flags: during the scans a read's parent is BAD exactly when it is flagged
     uint32_t *err;
 };
 
@@ -334,7 +335,7 @@ __global__ void __launch_bounds__(256) k_edges_warp(EdgeCtx c)
         prev_km = __shfl_sync(FULLW, km, 31);
         const bool nz = valid && km != 0 && !zbit(c.z, i);
         const uint32_t r = nz ? c.id[i] : 0;
-        const bool good = nz && c.parent[r] != BAD;
+        const bool good = nz && !c.filtered[r];  // the 1-byte flags keep the probe L2-friendly
         const uint32_t G = __ballot_sync(FULLW, good);
         const int fh = H ? __ffs(H) - 1 : 32;
         const bool arr_end = p + 32 >= c.n;
@@ -559,8 +560,8 @@ int filter_scan(Tuples &tp, const std::vector<uint64_t> &range_bounds, uint32_t 
     return 0;
 }
 
-int union_scan(Tuples &tp, const std::vector<uint64_t> &range_bounds, uint32_t *parent, uint64_t n_reads,
-               DeviceArena &arena, cudaStream_t st)
+int union_scan(Tuples &tp, const std::vector<uint64_t> &range_bounds, uint32_t *parent, const uint8_t *filtered,
+               uint64_t n_reads, DeviceArena &arena, cudaStream_t st)
 {
     const uint64_t n = tp.n;
     const int T = (int)range_bounds.size() - 1;
@@ -585,7 +586,7 @@ int union_scan(Tuples &tp, const std::vector<uint64_t> &range_bounds, uint32_t *
         MP_CUDA(cudaStreamSynchronize(st));
         EdgeCtx c;
         c.lo = tp.lo; c.hi = tp.hi; c.id = tp.id; c.z = tp.z; c.n = n;
-        c.first_valid = first; c.range_bounds = bounds; c.T = T; c.parent = parent; c.err = err;
+        c.first_valid = first; c.range_bounds = bounds; c.T = T; c.parent = parent; c.filtered = filtered; c.err = err;
         c.init_kmer = ((zw >> ((n - 1) & 31)) & 1u) ? 0 : ((last_lo >> 8) | ((uint64_t)last_hi << 56));
         c.init_min = first_id;
         c.init_min_ok = first_parent != BAD;

@@ -18,8 +18,8 @@ struct Tuples {
 int filter_scan(Tuples &tp, const std::vector<uint64_t> &range_bounds, uint32_t *parent, uint8_t *filtered,
                 DeviceArena &arena, cudaStream_t st, bool apply_zero);
 // K5: unionFindPar2 + unionFind + printStats compression for the scan.
-int union_scan(Tuples &tp, const std::vector<uint64_t> &range_bounds, uint32_t *parent, uint64_t n_reads,
-               DeviceArena &arena, cudaStream_t st);
+int union_scan(Tuples &tp, const std::vector<uint64_t> &range_bounds, uint32_t *parent, const uint8_t *filtered,
+               uint64_t n_reads, DeviceArena &arena, cudaStream_t st);
 // K6: sizes, unionFindPeReads(1000), final compression and the 17 partition bounds (host).
 int mate_union_and_plan(uint32_t *parent, uint64_t n_reads, uint32_t *size, uint64_t *bounds_out, DeviceArena &arena,
                         cudaStream_t st, int *rounds_out);

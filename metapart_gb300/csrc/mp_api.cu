@@ -645,7 +645,7 @@ int mp_job_partition(mp_job *j, const mp_part_params *p, const uint64_t *chunk_s
         }
         {
             StageTimer tm(j->st, &j->stage_ms[5]);
-            if ((rc = union_scan(tp, rb, j->d_parent, N, j->arena, j->st))) return rc;
+            if ((rc = union_scan(tp, rb, j->d_parent, j->d_filtered, N, j->arena, j->st))) return rc;
         }
         j->arena.release_scratch();
         snprintf(name, sizeof name, "stats%d_parent.bin", s);
