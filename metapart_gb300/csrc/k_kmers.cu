@@ -104,13 +104,11 @@ __global__ void __launch_bounds__(256) k_count_plain(const uint8_t *fq, const ui
                     kc_hi[kbase + i] = v ? (uint8_t)(canon >> 56) : KC_NONE;
                 }
             }
-            const uint32_t act = __ballot_sync(FULL, v);
+            // one reduction per k-mer: neighbouring positions almost never share a bucket, so grouping
+            // equal buckets within the warp first costs more than it saves
             if (v) {
-                const uint32_t peers = __match_any_sync(act, b);
-                if (lane == __ffs(peers) - 1) {
-                    if (ccc) atomicAdd(&ccc[b], (uint32_t)__popc(peers));
-                    else atomicAdd(&glob[b], (unsigned long long)__popc(peers));
-                }
+                if (ccc) atomicAdd(&ccc[b], 1u);
+                else atomicAdd(&glob[b], 1ull);
             }
             prv = cur;
             cur = nxt;

@@ -503,12 +503,23 @@ __global__ void __launch_bounds__(SS_THREADS) k_segsort(const uint64_t *__restri
             }
         }
         const long long t2 = clock64();
-        for (uint32_t e = threadIdx.x; e < cnt; e += SS_THREADS) {
-            const uint32_t sidx = cur < 0 ? e : (uint32_t)sm.perm[cur][e];
-            const uint64_t key = sm.key[sidx];
-            const uint64_t bucket = b0 + (key >> lowbits);
-            lo_out[start + e] = (bucket << lowbits) | (key & lowmask);
-            id_out[start + e] = id_in[start + sidx];
+        for (uint32_t e0 = threadIdx.x; e0 < cnt; e0 += 4 * SS_THREADS) {  // four id gathers in flight
+            uint32_t sidx[4], idv[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const uint32_t e = e0 + q * SS_THREADS;
+                sidx[q] = e < cnt ? (cur < 0 ? e : (uint32_t)sm.perm[cur][e]) : 0u;
+                idv[q] = e < cnt ? id_in[start + sidx[q]] : 0u;
+            }
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const uint32_t e = e0 + q * SS_THREADS;
+                if (e >= cnt) break;
+                const uint64_t key = sm.key[sidx[q]];
+                const uint64_t bucket = b0 + (key >> lowbits);
+                lo_out[start + e] = (bucket << lowbits) | (key & lowmask);
+                id_out[start + e] = idv[q];
+            }
         }
         __syncthreads();  // the next unit reuses the shared arrays
         cyc[0] += (unsigned long long)(t1 - t0);

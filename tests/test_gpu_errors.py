@@ -106,3 +106,17 @@ def test_context_usable_after_errors(ctx):
         assert int(bounds[16]) == 2000
         out, sizes = job.output()
         assert int(sizes.sum()) == len(data)
+
+
+def test_no_kmers_at_all(ctx):
+    # every read shorter than k: the reference's range planner crashes on the empty histogram; here it is a
+    # typed error from the partition, after a count that reports an all-zero histogram
+    recs = b"".join(b"@r%d\n%s\n+\n%s\n" % (i, b"ACGTACGTAC"[: 5 + i % 6], b"I" * (5 + i % 6)) for i in range(40))
+    with native.Job(ctx) as j:
+        j.load(recs)
+        starts = np.array([0, len(recs)], dtype=np.uint64)
+        cnt = j.count(27, starts)
+        assert int(cnt.hist[-1]) == 0
+        with pytest.raises(native.MetapartError) as e:
+            j.partition(27, 1, 1, starts, cnt.chunk_first_read, cnt.hist)
+        assert code(e.value) == EUNSUP
