@@ -135,12 +135,18 @@ __global__ void __launch_bounds__(ST, 3) k_onesweep(const uint64_t *__restrict__
         hv[j >> 2] |= h << (8 * (j & 3));
         rd[j] = (v ? digit_of<SRC>(key[j], h, shift) : 256u) << 16;
     }
-    // warp-level multi-split: stable rank of each tuple among equal digits of its warp
+    // warp-level multi-split: stable rank of each tuple among equal digits of its warp; the lanes holding a
+    // digit come from its eight bit-plane ballots
     const uint32_t lt = (1u << lane) - 1;
 #pragma unroll
     for (int j = 0; j < SI; j++) {
         const uint32_t d = rd[j] >> 16;
-        const uint32_t peers = __match_any_sync(FULLM, d);
+        uint32_t peers = __ballot_sync(FULLM, d < 256);
+#pragma unroll
+        for (int b = 0; b < 8; b++) {
+            const uint32_t bb = __ballot_sync(FULLM, (d >> b) & 1u);
+            peers &= ((d >> b) & 1u) ? bb : ~bb;
+        }
         uint32_t pre = 0;
         if (d < 256) pre = sm.whist[warp][d];
         __syncwarp();
