@@ -60,6 +60,7 @@ __device__ __forceinline__ uint32_t chunk_of(const uint64_t *chunk_rec, int nchu
 // when the window holds an N.  Written by the count pass when kc_lo is given; the partition's
 // scans then filter this array instead of recomputing k-mers.
 constexpr uint8_t KC_NONE = 0xFF;
+constexpr int KC_PER_LANE = 10;  // cached positions per lane of a read: L - k + 1 <= 300
 
 __global__ void __launch_bounds__(256) k_count_plain(const uint8_t *fq, const uint64_t *seq_off, const uint32_t *seq_len,
                                                      uint64_t r0, uint64_t r1, int k, const uint64_t *chunk_rec,
@@ -364,10 +365,19 @@ __global__ void __launch_bounds__(256) k_kc_count_scans(const uint64_t *kc_off, 
         if (np > 300) {  // L - k >= 300 (enumerateKmers.c:155)
             if (lane == 0) atomicOr(err, DERR_LONG_READ);
         } else {
-            for (uint64_t i = lane; i < np; i += 32) {
-                const uint8_t h = kc_hi[p0 + i];
-                if (h == KC_NONE) continue;
-                const uint64_t km = (kc_lo[p0 + i] >> 8) | ((uint64_t)h << 56);
+            // every position of the read (at most 300: 10 per lane) loaded at once
+            uint64_t lv[KC_PER_LANE];
+            uint32_t hv[KC_PER_LANE];
+#pragma unroll
+            for (int t = 0; t < KC_PER_LANE; t++) {
+                const uint64_t i = (uint64_t)t * 32 + lane;
+                lv[t] = i < np ? kc_lo[p0 + i] : 0ull;
+                hv[t] = i < np ? (uint32_t)kc_hi[p0 + i] : (uint32_t)KC_NONE;
+            }
+#pragma unroll
+            for (int t = 0; t < KC_PER_LANE; t++) {
+                if (hv[t] == KC_NONE) continue;
+                const uint64_t km = (lv[t] >> 8) | ((uint64_t)hv[t] << 56);
                 const uint32_t b = (uint32_t)(km >> sh);
                 if (b < b_lo || b >= b_hi) continue;
                 int sc = 0;
@@ -407,22 +417,26 @@ __global__ void __launch_bounds__(256) k_kc_write(const uint64_t *kc_off, const 
             id = (p == BAD) ? (uint32_t)r : p;  // findRoot after full compression (metapart.c:543-568)
         }
         uint64_t base = out_off[r];
-        for (uint64_t i0 = 0; i0 < np; i0 += 32) {
-            const uint64_t i = i0 + lane;
-            uint64_t l = 0;
-            uint8_t h = KC_NONE;
-            if (i < np) {
-                l = kc_lo[p0 + i];
-                h = kc_hi[p0 + i];
-            }
-            const uint64_t km = (l >> 8) | ((uint64_t)h << 56);
+        // every position of the read (at most 300: 10 per lane) loaded at once
+        uint64_t lv[KC_PER_LANE];
+        uint32_t hv[KC_PER_LANE];
+#pragma unroll
+        for (int t = 0; t < KC_PER_LANE; t++) {
+            const uint64_t i = (uint64_t)t * 32 + lane;
+            lv[t] = i < np ? kc_lo[p0 + i] : 0ull;
+            hv[t] = i < np ? (uint32_t)kc_hi[p0 + i] : (uint32_t)KC_NONE;
+        }
+#pragma unroll
+        for (int t = 0; t < KC_PER_LANE; t++) {
+            if ((uint64_t)t * 32 >= np) break;  // uniform across the warp
+            const uint64_t km = (lv[t] >> 8) | ((uint64_t)hv[t] << 56);
             const uint32_t b = (uint32_t)(km >> sh);
-            const bool v = h != KC_NONE && b >= lo && b < hi;
+            const bool v = hv[t] != KC_NONE && b >= lo && b < hi;
             const uint32_t bal = __ballot_sync(FULL, v);
             if (v) {
                 const uint64_t pos = base + __popc(bal & ((1u << lane) - 1));
-                o_lo[pos] = l;
-                if (o_hi) o_hi[pos] = h;
+                o_lo[pos] = lv[t];
+                if (o_hi) o_hi[pos] = (uint8_t)hv[t];
                 o_id[pos] = id;
             }
             base += __popc(bal);
