@@ -566,6 +566,122 @@ __global__ void k_big_scatter(const uint64_t *__restrict__ bstart, const uint32_
     }
 }
 
+// ---- planning of one scan's bucket sort on the device, from the .kmerHist prefix (d_hist, 1048577 u64)
+
+
+// Digit counts of the three bucket bytes (weighted by the bucket counts) and the populated-bucket flags.
+__global__ void k_bp_count(const uint64_t *__restrict__ hist, uint64_t lo, uint64_t nbk, unsigned long long *dcnt,
+                           uint32_t *pop)
+{
+    __shared__ unsigned long long h[3 * 256];
+    for (int i = threadIdx.x; i < 3 * 256; i += blockDim.x) h[i] = 0;
+    __syncthreads();
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nbk; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t b = lo + i, c = hist[b + 1] - hist[b];
+        pop[i] = c ? 1u : 0u;
+        if (!c) continue;
+#pragma unroll
+        for (int d = 0; d < 3; d++) atomicAdd(&h[d * 256 + ((b >> (8 * d)) & 0xFF)], (unsigned long long)c);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < 3 * 256; i += blockDim.x)
+        if (h[i]) atomicAdd(&dcnt[i], h[i]);
+}
+
+// Exclusive digit offsets; konst[d] = 1 when digit d takes one value for all n tuples.  One block of 256.
+__global__ void k_bp_digits(const unsigned long long *dcnt, uint64_t n, uint64_t *dbase, uint32_t *konst)
+{
+    __shared__ unsigned long long ws[8];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int d = 0; d < 3; d++) {
+        const unsigned long long c = dcnt[d * 256 + threadIdx.x];
+        unsigned long long x = c;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned long long y = __shfl_up_sync(FULLM, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) ws[warp] = x;
+        __syncthreads();
+        unsigned long long before = 0;
+        for (int w = 0; w < warp; w++) before += ws[w];
+        dbase[d * 256 + threadIdx.x] = before + x - c;
+        const int one = __syncthreads_or(c == n);  // also keeps ws intact until every warp has read it
+        if (threadIdx.x == 0) konst[d] = (uint32_t)one;
+    }
+}
+
+__global__ void k_bp_compact(const uint32_t *pop, const uint64_t *popoff, uint64_t lo, uint64_t nbk, uint32_t *P)
+{
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < nbk && pop[i]) P[popoff[i]] = (uint32_t)(lo + i);
+}
+
+constexpr int BP_BLOCK = 256;  // populated buckets packed greedily by one thread
+
+// Greedy packing of consecutive populated buckets into units (at most SS_CAP tuples, SS_MAXB buckets),
+// one thread per block of BP_BLOCK populated buckets; buckets above SS_CAP are listed apart.  Units never
+// cross a block, so each block ends with one partial unit.  Block g writes its units from g * BP_BLOCK
+// into the staging arrays and their counts to nu_blk[g], nb_blk[g].
+__global__ void k_bp_greedy(const uint32_t *P, uint64_t np, const uint64_t *__restrict__ hist, uint64_t lo,
+                            uint64_t *sus, uint32_t *suc, uint32_t *sub, uint64_t *sbs, uint32_t *sbc, uint32_t *sbb,
+                            uint32_t *nu_blk, uint32_t *nb_blk)
+{
+    const uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const uint64_t i0 = g * BP_BLOCK;
+    if (i0 >= np) return;
+    const uint64_t i1 = min(np, i0 + BP_BLOCK), base = hist[lo];
+    uint32_t nu = 0, nb = 0, u_b0 = 0;
+    uint64_t u_start = 0, u_cnt = 0;
+    bool have = false;
+    for (uint64_t i = i0; i < i1; i++) {
+        const uint64_t bk = P[i], c = hist[bk + 1] - hist[bk], s = hist[bk] - base;
+        if (c > (uint64_t)SS_CAP) {
+            if (have) {
+                sus[i0 + nu] = u_start; suc[i0 + nu] = (uint32_t)u_cnt; sub[i0 + nu] = u_b0; nu++;
+                have = false;
+            }
+            sbs[i0 + nb] = s; sbc[i0 + nb] = (uint32_t)c; sbb[i0 + nb] = (uint32_t)bk; nb++;
+            continue;
+        }
+        if (have && (u_cnt + c > (uint64_t)SS_CAP || bk - u_b0 >= SS_MAXB)) {
+            sus[i0 + nu] = u_start; suc[i0 + nu] = (uint32_t)u_cnt; sub[i0 + nu] = u_b0; nu++;
+            have = false;
+        }
+        if (!have) {
+            have = true;
+            u_start = s;
+            u_cnt = 0;
+            u_b0 = (uint32_t)bk;
+        }
+        u_cnt += c;
+    }
+    if (have) { sus[i0 + nu] = u_start; suc[i0 + nu] = (uint32_t)u_cnt; sub[i0 + nu] = u_b0; nu++; }
+    nu_blk[g] = nu;
+    nb_blk[g] = nb;
+}
+
+// Staged per-block units and oversized buckets into dense arrays (offsets from scans of the block counts).
+__global__ void k_bp_gather(uint64_t nblk, const uint32_t *nu_blk, const uint64_t *uoff, const uint32_t *nb_blk,
+                            const uint64_t *boff, const uint64_t *sus, const uint32_t *suc, const uint32_t *sub,
+                            const uint64_t *sbs, const uint32_t *sbc, const uint32_t *sbb, uint64_t *us, uint32_t *uc,
+                            uint32_t *ub, uint64_t *bs, uint32_t *bc, uint32_t *bb)
+{
+    const uint64_t g = blockIdx.x;
+    if (g >= nblk) return;
+    const uint64_t i0 = g * BP_BLOCK;
+    for (uint32_t q = threadIdx.x; q < nu_blk[g]; q += blockDim.x) {
+        us[uoff[g] + q] = sus[i0 + q];
+        uc[uoff[g] + q] = suc[i0 + q];
+        ub[uoff[g] + q] = sub[i0 + q];
+    }
+    for (uint32_t q = threadIdx.x; q < nb_blk[g]; q += blockDim.x) {
+        bs[boff[g] + q] = sbs[i0 + q];
+        bc[boff[g] + q] = sbc[i0 + q];
+        bb[boff[g] + q] = sbb[i0 + q];
+    }
+}
+
 // Widest digit of the unit sort (MP_UNIT_SORT_MAX_BITS, 5..10; default 10).  The tests also run
 // narrower digits, which change every unit's pass plan.
 static int unit_sort_max_bits()
@@ -596,40 +712,48 @@ static void sort_kernel_attrs()
     });
 }
 
-int bucket_sort(SortBufs &b, uint64_t n, bool has_hi, int k, const uint64_t *hist, uint64_t scan_lo, uint64_t scan_hi,
+int bucket_sort(SortBufs &b, uint64_t n, bool has_hi, int k, const uint64_t *d_hist, uint64_t scan_lo, uint64_t scan_hi,
                 DeviceArena &arena, cudaStream_t st, SortStats *stats, int *out_lo_buf, int *out_hi_buf)
 {
     if (stats) *stats = SortStats{};
     *out_lo_buf = *out_hi_buf = b.cur;
     if (n <= 1) return 0;
+    if (scan_hi <= scan_lo) return set_error(MP_EFMT, "the histogram does not match the scan's tuples");
     const int bsh = 2 * (k - 10), lowbits = 2 * (k - 10) + 8;
-    // bucket digit offsets from the histogram: digit d = byte d of the bucket
-    std::vector<uint64_t> base(3 * 256, 0), cnt(3 * 256, 0);
-    for (uint64_t bk = scan_lo; bk < scan_hi; bk++) {
-        const uint64_t c = hist[bk + 1] - hist[bk];
-        for (int d = 0; d < 3; d++) cnt[d * 256 + ((bk >> (8 * d)) & 0xFF)] += c;
+    const uint64_t nbk = scan_hi - scan_lo;
+    // ---- plan on the device: digit offsets of the bucket bytes, populated buckets
+    unsigned long long *dcnt = arena.alloc<unsigned long long>(3 * 256);
+    uint64_t *dbase = arena.alloc<uint64_t>(3 * 256), *tot = arena.alloc<uint64_t>(4), *popoff = arena.alloc<uint64_t>(nbk + 2);
+    uint32_t *konst = arena.alloc<uint32_t>(4), *pop = arena.alloc<uint32_t>(nbk + 1);
+    const size_t tbp = scan_tmp_bytes(nbk + 1);
+    void *tmp = arena.alloc<uint8_t>(tbp);
+    if (!dcnt || !dbase || !tot || !popoff || !konst || !pop || !tmp) return set_error(MP_ENOMEM, "device memory for the bucket sort");
+    MP_CUDA(cudaMemsetAsync(dcnt, 0, 3 * 256 * sizeof(unsigned long long), st));
+    MP_CUDA(cudaMemsetAsync(pop + nbk, 0, sizeof(uint32_t), st));
+    {
+        const unsigned g = (unsigned)std::min<uint64_t>((nbk + 255) / 256, 152u * 8u);
+        (mp::count_launch(), k_bp_count<<<g, 256, 0, st>>>(d_hist, scan_lo, nbk, dcnt, pop));
     }
+    (mp::count_launch(), k_bp_digits<<<1, 256, 0, st>>>(dcnt, n, dbase, konst));
+    scan_u32_to_u64(pop, popoff, nbk + 1, tot, tmp, tbp, st);
+    uint64_t hd[3] = {0, 0, 0};  // populated buckets; digit 0's last count and offset
+    uint32_t hk[4] = {0, 0, 0, 0};
+    MP_CUDA(cudaMemcpyAsync(&hd[0], tot, 8, cudaMemcpyDeviceToHost, st));
+    MP_CUDA(cudaMemcpyAsync(&hd[1], dcnt + 255, 8, cudaMemcpyDeviceToHost, st));
+    MP_CUDA(cudaMemcpyAsync(&hd[2], dbase + 255, 8, cudaMemcpyDeviceToHost, st));
+    MP_CUDA(cudaMemcpyAsync(hk, konst, 3 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    MP_CUDA(cudaStreamSynchronize(st));
+    if (hd[1] + hd[2] != n) return set_error(MP_EFMT, "the histogram does not match the scan's tuples");
+    const uint64_t np = hd[0];
     std::vector<int> passes;
-    for (int d = 0; d < 3; d++) {
-        uint64_t acc = 0;
-        bool constant = false;
-        for (int v = 0; v < 256; v++) {
-            base[d * 256 + v] = acc;
-            if (cnt[d * 256 + v] == n) constant = true;
-            acc += cnt[d * 256 + v];
-        }
-        if (acc != n) return set_error(MP_EFMT, "the histogram does not match the scan's tuples");
-        if (!constant) passes.push_back(d);
-    }
+    for (int d = 0; d < 3; d++)
+        if (!hk[d]) passes.push_back(d);
     const uint64_t tiles = (n + STILE - 1) / STILE;
-    uint64_t *dbase = arena.alloc<uint64_t>(3 * 256);
     uint32_t *ctr = arena.alloc<uint32_t>(8), *err = arena.alloc<uint32_t>(1);
     unsigned long long *trace = arena.alloc<unsigned long long>(8);
-    if (!trace) return set_error(MP_ENOMEM, "device memory for the bucket sort");
-    MP_CUDA(cudaMemsetAsync(trace, 0, 8 * sizeof(unsigned long long), st));
     unsigned long long *status = passes.empty() ? nullptr : arena.alloc<unsigned long long>(tiles * 256);
-    if (!dbase || !ctr || !err || (!passes.empty() && !status)) return set_error(MP_ENOMEM, "device memory for the bucket sort");
-    MP_CUDA(cudaMemcpyAsync(dbase, base.data(), base.size() * 8, cudaMemcpyHostToDevice, st));
+    if (!ctr || !err || !trace || (!passes.empty() && !status)) return set_error(MP_ENOMEM, "device memory for the bucket sort");
+    MP_CUDA(cudaMemsetAsync(trace, 0, 8 * sizeof(unsigned long long), st));
     MP_CUDA(cudaMemsetAsync(ctr, 0, 8 * sizeof(uint32_t), st));
     MP_CUDA(cudaMemsetAsync(err, 0, sizeof(uint32_t), st));
     if (status) MP_CUDA(cudaMemsetAsync(status, 0, tiles * 256 * sizeof(unsigned long long), st));
@@ -647,51 +771,52 @@ int bucket_sort(SortBufs &b, uint64_t n, bool has_hi, int k, const uint64_t *his
         b.cur = dst;
     }
     cudaEventRecord(ev[1], st);
-    // units of consecutive buckets, and the big buckets
-    std::vector<uint64_t> us, bs, bo;
-    std::vector<uint32_t> uc, ub, bc, bb;
-    {
-        uint64_t pos = 0, u_start = 0, u_cnt = 0, off = 0;
-        uint32_t u_b0 = (uint32_t)scan_lo;
-        bool have = false;
-        for (uint64_t bk = scan_lo; bk < scan_hi; bk++) {
-            const uint64_t c = hist[bk + 1] - hist[bk];
-            if (c == 0) continue;
-            if (c > (uint64_t)SS_CAP) {
-                if (have) { us.push_back(u_start); uc.push_back((uint32_t)u_cnt); ub.push_back(u_b0); have = false; }
-                bs.push_back(pos); bc.push_back((uint32_t)c); bb.push_back((uint32_t)bk); bo.push_back(off);
-                off += c;
-            } else {
-                if (have && (u_cnt + c > (uint64_t)SS_CAP || bk - u_b0 >= SS_MAXB)) {
-                    us.push_back(u_start); uc.push_back((uint32_t)u_cnt); ub.push_back(u_b0); have = false;
-                }
-                if (!have) { have = true; u_start = pos; u_cnt = 0; u_b0 = (uint32_t)bk; }
-                u_cnt += c;
-            }
-            pos += c;
-        }
-        if (have) { us.push_back(u_start); uc.push_back((uint32_t)u_cnt); ub.push_back(u_b0); }
+    // ---- units of consecutive buckets and the oversized buckets, planned on the device
+    const uint64_t nblk = (np + BP_BLOCK - 1) / BP_BLOCK;
+    const uint64_t cap = nblk * BP_BLOCK + 1;
+    uint32_t *P = arena.alloc<uint32_t>(np + 1), *nu_blk = arena.alloc<uint32_t>(nblk + 1), *nb_blk = arena.alloc<uint32_t>(nblk + 1);
+    uint64_t *uoff = arena.alloc<uint64_t>(nblk + 2), *boff = arena.alloc<uint64_t>(nblk + 2);
+    uint64_t *s_us = arena.alloc<uint64_t>(cap), *s_bs = arena.alloc<uint64_t>(cap);
+    uint32_t *s_uc = arena.alloc<uint32_t>(cap), *s_ub = arena.alloc<uint32_t>(cap);
+    uint32_t *s_bc = arena.alloc<uint32_t>(cap), *s_bb = arena.alloc<uint32_t>(cap);
+    uint64_t *d_us = arena.alloc<uint64_t>(np + 1), *d_bs = arena.alloc<uint64_t>(np + 1);
+    uint32_t *d_uc = arena.alloc<uint32_t>(np + 1), *d_ub = arena.alloc<uint32_t>(np + 1);
+    uint32_t *d_bc = arena.alloc<uint32_t>(np + 1), *d_bb = arena.alloc<uint32_t>(np + 1);
+    const size_t tb2 = scan_tmp_bytes(nblk + 1);
+    void *tmp2 = arena.alloc<uint8_t>(tb2), *tmp3 = arena.alloc<uint8_t>(tb2);
+    if (!P || !nu_blk || !nb_blk || !uoff || !boff || !s_us || !s_bs || !s_uc || !s_ub || !s_bc || !s_bb || !d_us || !d_bs ||
+        !d_uc || !d_ub || !d_bc || !d_bb || !tmp2 || !tmp3)
+        return set_error(MP_ENOMEM, "device memory for sort units");
+    (mp::count_launch(), k_bp_compact<<<(unsigned)((nbk + 255) / 256), 256, 0, st>>>(pop, popoff, scan_lo, nbk, P));
+    MP_CUDA(cudaMemsetAsync(nu_blk, 0, (nblk + 1) * sizeof(uint32_t), st));
+    MP_CUDA(cudaMemsetAsync(nb_blk, 0, (nblk + 1) * sizeof(uint32_t), st));
+    if (nblk) {
+        (mp::count_launch(), k_bp_greedy<<<(unsigned)((nblk + 127) / 128), 128, 0, st>>>(P, np, d_hist, scan_lo, s_us, s_uc, s_ub,
+                                                                                      s_bs, s_bc, s_bb, nu_blk, nb_blk));
     }
+    scan_u32_to_u64(nu_blk, uoff, nblk + 1, tot + 1, tmp2, tb2, st);
+    scan_u32_to_u64(nb_blk, boff, nblk + 1, tot + 2, tmp3, tb2, st);
+    if (nblk)
+        (mp::count_launch(), k_bp_gather<<<(unsigned)nblk, 128, 0, st>>>(nblk, nu_blk, uoff, nb_blk, boff, s_us, s_uc, s_ub, s_bs,
+                                                                       s_bc, s_bb, d_us, d_uc, d_ub, d_bs, d_bc, d_bb));
+    uint64_t hn[2] = {0, 0};
+    MP_CUDA(cudaMemcpyAsync(hn, tot + 1, 2 * sizeof(uint64_t), cudaMemcpyDeviceToHost, st));
+    MP_CUDA(cudaStreamSynchronize(st));
+    const uint64_t nu = hn[0], nb = hn[1];
     const int in = b.cur, out = b.cur ^ 1;
-    const size_t nu = us.size(), nb = bs.size();
-    uint64_t *d_us = arena.alloc<uint64_t>(nu + 1), *d_bs = arena.alloc<uint64_t>(nb + 1), *d_bo = arena.alloc<uint64_t>(nb + 1);
-    uint32_t *d_uc = arena.alloc<uint32_t>(nu + 1), *d_ub = arena.alloc<uint32_t>(nu + 1);
-    uint32_t *d_bc = arena.alloc<uint32_t>(nb + 1), *d_bb = arena.alloc<uint32_t>(nb + 1);
-    if (!d_us || !d_bs || !d_bo || !d_uc || !d_ub || !d_bc || !d_bb) return set_error(MP_ENOMEM, "device memory for sort units");
-    if (nu) {
-        MP_CUDA(cudaMemcpyAsync(d_us, us.data(), nu * 8, cudaMemcpyHostToDevice, st));
-        MP_CUDA(cudaMemcpyAsync(d_uc, uc.data(), nu * 4, cudaMemcpyHostToDevice, st));
-        MP_CUDA(cudaMemcpyAsync(d_ub, ub.data(), nu * 4, cudaMemcpyHostToDevice, st));
-        (mp::count_launch(), k_segsort<<<(unsigned)std::min<size_t>(nu, (size_t)sm_count()), SS_THREADS, sizeof(SegSmem), st>>>(
+    if (nu)
+        (mp::count_launch(), k_segsort<<<(unsigned)std::min<uint64_t>(nu, (uint64_t)sm_count()), SS_THREADS, sizeof(SegSmem), st>>>(
             d_us, d_uc, d_ub, (uint32_t)nu, b.lo[in], has_hi ? b.hi[in] : nullptr, b.id[in], b.lo[out], b.id[out], bsh,
             lowbits, unit_sort_max_bits(), trace));
-    }
     cudaEventRecord(ev[2], st);
     uint64_t nbig = 0;
     if (nb) {
-        MP_CUDA(cudaMemcpyAsync(d_bs, bs.data(), nb * 8, cudaMemcpyHostToDevice, st));
-        MP_CUDA(cudaMemcpyAsync(d_bc, bc.data(), nb * 4, cudaMemcpyHostToDevice, st));
-        MP_CUDA(cudaMemcpyAsync(d_bb, bb.data(), nb * 4, cudaMemcpyHostToDevice, st));
+        std::vector<uint32_t> bc(nb);
+        std::vector<uint64_t> bo(nb);
+        MP_CUDA(cudaMemcpyAsync(bc.data(), d_bc, nb * 4, cudaMemcpyDeviceToHost, st));
+        MP_CUDA(cudaStreamSynchronize(st));
+        uint64_t *d_bo = arena.alloc<uint64_t>(nb + 1);
+        if (!d_bo) return set_error(MP_ENOMEM, "device memory for oversized buckets");
         // batches of oversized buckets whose index fits above the low key bits
         const size_t per_batch = lowbits >= 44 ? ((size_t)1 << (64 - lowbits)) : ((size_t)1 << 20);
         uint64_t maxbatch = 0;
@@ -708,7 +833,7 @@ int bucket_sort(SortBufs &b, uint64_t n, bool has_hi, int k, const uint64_t *his
             if (!t.lo[q] || !t.id[q]) return set_error(MP_ENOMEM, "device memory for oversized buckets");
         }
         for (size_t b0 = 0; b0 < nb; b0 += per_batch) {
-            const size_t b1 = std::min(nb, b0 + per_batch);
+            const size_t b1 = std::min<size_t>(nb, b0 + per_batch);
             uint64_t acc = 0;
             for (size_t q = b0; q < b1; q++) { bo[q] = acc; acc += bc[q]; }
             MP_CUDA(cudaMemcpyAsync(d_bo + b0, bo.data() + b0, (b1 - b0) * 8, cudaMemcpyHostToDevice, st));

@@ -29,9 +29,9 @@ struct SortStats {
 int radix_sort(SortBufs &b, uint64_t n, bool has_hi, DeviceArena &arena, cudaStream_t st, SortStats *stats);
 
 // Stable sort of one scan's tuples by (k-mer, adjacency) using the scan's m-mer bucket counts
-// (hist, buckets [scan_lo, scan_hi)).  On return lo/id are in b.*[*out_lo_buf] and hi in
-// b.hi[*out_hi_buf].
-int bucket_sort(SortBufs &b, uint64_t n, bool has_hi, int k, const uint64_t *hist, uint64_t scan_lo, uint64_t scan_hi,
+// (d_hist: the 1048577-entry .kmerHist prefix in device memory, buckets [scan_lo, scan_hi)).  On return
+// lo/id are in b.*[*out_lo_buf] and hi in b.hi[*out_hi_buf].
+int bucket_sort(SortBufs &b, uint64_t n, bool has_hi, int k, const uint64_t *d_hist, uint64_t scan_lo, uint64_t scan_hi,
                 DeviceArena &arena, cudaStream_t st, SortStats *stats, int *out_lo_buf, int *out_hi_buf);
 
 }  // namespace mp

@@ -1,4 +1,5 @@
 // C ABI of libmetapart_gpu.so (include/metapart_gpu.h): contexts, jobs and the stage drivers.
+#include <algorithm>
 #include <atomic>
 #include <cstdarg>
 #include <cstdio>
@@ -185,6 +186,27 @@ __global__ void k_sizes_raw(const uint32_t *parent, uint64_t n, uint32_t *size)
     atomicAdd(&size[(p == BAD || p == x) ? (uint32_t)x : p], 1u);
 }
 
+// The reference's threshold walk over the prefix histogram (metapart.c:3728-3791):
+//   for (i = 0; i < NB; i++) if (hist[i] >= step * cr) { record(cr, i); cr++; }
+// hist is non-decreasing, so the cr-th hit is the later of the first bucket whose prefix reaches
+// step * cr and the bucket after the previous hit: one binary search per hit instead of a pass over
+// all buckets.  Hits after the maxc-th are not walked (the caller only tests the final counter
+// against the last index).  Returns the final counter.
+template <class F> static uint64_t threshold_walk(const uint64_t *hist, uint64_t step, uint64_t maxc, F record)
+{
+    uint64_t cr = 1;
+    int64_t prev = -1;
+    while (cr <= maxc) {
+        const uint64_t lb = (uint64_t)(std::lower_bound(hist, hist + NB, step * cr) - hist);
+        const uint64_t i = std::max<uint64_t>(lb, (uint64_t)(prev + 1));
+        if (i >= NB) break;
+        record(cr, i);
+        prev = (int64_t)i;
+        cr++;
+    }
+    return cr;
+}
+
 // The reference's scan / thread k-mer range planner at one rank (metapart.c:3720-3791).
 int plan_ranges(const uint64_t *hist, int S, int T, std::vector<uint64_t> &scanR, std::vector<uint64_t> &thrR)
 {
@@ -193,47 +215,37 @@ int plan_ranges(const uint64_t *hist, int S, int T, std::vector<uint64_t> &scanR
     scanR.assign(S + 1, 0);
     thrR.assign((size_t)S * T + 1, 0);
     const uint64_t avg = total / (uint64_t)S + (total % (uint64_t)S ? 1 : 0);
-    uint64_t cr = 1, i;
-    for (i = 0; i < NB; i++)
-        if (hist[i] >= avg * cr) {
-            if (cr <= (uint64_t)S) scanR[cr] = i;
-            cr++;
-        }
-    if (cr == (uint64_t)S) scanR[cr] = i;
+    uint64_t cr = threshold_walk(hist, avg, (uint64_t)S, [&](uint64_t c, uint64_t i) { scanR[c] = i; });
+    if (cr == (uint64_t)S) scanR[cr] = NB;
     const uint64_t avgT = avg / (uint64_t)T;
-    cr = 1;
-    for (i = 0; i < NB; i++)
-        if (hist[i] >= cr * avgT) {
-            if (cr <= (uint64_t)S * T) thrR[cr] = (cr % (uint64_t)T == 0) ? scanR[cr / T] : i;
-            cr++;
-        }
-    if (cr == (uint64_t)S * T) thrR[cr] = i;
+    cr = threshold_walk(hist, avgT, (uint64_t)S * T, [&](uint64_t c, uint64_t i) {
+        thrR[c] = (c % (uint64_t)T == 0) ? scanR[c / T] : i;
+    });
+    if (cr == (uint64_t)S * T) thrR[cr] = NB;
     return 0;
 }
 
 // Tuple-index bounds of the thread ranges of one scan: the range partition bins a bucket
 // to the last range whose start is not above it (metapart.c:2019-2022); the reference
 // sizes its bins from [start_t, start_t+1) (metapart.c:1810-1850), so the two must agree.
+// A bucket's bin is the largest t with max(ltr[0..t]) <= bucket, so bin t holds the buckets
+// [M_t, M_t+1) with M_t the running maximum: each bin's count is one difference of the prefix.
 int range_bounds(const uint64_t *hist, const uint64_t *ltr, int T, uint64_t scan_lo, uint64_t scan_hi,
                  std::vector<uint64_t> &bounds)
 {
-    std::vector<uint64_t> cnt(T, 0);
-    // cb + 1 is the first range start above b; it only moves forward as b grows
-    int cb = 0;
-    for (uint64_t b = scan_lo; b < scan_hi; b++) {
-        const uint64_t c = hist[b + 1] - hist[b];
-        if (!c) continue;
-        while (cb <= T && b >= ltr[cb]) cb++;
-        cb--;
-        if (cb < 0 || cb >= T) return set_error(MP_EUNSUP, "thread k-mer ranges do not cover bucket %llu", (unsigned long long)b);
-        cnt[cb] += c;
-        cb++;
-    }
+    if (scan_hi < scan_lo) scan_hi = scan_lo;  // an empty scan (the planner leaves trailing bounds at 0)
+    auto clip = [&](uint64_t x) { return x < scan_lo ? scan_lo : (x > scan_hi ? scan_hi : x); };
+    std::vector<uint64_t> M(T + 1);
+    M[0] = ltr[0];
+    for (int t = 1; t <= T; t++) M[t] = std::max(M[t - 1], ltr[t]);
+    if (hist[clip(M[0])] != hist[scan_lo] || hist[scan_hi] != hist[clip(M[T])])
+        return set_error(MP_EUNSUP, "thread k-mer ranges do not cover the scan's populated buckets");
     bounds.assign(T + 1, 0);
     for (int t = 0; t < T; t++) {
+        const uint64_t c = hist[clip(M[t + 1])] - hist[clip(M[t])];
         const uint64_t ref = ltr[t + 1] > ltr[t] ? hist[ltr[t + 1]] - hist[ltr[t]] : 0;
-        if (ref != cnt[t]) return set_error(MP_EUNSUP, "thread k-mer ranges are not monotone over populated buckets");
-        bounds[t + 1] = bounds[t] + cnt[t];
+        if (ref != c) return set_error(MP_EUNSUP, "thread k-mer ranges are not monotone over populated buckets");
+        bounds[t + 1] = bounds[t] + c;
     }
     return 0;
 }
@@ -532,6 +544,10 @@ int mp_job_partition(mp_job *j, const mp_part_params *p, const uint64_t *chunk_s
     const bool has_hi = 2 * k + 8 > 64;
     char name[64], name2[64];
     // tuples per read of every scan in one pass (plain variant, monotone scan bounds)
+    // the histogram prefix on the device, for the sort's planning kernels
+    uint64_t *d_hist = j->arena.alloc_persistent<uint64_t>(NB + 1);
+    if (!d_hist) return set_error(MP_ENOMEM, "device memory for the histogram");
+    MP_CUDA(cudaMemcpyAsync(d_hist, hist, (NB + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, j->st));
     uint32_t *cnt_all = nullptr, *d_b = nullptr;
     // the count pass's k-mer cache serves this partition when it holds the same k (plain variant)
     const bool use_kc = j->kc_lo && j->kc_k == k && !p->min3 && S <= 8;
@@ -607,7 +623,7 @@ int mp_job_partition(mp_job *j, const mp_part_params *p, const uint64_t *chunk_s
         {
             StageTimer tm(j->st, &j->stage_ms[3]);
             SortStats ss;
-            if ((rc = bucket_sort(sb, n, has_hi, k, hist, lo, hi, j->arena, j->st, &ss, &lo_buf, &hi_buf))) return rc;
+            if ((rc = bucket_sort(sb, n, has_hi, k, d_hist, lo, hi, j->arena, j->st, &ss, &lo_buf, &hi_buf))) return rc;
             j->sort_stats = ss;
             j->sort_passes_total += ss.passes;
             j->sort_ms_total += ss.pass_ms;
@@ -653,6 +669,7 @@ int mp_job_partition(mp_job *j, const mp_part_params *p, const uint64_t *chunk_s
     }
     j->arena.free_persistent(cnt_all);
     j->arena.free_persistent(d_b);
+    j->arena.free_persistent(d_hist);
     drop_kmer_cache(j);  // its HBM goes back before the mate union and the output
     {
         StageTimer tm(j->st, &j->stage_ms[6]);
