@@ -411,12 +411,18 @@ __global__ void k_compress(uint32_t *parent, uint64_t n)
 }
 
 // compSizes after a reset to 1 and printStats (metapart.c:4010-4030): 1 + non-root members.
+// Component sizes (1 + members below each root).  The reads of a large component meet in most warps,
+// so the lanes of one root add together: one atomic per root and warp instead of one per read.
 __global__ void k_sizes(const uint32_t *parent, uint64_t n, uint32_t *size)
 {
     const uint64_t x = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (x >= n) return;
-    const uint32_t p = parent[x];
-    atomicAdd(&size[(p == BAD || p == x) ? (uint32_t)x : p], 1u);
+    uint32_t r = 0xFFFFFFFFu;
+    if (x < n) {
+        const uint32_t p = parent[x];
+        r = (p == BAD || p == x) ? (uint32_t)x : p;
+    }
+    const uint32_t peers = __match_any_sync(FULLW, r);
+    if (x < n && (threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&size[r], (uint32_t)__popc(peers));
 }
 
 // -------------------------------------------------------------- K6 mate union
