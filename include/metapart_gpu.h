@@ -210,8 +210,11 @@ int mp_job_sort_stats(const mp_job *job, uint64_t *tuples, int *passes, double *
 
 /* Where the last partition's sort time went, summed over its scans: the m-mer bucket digit passes, the
  * shared-memory sort of bucket units, and the buckets too large for a unit (ms, and their counts);
- * unit_counters (nullable, 4 entries): the unit sort's digit passes and its SM cycles in the load,
- * digit-pass and store phases, each summed over units.  Tracing only; no counterpart in the reference. */
+ * unit_counters (nullable, 11 entries): [0] the unit sort's digit passes, [1..3] its SM cycles in the load,
+ * digit-pass and store phases, each summed over units; [4..8] the bucket digit passes' SM cycles in the
+ * tile-id fetch, loads and ranks, digit scan, tile order and look-back, and stores, each summed over
+ * tiles; [9] [10] the status words digit 0's look-back read and its polls of words not yet posted.
+ * Tracing only; no counterpart in the reference. */
 int mp_job_sort_split(const mp_job *job, double *pass_ms, double *unit_ms, double *big_ms, uint64_t *units,
                       uint64_t *big_buckets, uint64_t *big_tuples, uint64_t *unit_counters);
 

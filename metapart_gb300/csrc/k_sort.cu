@@ -11,6 +11,7 @@
 // counts, looks back over earlier tiles for its global offsets, reorders the tile in
 // shared memory and writes each digit's run contiguously.
 #include <algorithm>
+#include <cstddef>
 #include <cstdlib>
 #include <cstdio>
 #include <mutex>
@@ -20,12 +21,13 @@
 
 namespace mp {
 
-constexpr int ST = 256;  // threads per tile (two resident tiles per SM)
+constexpr int ST = 256;  // threads per tile (three resident tiles per SM)
 constexpr int SI = 16;
 constexpr int STILE = ST * SI;
 constexpr int SW = ST / 32;
 constexpr unsigned FULLM = 0xFFFFFFFFu;
 constexpr uint32_t SPIN_CAP = 1u << 22;
+constexpr int LB = 4;  // look-back: predecessor status words read per round
 
 struct SortSmem {
     uint64_t keys[STILE];
@@ -84,6 +86,7 @@ __global__ void __launch_bounds__(256) k_hist_upfront(const uint64_t *__restrict
 // Opt-in shared memory sizes of the sort kernels, set once per device (thread-safe).
 static void sort_kernel_attrs();
 static int sm_count();
+static uint32_t onesweep_prefetch_tiles();
 
 template <int SRC>
 __device__ __forceinline__ uint32_t digit_of(uint64_t lo, uint32_t hi, int shift)
@@ -99,14 +102,17 @@ __global__ void __launch_bounds__(ST, 3) k_onesweep(const uint64_t *__restrict__
                                                     uint8_t *__restrict__ out_hi, uint32_t *__restrict__ out_id, uint64_t n,
                                                     int shift, const uint64_t *__restrict__ dbase,
                                                     unsigned long long *status, uint32_t *tile_ctr, uint32_t epoch,
-                                                    uint32_t *err, uint32_t pf_tiles)
+                                                    uint32_t *err, uint32_t pf_tiles, unsigned long long *trace)
 {
     extern __shared__ __align__(16) unsigned char smraw[];
     SortSmem &sm = *reinterpret_cast<SortSmem *>(smraw);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    long long ts[5];  // thread 0's clock at the phase boundaries (trace only)
+    ts[0] = clock64();
     for (int i = threadIdx.x; i < SW * 256; i += ST) (&sm.whist[0][0])[i] = 0;
     if (threadIdx.x == 0) sm.tile_id = atomicAdd(tile_ctr, 1u);
     __syncthreads();
+    ts[1] = clock64();
     const uint64_t tile = sm.tile_id;
     const uint64_t base = tile * STILE;
     const bool has_hi = in_hi != nullptr;
@@ -130,13 +136,15 @@ __global__ void __launch_bounds__(ST, 3) k_onesweep(const uint64_t *__restrict__
         const uint64_t idx = base + (uint64_t)warp * (32 * SI) + (uint64_t)j * 32 + lane;
         const bool v = idx < n;
         key[j] = v ? in_lo[idx] : 0ull;
-        val[j] = v ? in_id[idx] : 0u;
         const uint32_t h = (has_hi && v) ? (uint32_t)in_hi[idx] : 0u;
         hv[j >> 2] |= h << (8 * (j & 3));
         rd[j] = (v ? digit_of<SRC>(key[j], h, shift) : 256u) << 16;
     }
-    // warp-level multi-split: stable rank of each tuple among equal digits of its warp; the lanes holding a
-    // digit come from its eight bit-plane ballots
+    // warp-level multi-split: stable rank of each tuple among equal digits of its warp.  First every
+    // tuple's peers (the lanes holding its digit, from eight bit-plane ballots), packed into rd as the
+    // peers below its lane (bits 0-4), their number (5-10) and whether it leads them (11); no memory
+    // is touched, so the ballots of all tuples issue back to back.  Then one read-modify-write of the
+    // warp's running digit count per tuple.
     const uint32_t lt = (1u << lane) - 1;
 #pragma unroll
     for (int j = 0; j < SI; j++) {
@@ -147,16 +155,28 @@ __global__ void __launch_bounds__(ST, 3) k_onesweep(const uint64_t *__restrict__
             const uint32_t bb = __ballot_sync(FULLM, (d >> b) & 1u);
             peers &= ((d >> b) & 1u) ? bb : ~bb;
         }
+        rd[j] |= (uint32_t)__popc(peers & lt) | ((uint32_t)__popc(peers) << 5) | ((peers & lt) == 0 ? 1u << 11 : 0u);
+    }
+#pragma unroll
+    for (int j = 0; j < SI; j++) {
+        const uint32_t d = rd[j] >> 16;
         uint32_t pre = 0;
         if (d < 256) pre = sm.whist[warp][d];
         __syncwarp();
         if (d < 256) {
-            rd[j] |= pre + __popc(peers & lt);
-            if ((peers & lt) == 0) sm.whist[warp][d] = pre + __popc(peers);
+            if ((rd[j] >> 11) & 1u) sm.whist[warp][d] = pre + ((rd[j] >> 5) & 63u);
+            rd[j] = (d << 16) | (pre + (rd[j] & 31u));
         }
         __syncwarp();
     }
+    // the ids are needed only for the tile order below: loaded now, they arrive during the digit scan
+#pragma unroll
+    for (int j = 0; j < SI; j++) {
+        const uint64_t idx = base + (uint64_t)warp * (32 * SI) + (uint64_t)j * 32 + lane;
+        val[j] = idx < n ? in_id[idx] : 0u;
+    }
     __syncthreads();
+    ts[2] = clock64();
     // threads 0..255 own one digit each: warp prefixes, the tile count, its look-back
     const uint32_t d = threadIdx.x;
     const bool dig = d < 256;
@@ -187,6 +207,7 @@ __global__ void __launch_bounds__(ST, 3) k_onesweep(const uint64_t *__restrict__
     }
     if (threadIdx.x == 0) sm.nvalid = (uint32_t)min((uint64_t)STILE, n - base);
     __syncthreads();
+    ts[3] = clock64();
     // tile order in shared memory first: the look-back below then finds more predecessors done
 #pragma unroll
     for (int j = 0; j < SI; j++) {
@@ -198,31 +219,53 @@ __global__ void __launch_bounds__(ST, 3) k_onesweep(const uint64_t *__restrict__
             if (has_hi) sm.his[s] = (uint8_t)(hv[j >> 2] >> (8 * (j & 3)));
         }
     }
+    uint32_t lb_steps = 0, lb_waits = 0;  // thread 0's look-back: status words summed, polls that found none posted
     if (dig) {
         // decoupled look-back for digit d
         const unsigned long long E = (unsigned long long)epoch << 60, PF = 1ull << 59, CM = PF - 1;
         unsigned long long excl = 0;
         if (tile > 0) {
+            // LB predecessors' words are read at once, then summed in order up to the first prefix;
+            // a word not yet posted ends the round and the next round starts from it
             int64_t p = (int64_t)tile - 1;
             uint32_t spins = 0;
-            while (p >= 0) {
-                const unsigned long long v = ld_relaxed(status + (uint64_t)p * 256 + d);
-                if ((v >> 60) != epoch) {
+            bool found = false;
+            while (!found) {
+                unsigned long long v[LB];
+#pragma unroll
+                for (int q = 0; q < LB; q++) {
+                    const int64_t pq = p - q;
+                    v[q] = pq >= 0 ? ld_relaxed(status + (uint64_t)pq * 256 + d) : (E | PF);  // before tile 0: prefix 0
+                }
+                int adv = 0;
+                bool stall = false;
+#pragma unroll
+                for (int q = 0; q < LB; q++) {
+                    if (found || stall) continue;
+                    if ((v[q] >> 60) != epoch) {
+                        stall = true;
+                        continue;
+                    }
+                    excl += v[q] & CM;
+                    adv++;
+                    found = (v[q] & PF) != 0;
+                }
+                p -= adv;
+                lb_steps += (uint32_t)adv;
+                if (stall && !found) {
+                    lb_waits++;
                     if (++spins > SPIN_CAP) {
                         atomicOr(err, DERR_SPIN);
                         break;
                     }
-                    continue;
                 }
-                excl += v & CM;
-                if (v & PF) break;
-                p--;
             }
             st_relaxed(status + tile * 256 + d, E | PF | (excl + cnt));
         }
         sm.gbase[d] = dbase[d] + excl;
     }
     __syncthreads();
+    ts[4] = clock64();
     const uint32_t nv = sm.nvalid;
     for (uint32_t s = threadIdx.x; s < nv; s += ST) {
         const uint64_t kk = sm.keys[s];
@@ -232,6 +275,15 @@ __global__ void __launch_bounds__(ST, 3) k_onesweep(const uint64_t *__restrict__
         out_lo[g] = kk;
         out_id[g] = sm.vals[s];
         if (has_hi) out_hi[g] = sm.his[s];
+    }
+    // [0] tile id, [1] loads and ranks, [2] digit scan, [3] tile order and look-back, [4] stores (cycles);
+    // [5] [6] look-back status words read and polls of unposted words (digit 0)
+    if (trace && threadIdx.x == 0) {
+        const long long te = clock64();
+        for (int q = 0; q < 4; q++) atomicAdd(&trace[q], (unsigned long long)(ts[q + 1] - ts[q]));
+        atomicAdd(&trace[4], (unsigned long long)(te - ts[4]));
+        atomicAdd(&trace[5], (unsigned long long)lb_steps);
+        atomicAdd(&trace[6], (unsigned long long)lb_waits);
     }
 }
 
@@ -281,7 +333,7 @@ int radix_sort(SortBufs &b, uint64_t n, bool has_hi, DeviceArena &arena, cudaStr
     }
     MP_CUDA(cudaMemcpyAsync(dbase, base.data(), base.size() * sizeof(uint64_t), cudaMemcpyHostToDevice, st));
     sort_kernel_attrs();
-    const uint32_t pf = 2u * (uint32_t)sm_count();  // resident tiles: the prefetch distance
+    const uint32_t pf = onesweep_prefetch_tiles();
     std::vector<cudaEvent_t> ev(passes.size() + 1);
     for (auto &e : ev) cudaEventCreate(&e);
     cudaEventRecord(ev[0], st);
@@ -293,11 +345,11 @@ int radix_sort(SortBufs &b, uint64_t n, bool has_hi, DeviceArena &arena, cudaStr
         if (dgt < 8)
             (mp::count_launch(), k_onesweep<0><<<(unsigned)tiles, ST, sizeof(SortSmem), st>>>(b.lo[src], ih, b.id[src], b.lo[dst], oh,
                                                                          b.id[dst], n, 8 * dgt, dbase + dgt * 256, status,
-                                                                         ctr + pi, (uint32_t)(pi + 1), err, pf));
+                                                                         ctr + pi, (uint32_t)(pi + 1), err, pf, nullptr));
         else
             (mp::count_launch(), k_onesweep<1><<<(unsigned)tiles, ST, sizeof(SortSmem), st>>>(b.lo[src], ih, b.id[src], b.lo[dst], oh,
                                                                          b.id[dst], n, 0, dbase + dgt * 256, status,
-                                                                         ctr + pi, (uint32_t)(pi + 1), err, pf));
+                                                                         ctr + pi, (uint32_t)(pi + 1), err, pf, nullptr));
         cudaEventRecord(ev[pi + 1], st);
         b.cur = dst;
     }
@@ -349,25 +401,21 @@ constexpr int SS_BINS = 1 << SS_MAXBITS;
 struct SegSmem {
     uint64_t key[SS_CAP];                // 96 KB
     uint16_t perm[2][SS_CAP];            // 48 KB
-    uint16_t whist[SS_WARPS][SS_BINS];   // 64 KB: digit counts per warp, then each (warp, digit)'s first position
+    uint16_t whist[SS_WARPS][SS_BINS];   // 64 KB: digit counts per warp, then each (warp, digit)'s offset in the digit
+    uint16_t dstart[SS_BINS];            // first position of each digit
     uint32_t wsum[SS_WARPS];
     unsigned long long kor, kand;
 };
+static_assert(offsetof(SegSmem, whist) % 16 == 0, "histogram rows are cleared with 16-byte stores");
 
 // One stable counting-sort pass over a unit: perm[cur] (or the identity) -> perm[cur ^ 1] by the
 // digit (key >> sh) & mask, nbins = a power of two >= 32 covering the mask.  Items are ranked in
-// warp-blocked order with match_any, so equal digits keep their order.
+// warp-blocked order with match_any, so equal digits keep their order.  Every warp's histogram row
+// is zero on entry and on exit: a warp clears its own row once its scatter has read it.
 __device__ void seg_pass(SegSmem &sm, int cur, uint32_t cnt, int sh, uint32_t mask, uint32_t nbins, bool identity)
 {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t lt = (1u << lane) - 1;
-    {
-        uint32_t *w32 = reinterpret_cast<uint32_t *>(&sm.whist[0][0]);
-        const uint32_t words = nbins / 2;  // per warp row
-        for (uint32_t i = threadIdx.x; i < SS_WARPS * words; i += SS_THREADS)
-            w32[(i / words) * (SS_BINS / 2) + (i % words)] = 0;
-    }
-    __syncthreads();
     uint32_t src[SS_ITEMS], rd[SS_ITEMS];  // rd: rank (bits 0-15) | digit (bits 16-27; nbins = none)
 #pragma unroll
     for (int j = 0; j < SS_ITEMS; j++) {
@@ -390,7 +438,7 @@ __device__ void seg_pass(SegSmem &sm, int cur, uint32_t cnt, int sh, uint32_t ma
         __syncwarp();
     }
     __syncthreads();
-    // thread d: exclusive prefix of digit d over the warps, then over the digits
+    // thread d: exclusive prefix of digit d over the warps (into the rows), then the digit's start
     uint32_t colsum = 0, x = 0;
     const uint32_t d = threadIdx.x;
     if (d < nbins) {  // nbins is a multiple of 32: whole warps take part in the shuffles
@@ -417,14 +465,19 @@ __device__ void seg_pass(SegSmem &sm, int cur, uint32_t cnt, int sh, uint32_t ma
     if (d < nbins) {
         uint32_t before = x - colsum;
         for (int w = 0; w < warp; w++) before += sm.wsum[w];
-#pragma unroll
-        for (int w = 0; w < SS_WARPS; w++) sm.whist[w][d] = (uint16_t)(sm.whist[w][d] + before);
+        sm.dstart[d] = (uint16_t)before;
     }
     __syncthreads();
 #pragma unroll
     for (int j = 0; j < SS_ITEMS; j++) {
         const uint32_t dd = rd[j] >> 16;
-        if (dd < nbins) sm.perm[cur ^ 1][sm.whist[warp][dd] + (rd[j] & 0xFFFF)] = (uint16_t)src[j];
+        if (dd < nbins)
+            sm.perm[cur ^ 1][(uint32_t)sm.dstart[dd] + sm.whist[warp][dd] + (rd[j] & 0xFFFF)] = (uint16_t)src[j];
+    }
+    __syncwarp();
+    {
+        uint4 *row = reinterpret_cast<uint4 *>(&sm.whist[warp][0]);
+        for (uint32_t i = lane; i < nbins / 8; i += 32) row[i] = make_uint4(0, 0, 0, 0);
     }
     __syncthreads();
 }
@@ -445,6 +498,10 @@ __global__ void __launch_bounds__(SS_THREADS) k_segsort(const uint64_t *__restri
     const int lane = threadIdx.x & 31;
     const uint64_t lowmask = (1ull << lowbits) - 1;
     unsigned long long cyc[3] = {0, 0, 0}, npass = 0;
+    {
+        uint4 *w4 = reinterpret_cast<uint4 *>(&sm.whist[0][0]);
+        for (uint32_t i = threadIdx.x; i < sizeof sm.whist / 16; i += SS_THREADS) w4[i] = make_uint4(0, 0, 0, 0);
+    }
     for (uint32_t u = blockIdx.x; u < nunits; u += gridDim.x) {
         const long long t0 = clock64();
         const uint64_t start = ustart[u];
@@ -699,6 +756,17 @@ static int sm_count()
     return n > 0 ? n : 1;
 }
 
+// How far ahead (in tiles) a digit-pass tile prefetches its successor into L2: a number of SM
+// waves (MP_ONESWEEP_PF_WAVES, 0 = no prefetch) times the SM count.  Three tiles are resident per
+// SM, so a distance of at least three waves lands on tiles that have not started yet.
+static uint32_t onesweep_prefetch_tiles()
+{
+    const char *e = getenv("MP_ONESWEEP_PF_WAVES");
+    int w = e && *e ? atoi(e) : 2;
+    w = w < 0 ? 0 : (w > 16 ? 16 : w);
+    return (uint32_t)w * (uint32_t)sm_count();
+}
+
 static void sort_kernel_attrs()
 {
     static std::once_flag once[64];
@@ -750,15 +818,15 @@ int bucket_sort(SortBufs &b, uint64_t n, bool has_hi, int k, const uint64_t *d_h
         if (!hk[d]) passes.push_back(d);
     const uint64_t tiles = (n + STILE - 1) / STILE;
     uint32_t *ctr = arena.alloc<uint32_t>(8), *err = arena.alloc<uint32_t>(1);
-    unsigned long long *trace = arena.alloc<unsigned long long>(8);
+    unsigned long long *trace = arena.alloc<unsigned long long>(16);  // [0..3] unit sort, [8..12] digit passes
     unsigned long long *status = passes.empty() ? nullptr : arena.alloc<unsigned long long>(tiles * 256);
     if (!ctr || !err || !trace || (!passes.empty() && !status)) return set_error(MP_ENOMEM, "device memory for the bucket sort");
-    MP_CUDA(cudaMemsetAsync(trace, 0, 8 * sizeof(unsigned long long), st));
+    MP_CUDA(cudaMemsetAsync(trace, 0, 16 * sizeof(unsigned long long), st));
     MP_CUDA(cudaMemsetAsync(ctr, 0, 8 * sizeof(uint32_t), st));
     MP_CUDA(cudaMemsetAsync(err, 0, sizeof(uint32_t), st));
     if (status) MP_CUDA(cudaMemsetAsync(status, 0, tiles * 256 * sizeof(unsigned long long), st));
     sort_kernel_attrs();
-    const uint32_t pf = 2u * (uint32_t)sm_count();  // resident tiles: the prefetch distance
+    const uint32_t pf = onesweep_prefetch_tiles();
     cudaEvent_t ev[5];
     for (auto &e : ev) cudaEventCreate(&e);
     cudaEventRecord(ev[0], st);
@@ -767,7 +835,7 @@ int bucket_sort(SortBufs &b, uint64_t n, bool has_hi, int k, const uint64_t *d_h
         const int src = b.cur, dst = b.cur ^ 1;
         (mp::count_launch(), k_onesweep<2><<<(unsigned)tiles, ST, sizeof(SortSmem), st>>>(
             b.lo[src], has_hi ? b.hi[src] : nullptr, b.id[src], b.lo[dst], has_hi ? b.hi[dst] : nullptr, b.id[dst], n,
-            bsh + 8 * d, dbase + d * 256, status, ctr + pi, (uint32_t)(pi + 1), err, pf));
+            bsh + 8 * d, dbase + d * 256, status, ctr + pi, (uint32_t)(pi + 1), err, pf, trace + 8));
         b.cur = dst;
     }
     cudaEventRecord(ev[1], st);
@@ -849,7 +917,7 @@ int bucket_sort(SortBufs &b, uint64_t n, bool has_hi, int k, const uint64_t *d_h
         }
     }
     cudaEventRecord(ev[3], st);
-    unsigned long long ht[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    unsigned long long ht[16] = {};
     MP_CUDA(cudaMemcpyAsync(ht, trace, sizeof ht, cudaMemcpyDeviceToHost, st));
     uint32_t herr = 0;
     MP_CUDA(cudaMemcpyAsync(&herr, err, sizeof herr, cudaMemcpyDeviceToHost, st));
@@ -871,6 +939,7 @@ int bucket_sort(SortBufs &b, uint64_t n, bool has_hi, int k, const uint64_t *d_h
         stats->big_tuples = nbig;
         stats->unit_passes = ht[0];
         for (int q = 0; q < 3; q++) stats->phase_cycles[q] = ht[1 + q];
+        for (int q = 0; q < 7; q++) stats->pass_cycles[q] = ht[8 + q];
     }
     for (auto &e : ev) cudaEventDestroy(e);
     arena.free_scratch(status);
@@ -988,11 +1057,11 @@ int sort_tuples_noalloc(const uint64_t *lo_in, const uint8_t *hi_in, const uint3
         if (dgt < 8)
             (mp::count_launch(), k_onesweep<0><<<(unsigned)tiles, ST, sizeof(SortSmem), st>>>(
                 src_lo, src_hi, src_id, d_lo, d_hi, d_id, n, 8 * dgt, S->dbase + dgt * 256, S->status, S->ctr + i,
-                (uint32_t)(i + 1), &S->err, 0u));
+                (uint32_t)(i + 1), &S->err, 0u, nullptr));
         else
             (mp::count_launch(), k_onesweep<1><<<(unsigned)tiles, ST, sizeof(SortSmem), st>>>(
                 src_lo, src_hi, src_id, d_lo, d_hi, d_id, n, 0, S->dbase + dgt * 256, S->status, S->ctr + i,
-                (uint32_t)(i + 1), &S->err, 0u));
+                (uint32_t)(i + 1), &S->err, 0u, nullptr));
         src_lo = d_lo;
         src_hi = d_hi;
         src_id = d_id;

@@ -23,6 +23,9 @@ struct SortStats {
     uint64_t units = 0, big_buckets = 0, big_tuples = 0;
     uint64_t unit_passes = 0;                 // unit sort: digit passes, summed over units
     uint64_t phase_cycles[3] = {0, 0, 0};     // unit sort: SM cycles summed over units in load, passes, store
+    uint64_t pass_cycles[7] = {};  // bucket digit passes: SM cycles summed over tiles in the tile-id fetch, loads +
+                                   //   ranks, digit scan, tile order + look-back, stores; then digit 0's look-back
+                                   //   status words read and polls of unposted words, summed over tiles
 };
 
 // Stable sort of b[cur][0, n) by (hi, lo); on return b.cur names the sorted buffer.

@@ -84,7 +84,7 @@ struct mp_job {
     uint64_t sort_bytes_total = 0, sort_tuples_total = 0;
     double seg_ms_total = 0, big_ms_total = 0;
     uint64_t units_total = 0, big_buckets_total = 0, big_tuples_total = 0;
-    uint64_t unit_passes_total = 0, phase_total[3] = {0, 0, 0};
+    uint64_t unit_passes_total = 0, phase_total[3] = {0, 0, 0}, pass_cycles_total[7] = {};
     int pe_rounds = 0;
 };
 
@@ -528,6 +528,7 @@ int mp_job_partition(mp_job *j, const mp_part_params *p, const uint64_t *chunk_s
     j->units_total = j->big_buckets_total = j->big_tuples_total = 0;
     j->unit_passes_total = 0;
     for (auto &v : j->phase_total) v = 0;
+    for (auto &v : j->pass_cycles_total) v = 0;
     if (j->d_parent) { j->arena.free_persistent(j->d_parent); j->d_parent = nullptr; }
     if (j->d_size) { j->arena.free_persistent(j->d_size); j->d_size = nullptr; }
     if (j->d_filtered) { j->arena.free_persistent(j->d_filtered); j->d_filtered = nullptr; }
@@ -636,6 +637,7 @@ int mp_job_partition(mp_job *j, const mp_part_params *p, const uint64_t *chunk_s
             j->big_tuples_total += ss.big_tuples;
             j->unit_passes_total += ss.unit_passes;
             for (int q = 0; q < 3; q++) j->phase_total[q] += ss.phase_cycles[q];
+            for (int q = 0; q < 7; q++) j->pass_cycles_total[q] += ss.pass_cycles[q];
         }
         Tuples tp;
         tp.lo = sb.lo[lo_buf];
@@ -761,6 +763,7 @@ int mp_job_sort_split(const mp_job *j, double *pass_ms, double *unit_ms, double 
     if (unit_counters) {
         unit_counters[0] = j->unit_passes_total;
         for (int q = 0; q < 3; q++) unit_counters[1 + q] = j->phase_total[q];
+        for (int q = 0; q < 7; q++) unit_counters[4 + q] = j->pass_cycles_total[q];
     }
     if (pass_ms) *pass_ms = j->sort_ms_total;
     if (unit_ms) *unit_ms = j->seg_ms_total;

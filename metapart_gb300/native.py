@@ -243,12 +243,14 @@ class Job:
     def sort_split(self) -> dict:
         a, u, g = C.c_double(), C.c_double(), C.c_double()
         nu, nb, nt = C.c_uint64(), C.c_uint64(), C.c_uint64()
-        uc = (C.c_uint64 * 4)()
+        uc = (C.c_uint64 * 11)()
         _check(lib().mp_job_sort_split(self.h, C.byref(a), C.byref(u), C.byref(g), C.byref(nu), C.byref(nb),
                                        C.byref(nt), uc), "sort_split")
         return {"digit_pass_ms": a.value, "unit_sort_ms": u.value, "big_bucket_ms": g.value, "units": nu.value,
                 "big_buckets": nb.value, "big_tuples": nt.value, "unit_passes": uc[0],
-                "unit_cycles": {"load": uc[1], "passes": uc[2], "store": uc[3]}}
+                "unit_cycles": {"load": uc[1], "passes": uc[2], "store": uc[3]},
+                "pass_cycles": {"tile_id": uc[4], "load_rank": uc[5], "scan": uc[6], "order_lookback": uc[7],
+                                "store": uc[8], "lookback_words": uc[9], "lookback_waits": uc[10]}}
 
 
 def fastq_index_ptr(num_chunks: int, host_ptr: int, nbytes: int, interleaved: bool = False):
