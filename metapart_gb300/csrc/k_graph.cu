@@ -64,18 +64,19 @@ __device__ __forceinline__ uint32_t judge_run(const uint32_t *before, const uint
 {
     int nin = 0, nout = 0, mxi = 0, mxo = 0;
     uint32_t cmi = 0, cmo = 0, smi = 0, smo = 0;
+    // the first code with the largest count is the max; a count equal to it is the second max
 #pragma unroll
     for (int q = 0; q < 7; q++) {
-        if (before[q]) {
-            if (before[q] > cmi) { smi = cmi; cmi = before[q]; mxi = q; }
-            else if (before[q] > smi) smi = before[q];
-            nin++;
-        }
-        if (after[q]) {
-            if (after[q] > cmo) { smo = cmo; cmo = after[q]; mxo = q; }
-            else if (after[q] > smo) smo = after[q];
-            nout++;
-        }
+        const uint32_t b = before[q], a = after[q];
+        const bool gb = b > cmi, ga = a > cmo;
+        nin += b != 0;
+        nout += a != 0;
+        smi = gb ? cmi : max(smi, b);
+        smo = ga ? cmo : max(smo, a);
+        mxi = gb ? q : mxi;
+        mxo = ga ? q : mxo;
+        cmi = max(cmi, b);
+        cmo = max(cmo, a);
     }
     if (nin <= 1 && nout <= 1) return 0;
     uint32_t J = J_ANY | (nin > 1 ? J_NIN : 0) | (nout > 1 ? J_NOUT : 0) | ((uint32_t)mxi << 3) | ((uint32_t)mxo << 6);
@@ -177,11 +178,12 @@ __global__ void __launch_bounds__(256) k_filter_warp(const uint64_t *lo, const u
             continue;
         }
         if (open && ohom) {  // counts of the uniform part carried in
-            const uint32_t len = (uint32_t)(p - rs);
+            const uint32_t len = (uint32_t)(p - rs), rb = run_adj & 7, ra = (run_adj >> 3) & 7;
 #pragma unroll
-            for (int c = 0; c < 7; c++) cb[c] = ca[c] = 0;
-            if ((run_adj & 7) < 7) cb[run_adj & 7] = len;
-            if (((run_adj >> 3) & 7) < 7) ca[(run_adj >> 3) & 7] = len;
+            for (int c = 0; c < 7; c++) {  // code 7 counts nowhere; no dynamic index, so the counts stay in registers
+                cb[c] = (uint32_t)c == rb ? len : 0u;
+                ca[c] = (uint32_t)c == ra ? len : 0u;
+            }
             deg = len;
             ohom = false;
         }
