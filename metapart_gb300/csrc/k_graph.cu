@@ -268,10 +268,46 @@ __device__ __forceinline__ uint32_t uf_find(uint32_t *parent, uint32_t x)
     return x;
 }
 
+// uf_find of x and of y advanced together (the same steps and path halving), so the parent loads of
+// the two walks are in flight at the same time.
+__device__ __forceinline__ void uf_find2(uint32_t *parent, uint32_t &x, uint32_t &y)
+{
+    bool dx = false, dy = false;
+    for (;;) {
+        const uint32_t px = dx ? x : parent[x];
+        const uint32_t py = dy ? y : parent[y];
+        dx = dx || px == x || px == BAD;
+        dy = dy || py == y || py == BAD;
+        if (dx && dy) return;
+        const uint32_t gx = dx ? x : parent[px];
+        const uint32_t gy = dy ? y : parent[py];
+        if (!dx) {
+            if (gx == px || gx == BAD) {
+                x = px;
+                dx = true;
+            } else {
+                parent[x] = gx;  // path halving: gx is an ancestor of x
+                x = gx;
+            }
+        }
+        if (!dy) {
+            if (gy == py || gy == BAD) {
+                y = py;
+                dy = true;
+            } else {
+                parent[y] = gy;
+                y = gy;
+            }
+        }
+        if (dx && dy) return;
+    }
+}
+
 __device__ __forceinline__ void uf_union(uint32_t *parent, uint32_t a, uint32_t b, uint32_t *err)
 {
     for (uint32_t it = 0; it < UF_CAP; it++) {
-        const uint32_t ra = uf_find(parent, a), rb = uf_find(parent, b);
+        uint32_t ra = a, rb = b;
+        uf_find2(parent, ra, rb);
         if (ra == rb) return;
         const uint32_t hi = ra > rb ? ra : rb, lo = ra > rb ? rb : ra;
         if (atomicCAS(&parent[lo], lo, hi) == lo) return;
@@ -324,19 +360,31 @@ __global__ void __launch_bounds__(256) k_edges_warp(EdgeCtx c)
     bool open = false, has_anchor = false;
     uint32_t anchor = 0;
     uint64_t prev_km = c0 ? kmer_of(c.lo, c.hi, c0 - 1) : 0;
+    // the next window's k-mer, read id and zero-mark word (windows start at multiples of 32), loaded one
+    // window ahead
+    uint64_t nkm = c0 + lane < c.n ? kmer_of(c.lo, c.hi, c0 + lane) : 0;
+    uint32_t nid = c0 + lane < c.n ? c.id[c0 + lane] : 0, nzw = c.z[c0 >> 5];
     for (uint64_t p = c0;; p += 32) {
         const bool owned = p < c1;
         if (!owned && !open) break;
         const uint64_t i = p + lane;
         const bool valid = i < c.n;
-        const uint64_t km = valid ? kmer_of(c.lo, c.hi, i) : 0;
+        const uint64_t km = valid ? nkm : 0;
+        const uint32_t rid = nid, zw = nzw;
+        if (p + 32 < c.n) {
+            if (i + 32 < c.n) {
+                nkm = kmer_of(c.lo, c.hi, i + 32);
+                nid = c.id[i + 32];
+            }
+            nzw = c.z[(p + 32) >> 5];
+        }
         uint64_t pk = __shfl_up_sync(FULLW, km, 1);
         if (lane == 0) pk = prev_km;
         const bool head = valid && (i == 0 || km != pk);
         const uint32_t H = __ballot_sync(FULLW, head);
         prev_km = __shfl_sync(FULLW, km, 31);
-        const bool nz = valid && km != 0 && !zbit(c.z, i);
-        const uint32_t r = nz ? c.id[i] : 0;
+        const bool nz = valid && km != 0 && !((zw >> lane) & 1u);
+        const uint32_t r = nz ? rid : 0;
         const bool good = nz && !c.filtered[r];  // the 1-byte flags keep the probe L2-friendly
         const uint32_t G = __ballot_sync(FULLW, good);
         const int fh = H ? __ffs(H) - 1 : 32;
