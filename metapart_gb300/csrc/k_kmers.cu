@@ -345,23 +345,24 @@ __global__ void __launch_bounds__(256) k_enum_count_scans(const uint8_t *fq, con
 }
 
 // K2a from the k-mer cache: tuples per read of every scan (S <= MAX_SCAN_COUNT), one warp per read.
+// A lane holds at most KC_PER_LANE (< 16) positions of a read, so its counts of the S scans pack into
+// 4-bit fields of one word; each scan's count is then one warp reduction.
+static_assert(4 * MAX_SCAN_COUNT <= 32 && KC_PER_LANE < 16, "per-lane scan counts are packed in 4-bit fields");
 __global__ void __launch_bounds__(256) k_kc_count_scans(const uint64_t *kc_off, const uint64_t *kc_lo,
                                                         const uint8_t *kc_hi, uint64_t n_reads, int k,
                                                         const uint32_t *bounds, int S, uint32_t *cnt, uint64_t stride,
                                                         uint32_t *err)
 {
-    __shared__ uint32_t sb[MAX_SCAN_COUNT + 1];
-    if (threadIdx.x <= (unsigned)S) sb[threadIdx.x] = bounds[threadIdx.x];
-    __syncthreads();
+    uint32_t sb[MAX_SCAN_COUNT + 1];  // scan bounds in registers (S + 1 used)
+#pragma unroll
+    for (int q = 0; q <= MAX_SCAN_COUNT; q++) sb[q] = q <= S ? bounds[q] : 0xFFFFFFFFu;
     const int lane = threadIdx.x & 31;
     const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
     const int sh = 2 * (k - 10);
     const uint32_t b_lo = sb[0], b_hi = sb[S];
     for (uint64_t r = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < n_reads; r += nw) {
         const uint64_t p0 = kc_off[r], np = kc_off[r + 1] - p0;
-        uint32_t c[MAX_SCAN_COUNT];
-#pragma unroll
-        for (int q = 0; q < MAX_SCAN_COUNT; q++) c[q] = 0;
+        uint32_t packed = 0;
         if (np > 300) {  // L - k >= 300 (enumerateKmers.c:155)
             if (lane == 0) atomicOr(err, DERR_LONG_READ);
         } else {
@@ -376,21 +377,18 @@ __global__ void __launch_bounds__(256) k_kc_count_scans(const uint64_t *kc_off, 
             }
 #pragma unroll
             for (int t = 0; t < KC_PER_LANE; t++) {
-                if (hv[t] == KC_NONE) continue;
+                if ((uint64_t)t * 32 >= np) break;  // uniform across the warp
                 const uint64_t km = (lv[t] >> 8) | ((uint64_t)hv[t] << 56);
                 const uint32_t b = (uint32_t)(km >> sh);
-                if (b < b_lo || b >= b_hi) continue;
-                int sc = 0;
+                if (hv[t] == KC_NONE || b < b_lo || b >= b_hi) continue;
+                uint32_t sc = 0;  // scans whose start is at or below b, past the first
 #pragma unroll
-                for (int q = 1; q < MAX_SCAN_COUNT; q++) sc += (q < S && b >= sb[q]) ? 1 : 0;
-#pragma unroll
-                for (int q = 0; q < MAX_SCAN_COUNT; q++) c[q] += (sc == q) ? 1u : 0u;
+                for (int q = 1; q < MAX_SCAN_COUNT; q++) sc += b >= sb[q] ? 1u : 0u;
+                packed += 1u << (4 * sc);
             }
         }
         for (int q = 0; q < S; q++) {
-            uint32_t x = c[q];
-#pragma unroll
-            for (int o = 16; o; o >>= 1) x += __shfl_xor_sync(FULL, x, o);
+            const uint32_t x = __reduce_add_sync(FULL, (packed >> (4 * q)) & 15u);
             if (lane == 0) {
                 cnt[(uint64_t)q * stride + r] = x;
                 if (x > 255) atomicOr(err, DERR_TOO_MANY);  // the reference's per-read counter is a uint8_t
