@@ -218,8 +218,7 @@ def main():
         job.reset()
         f, o = native.fastq_index_ptr(args.chunks, host_in.data_ptr(), nbytes)
         st = native.chunk_starts_of(f, o, [nbytes])
-        job.load_ptr(host_in.data_ptr(), nbytes)
-        cnt = job.count(args.k, st, min3)
+        cnt = job.load_count(host_in.data_ptr(), nbytes, args.k, st, min3)
         job.partition(args.k, args.scans, args.threads, st, cnt.chunk_first_read, cnt.hist, min3)
         _, total = job.prepare_output()
         if out_host is None or out_host.numel() < total:
@@ -481,8 +480,7 @@ def batch_mode(args, dist):
                 job.reset()
                 f, ofs = native.fastq_index_ptr(p.num_chunks, t.data_ptr(), t.numel())
                 st = native.chunk_starts_of(f, ofs, [t.numel()])
-                job.load_ptr(t.data_ptr(), t.numel())
-                cnt = job.count(p.k, st)
+                cnt = job.load_count(t.data_ptr(), t.numel(), p.k, st)
                 bnd = job.partition(p.k, p.num_scans, p.num_threads, st, cnt.chunk_first_read, cnt.hist)
                 job.prepare_output()
                 sizes.append((job.output_to(o.data_ptr(), o.numel()), bnd.tolist()))

@@ -87,6 +87,20 @@ uint64_t mp_launch_count(void);
 int mp_job_count(mp_job *job, int k, int min3, const uint64_t *chunk_starts, int nchunks, uint64_t *hist_out,
                  uint32_t *chunk_counts_out, uint64_t *chunk_reads_out);
 
+/* mp_job_load_fastq followed by mp_job_count (without per-chunk bucket counts), with the upload
+ * overlapped: for pinned host bytes and the plain variant, the input goes up in segments of whole
+ * chunks on a second stream while the job's stream parses and counts the segments already in HBM.
+ * Results, errors and the job state afterwards are those of the two calls made one after the other
+ * (which is also what runs for pageable bytes, the 3-minimizer variant, or when a segment fails).
+ * The reference reads each chunk from disk inside genHistograms' count loop (genHistograms.c:82-575);
+ * this has no further counterpart there. */
+int mp_job_load_count(mp_job *job, const char *bytes, uint64_t nbytes, const uint64_t *file_sizes, int nfiles,
+                      int interleaved, int k, int min3, const uint64_t *chunk_starts, int nchunks, uint64_t *hist_out,
+                      uint64_t *chunk_reads_out);
+/* Pieces the job's k-mer cache is held in: 0 (no cache), 1 (mp_job_count), or one per upload segment
+ * of mp_job_load_count.  Tracing only; no counterpart in the reference. */
+int mp_job_kmer_cache_pieces(const mp_job *job);
+
 typedef struct {
     int k;            /* kmerSize */
     int min3;         /* 1: 3-minimizer variant (enumerateKmers_3minimizers.c) */

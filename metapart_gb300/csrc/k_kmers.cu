@@ -397,9 +397,10 @@ __global__ void __launch_bounds__(256) k_kc_count_scans(const uint64_t *kc_off, 
     }
 }
 
-// K2b from the k-mer cache: the tuples of buckets [lo, hi) at off[read], in position order.
+// K2b from the k-mer cache: the tuples of buckets [lo, hi) at off[read], in position order.  The
+// cache may be one of several pieces: its reads are r0 .. r0 + n_reads - 1 (kc_off is the piece's).
 __global__ void __launch_bounds__(256) k_kc_write(const uint64_t *kc_off, const uint64_t *kc_lo, const uint8_t *kc_hi,
-                                                  uint64_t n_reads, int k, uint32_t lo, uint32_t hi,
+                                                  uint64_t r0, uint64_t n_reads, int k, uint32_t lo, uint32_t hi,
                                                   const uint32_t *label, const uint64_t *out_off, uint64_t *o_lo,
                                                   uint8_t *o_hi, uint32_t *o_id)
 {
@@ -409,12 +410,13 @@ __global__ void __launch_bounds__(256) k_kc_write(const uint64_t *kc_off, const 
     for (uint64_t r = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < n_reads; r += nw) {
         const uint64_t p0 = kc_off[r], np = kc_off[r + 1] - p0;
         if (np == 0 || np > 300) continue;
-        uint32_t id = (uint32_t)r;
+        const uint64_t gr = r0 + r;
+        uint32_t id = (uint32_t)gr;
         if (label) {
-            const uint32_t p = label[r];
-            id = (p == BAD) ? (uint32_t)r : p;  // findRoot after full compression (metapart.c:543-568)
+            const uint32_t p = label[gr];
+            id = (p == BAD) ? (uint32_t)gr : p;  // findRoot after full compression (metapart.c:543-568)
         }
-        uint64_t base = out_off[r];
+        uint64_t base = out_off[gr];
         // every position of the read (at most 300: 10 per lane) loaded at once
         uint64_t lv[KC_PER_LANE];
         uint32_t hv[KC_PER_LANE];
@@ -539,12 +541,13 @@ int launch_kc_count_scans(const uint64_t *kc_off, const uint64_t *kc_lo, const u
     return 0;
 }
 
-void launch_kc_write(const uint64_t *kc_off, const uint64_t *kc_lo, const uint8_t *kc_hi, uint64_t n_reads, int k,
-                     uint32_t lo, uint32_t hi, const uint32_t *label, const uint64_t *off, uint64_t *o_lo, uint8_t *o_hi,
-                     uint32_t *o_id, cudaStream_t st)
+void launch_kc_write(const uint64_t *kc_off, const uint64_t *kc_lo, const uint8_t *kc_hi, uint64_t r0, uint64_t n_reads,
+                     int k, uint32_t lo, uint32_t hi, const uint32_t *label, const uint64_t *off, uint64_t *o_lo,
+                     uint8_t *o_hi, uint32_t *o_id, cudaStream_t st)
 {
-    (mp::count_launch(), k_kc_write<<<grid_for(n_reads, 8), 256, 0, st>>>(kc_off, kc_lo, kc_hi, n_reads, k, lo, hi, label,
-                                                                       off, o_lo, o_hi, o_id));
+    if (n_reads == 0) return;
+    (mp::count_launch(), k_kc_write<<<grid_for(n_reads, 8), 256, 0, st>>>(kc_off, kc_lo, kc_hi, r0, n_reads, k, lo, hi,
+                                                                       label, off, o_lo, o_hi, o_id));
 }
 
 void launch_enum_write(const uint8_t *fq, const ParsedReads &pr, int k, int min3, uint32_t lo, uint32_t hi,

@@ -14,9 +14,10 @@ void launch_count(const uint8_t *fq, const ParsedReads &pr, int k, int min3, con
 void launch_kc_positions(const ParsedReads &pr, int k, uint32_t *npos, cudaStream_t st);
 int launch_kc_count_scans(const uint64_t *kc_off, const uint64_t *kc_lo, const uint8_t *kc_hi, uint64_t n_reads, int k,
                           const uint32_t *bounds, int S, uint32_t *cnt, uint64_t stride, uint32_t *err, cudaStream_t st);
-void launch_kc_write(const uint64_t *kc_off, const uint64_t *kc_lo, const uint8_t *kc_hi, uint64_t n_reads, int k,
-                     uint32_t lo, uint32_t hi, const uint32_t *label, const uint64_t *off, uint64_t *o_lo, uint8_t *o_hi,
-                     uint32_t *o_id, cudaStream_t st);
+// One cache piece (reads r0 .. r0 + n_reads - 1, kc_off the piece's own); label, off and the ids are global.
+void launch_kc_write(const uint64_t *kc_off, const uint64_t *kc_lo, const uint8_t *kc_hi, uint64_t r0, uint64_t n_reads,
+                     int k, uint32_t lo, uint32_t hi, const uint32_t *label, const uint64_t *off, uint64_t *o_lo,
+                     uint8_t *o_hi, uint32_t *o_id, cudaStream_t st);
 
 // K2a: tuples per read in the bucket range [lo, hi).
 void launch_enum_count(const uint8_t *fq, const ParsedReads &pr, int k, int min3, uint32_t lo, uint32_t hi,

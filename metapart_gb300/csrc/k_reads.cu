@@ -146,16 +146,18 @@ __device__ __forceinline__ uint32_t nl_in_word(uint32_t w)
     return ~(y | x | 0x7F7F7F7Fu);
 }
 
-__global__ void __launch_bounds__(NL_THREADS) k_nl_count(const uint8_t *buf, uint64_t n, uint32_t *seg_counts)
+// buf is 16-byte aligned; its first `skip` (< 16) bytes are not part of the parsed range, whose byte 0 is
+// buf[skip] (newline positions are written relative to it).
+__global__ void __launch_bounds__(NL_THREADS) k_nl_count(const uint8_t *buf, uint64_t n, uint32_t skip, uint32_t *seg_counts)
 {
     const uint64_t s0 = (uint64_t)blockIdx.x * NL_SEG, s1 = min(n, s0 + NL_SEG);
     uint32_t c = 0;
     for (uint64_t p = s0 + (uint64_t)threadIdx.x * 16; p < s1; p += NL_THREADS * 16) {
-        if (p + 16 <= s1) {
+        if (p + 16 <= s1 && p >= skip) {
             uint4 v = *reinterpret_cast<const uint4 *>(buf + p);
             c += __popc(nl_in_word(v.x)) + __popc(nl_in_word(v.y)) + __popc(nl_in_word(v.z)) + __popc(nl_in_word(v.w));
         } else {
-            for (uint64_t q = p; q < s1; q++) c += buf[q] == '\n';
+            for (uint64_t q = max(p, (uint64_t)skip); q < min(s1, p + 16); q++) c += buf[q] == '\n';
         }
     }
     uint64_t tot;
@@ -173,8 +175,8 @@ __global__ void __launch_bounds__(NL_THREADS) k_nl_count(const uint8_t *buf, uin
     }
 }
 
-__global__ void __launch_bounds__(NL_THREADS) k_nl_write(const uint8_t *buf, uint64_t n, const uint64_t *seg_off,
-                                                         uint64_t *nl_pos)
+__global__ void __launch_bounds__(NL_THREADS) k_nl_write(const uint8_t *buf, uint64_t n, uint32_t skip,
+                                                         const uint64_t *seg_off, uint64_t *nl_pos)
 {
     const uint64_t s0 = (uint64_t)blockIdx.x * NL_SEG, s1 = min(n, s0 + NL_SEG);
     uint64_t out = seg_off[blockIdx.x];
@@ -182,13 +184,13 @@ __global__ void __launch_bounds__(NL_THREADS) k_nl_write(const uint8_t *buf, uin
         const uint64_t p = r + (uint64_t)threadIdx.x * 16;
         uint8_t b[16];
         int cnt = 0;
-        if (p + 16 <= s1) {
+        if (p + 16 <= s1 && p >= skip) {
             uint4 v = *reinterpret_cast<const uint4 *>(buf + p);
             memcpy(b, &v, 16);
             cnt = __popc(nl_in_word(v.x)) + __popc(nl_in_word(v.y)) + __popc(nl_in_word(v.z)) + __popc(nl_in_word(v.w));
         } else {
             for (int q = 0; q < 16; q++) {
-                b[q] = (p + q < s1) ? buf[p + q] : 0;
+                b[q] = (p + q < s1 && p + q >= skip) ? buf[p + q] : 0;
                 cnt += b[q] == '\n';
             }
         }
@@ -197,7 +199,7 @@ __global__ void __launch_bounds__(NL_THREADS) k_nl_write(const uint8_t *buf, uin
         uint64_t o = out + pre;
 #pragma unroll
         for (int q = 0; q < 16; q++)
-            if (b[q] == '\n') nl_pos[o++] = p + q;
+            if (b[q] == '\n') nl_pos[o++] = p + q - skip;
         out += tot;
     }
 }
@@ -236,15 +238,27 @@ __global__ void k_record_of_offset(const uint64_t *rec_start, uint64_t n_rec, co
 
 int parse_fastq(const uint8_t *d_buf, uint64_t n, ParsedReads *pr, DeviceArena &arena, cudaStream_t st)
 {
-    if (n == 0) return set_error(MP_EFMT, "empty FASTQ input");
-    const uint64_t segs = (n + NL_SEG - 1) / NL_SEG;
+    return parse_fastq_range(d_buf, 0, n, pr, arena, st);
+}
+
+int parse_fastq_range(const uint8_t *d_base, uint64_t begin, uint64_t end, ParsedReads *pr, DeviceArena &arena,
+                      cudaStream_t st)
+{
+    const uint64_t n = end - begin;
+    if (n == 0 || end < begin) return set_error(MP_EFMT, "empty FASTQ input");
+    // the kernels read 16-byte words from the 16-byte boundary at or below begin and skip the bytes before it
+    const uint64_t a0 = begin & ~15ull;
+    const uint32_t skip = (uint32_t)(begin - a0);
+    const uint8_t *d_buf = d_base + a0;
+    const uint64_t na = end - a0;
+    const uint64_t segs = (na + NL_SEG - 1) / NL_SEG;
     uint32_t *seg_counts = arena.alloc<uint32_t>(segs);
     uint64_t *seg_off = arena.alloc<uint64_t>(segs + 1);
     uint64_t *total = arena.alloc<uint64_t>(1);
     size_t tb = scan_tmp_bytes(segs);
     void *tmp = arena.alloc<uint8_t>(tb);
     if (!seg_counts || !seg_off || !total || !tmp) return set_error(MP_ENOMEM, "device memory for the FASTQ parse");
-    (mp::count_launch(), k_nl_count<<<(unsigned)segs, NL_THREADS, 0, st>>>(d_buf, n, seg_counts));
+    (mp::count_launch(), k_nl_count<<<(unsigned)segs, NL_THREADS, 0, st>>>(d_buf, na, skip, seg_counts));
     scan_u32_to_u64(seg_counts, seg_off, segs, total, tmp, tb, st);
     uint64_t n_nl = 0;
     MP_CUDA(cudaMemcpyAsync(&n_nl, total, sizeof n_nl, cudaMemcpyDeviceToHost, st));
@@ -252,7 +266,7 @@ int parse_fastq(const uint8_t *d_buf, uint64_t n, ParsedReads *pr, DeviceArena &
     if (n_nl == 0 || n_nl % 4) return set_error(MP_EFMT, "FASTQ line count %llu is not a multiple of 4", (unsigned long long)n_nl);
     uint64_t *nl = arena.alloc<uint64_t>(n_nl);
     if (!nl) return set_error(MP_ENOMEM, "device memory for newline positions");
-    (mp::count_launch(), k_nl_write<<<(unsigned)segs, NL_THREADS, 0, st>>>(d_buf, n, seg_off, nl));
+    (mp::count_launch(), k_nl_write<<<(unsigned)segs, NL_THREADS, 0, st>>>(d_buf, na, skip, seg_off, nl));
     const uint64_t n_rec = n_nl / 4;
     pr->n_reads = n_rec;
     pr->rec_start = arena.alloc_persistent<uint64_t>(n_rec + 1);
@@ -272,6 +286,27 @@ int parse_fastq(const uint8_t *d_buf, uint64_t n, ParsedReads *pr, DeviceArena &
     if (last_end != n) return set_error(MP_EFMT, "FASTQ input does not end with a complete record");
     arena.release_scratch();
     return 0;
+}
+
+// Record table of one input segment (offsets relative to the segment) into the job's table at read r0,
+// offsets moved by the segment's byte offset; n + 1 start entries (the last is the next segment's first).
+__global__ void k_concat_records(const uint64_t *rs, const uint64_t *so, const uint32_t *sl, uint64_t n, uint64_t base,
+                                 uint64_t *drs, uint64_t *dso, uint32_t *dsl)
+{
+    const uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r > n) return;
+    drs[r] = rs[r] + base;
+    if (r < n) {
+        dso[r] = so[r] + base;
+        dsl[r] = sl[r];
+    }
+}
+
+void concat_records(const ParsedReads &seg, uint64_t byte_base, ParsedReads &dst, uint64_t r0, cudaStream_t st)
+{
+    (mp::count_launch(), k_concat_records<<<(unsigned)((seg.n_reads + 1 + 255) / 256), 256, 0, st>>>(
+        seg.rec_start, seg.seq_off, seg.seq_len, seg.n_reads, byte_base, dst.rec_start + r0, dst.seq_off + r0,
+        dst.seq_len + r0));
 }
 
 int records_at_offsets(const ParsedReads *pr, const uint64_t *h_offsets, int nq, uint64_t *h_rec, DeviceArena &arena,

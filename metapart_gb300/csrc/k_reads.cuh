@@ -82,6 +82,12 @@ struct ParsedReads {
 };
 
 int parse_fastq(const uint8_t *d_buf, uint64_t n, ParsedReads *pr, DeviceArena &arena, cudaStream_t st);
+// The same for the bytes [begin, end) of a 16-byte aligned buffer (offsets relative to begin).
+int parse_fastq_range(const uint8_t *d_base, uint64_t begin, uint64_t end, ParsedReads *pr, DeviceArena &arena,
+                      cudaStream_t st);
+// Copies a segment's record table (parsed from the segment alone) into dst at read r0, its offsets
+// moved by byte_base; dst's arrays hold all reads.
+void concat_records(const ParsedReads &seg, uint64_t byte_base, ParsedReads &dst, uint64_t r0, cudaStream_t st);
 int records_at_offsets(const ParsedReads *pr, const uint64_t *h_offsets, int nq, uint64_t *h_rec, DeviceArena &arena,
                        cudaStream_t st);
 

@@ -50,6 +50,14 @@ struct mp_ctx {
     std::mutex mu;
 };
 
+// A piece of the k-mer cache: the reads r0 .. r0 + n - 1, their position offsets off (n + 1, from 0)
+// and per position lo = canon << 8 | adj, hi = canon >> 56 (KC_NONE: the window holds an N).
+struct KcPiece {
+    uint64_t r0 = 0, n = 0;
+    uint64_t *off = nullptr, *lo = nullptr;
+    uint8_t *hi = nullptr;
+};
+
 struct mp_job {
     mp_ctx *ctx = nullptr;
     cudaStream_t st = nullptr;
@@ -62,11 +70,12 @@ struct mp_job {
     uint32_t *d_parent = nullptr;
     uint32_t *d_size = nullptr;
     uint8_t *d_filtered = nullptr;
-    // k-mer cache written by the count pass (plain variant): per-read position offsets, lo, hi
+    // k-mer cache written by the count pass (plain variant), in pieces of consecutive reads (one piece,
+    // or one per input segment of mp_job_load_count)
     bool kc_on = true;
     int kc_k = 0;
-    uint64_t *kc_off = nullptr, *kc_lo = nullptr;
-    uint8_t *kc_hi = nullptr;
+    std::vector<KcPiece> kc;
+    cudaStream_t copy_st = nullptr;  // uploads of mp_job_load_count
     int T = 0, nchunks = 0;
     std::vector<uint64_t> chunk_rec;
     uint64_t bounds[17] = {0};
@@ -252,42 +261,64 @@ int range_bounds(const uint64_t *hist, const uint64_t *ltr, int T, uint64_t scan
 
 void drop_kmer_cache(mp_job *j)
 {
-    j->arena.free_persistent(j->kc_off);
-    j->arena.free_persistent(j->kc_lo);
-    j->arena.free_persistent(j->kc_hi);
-    j->kc_off = j->kc_lo = nullptr;
-    j->kc_hi = nullptr;
+    for (KcPiece &q : j->kc) {
+        j->arena.free_persistent(q.off);
+        j->arena.free_persistent(q.lo);
+        j->arena.free_persistent(q.hi);
+    }
+    j->kc.clear();
     j->kc_k = 0;
 }
 
-// Cache arrays for the plain variant's count pass; false (and no cache) when device memory or the
-// budget does not allow it -- the partition then computes its k-mers from the reads.
-bool make_kmer_cache(mp_job *j, int k)
+// One cache piece for the reads of pr (global reads r0 ..): position offsets by a scan of L - k + 1,
+// and the lo/hi arrays; false (nothing kept) when device memory or the budget does not allow it.
+static bool make_kc_piece(mp_job *j, const ParsedReads &pr, uint64_t r0, int k, KcPiece *out)
 {
-    const uint64_t N = j->pr.n_reads;
+    const uint64_t N = pr.n_reads;
+    KcPiece q;
+    q.r0 = r0;
+    q.n = N;
     uint32_t *npos = j->arena.alloc<uint32_t>(N + 1);
     uint64_t *tot = j->arena.alloc<uint64_t>(1);
     size_t tb = scan_tmp_bytes(N + 1);
     void *tmp = j->arena.alloc<uint8_t>(tb);
-    j->kc_off = j->arena.alloc_persistent<uint64_t>(N + 2);
-    if (!npos || !tot || !tmp || !j->kc_off) {
-        drop_kmer_cache(j);
-        return false;
-    }
-    launch_kc_positions(j->pr, k, npos, j->st);
-    if (cudaMemsetAsync(npos + N, 0, 4, j->st) != cudaSuccess) return false;
-    scan_u32_to_u64(npos, j->kc_off, N + 1, tot, tmp, tb, j->st);
+    q.off = j->arena.alloc_persistent<uint64_t>(N + 2);
     uint64_t P = 0;
-    if (cudaMemcpyAsync(&P, tot, 8, cudaMemcpyDeviceToHost, j->st) != cudaSuccess || cudaStreamSynchronize(j->st) != cudaSuccess) {
+    bool ok = npos && tot && tmp && q.off;
+    if (ok) {
+        launch_kc_positions(pr, k, npos, j->st);
+        ok = cudaMemsetAsync(npos + N, 0, 4, j->st) == cudaSuccess;
+    }
+    if (ok) {
+        scan_u32_to_u64(npos, q.off, N + 1, tot, tmp, tb, j->st);
+        ok = cudaMemcpyAsync(&P, tot, 8, cudaMemcpyDeviceToHost, j->st) == cudaSuccess &&
+             cudaStreamSynchronize(j->st) == cudaSuccess;
+    }
+    if (ok) {
+        q.lo = j->arena.alloc_persistent<uint64_t>(P + 1);
+        q.hi = j->arena.alloc_persistent<uint8_t>(P + 1);
+        ok = q.lo && q.hi;
+    }
+    if (!ok) {
+        j->arena.free_persistent(q.off);
+        j->arena.free_persistent(q.lo);
+        j->arena.free_persistent(q.hi);
+        return false;
+    }
+    *out = q;
+    return true;
+}
+
+// The cache for the plain variant's count pass, one piece for all reads; false (and no cache) when
+// device memory or the budget does not allow it -- the partition then computes its k-mers from the reads.
+bool make_kmer_cache(mp_job *j, int k)
+{
+    KcPiece q;
+    if (!make_kc_piece(j, j->pr, 0, k, &q)) {
         drop_kmer_cache(j);
         return false;
     }
-    j->kc_lo = j->arena.alloc_persistent<uint64_t>(P + 1);
-    j->kc_hi = j->arena.alloc_persistent<uint8_t>(P + 1);
-    if (!j->kc_lo || !j->kc_hi) {
-        drop_kmer_cache(j);
-        return false;
-    }
+    j->kc.assign(1, q);
     j->kc_k = k;
     return true;
 }
@@ -361,6 +392,7 @@ void mp_job_destroy(mp_job *job)
     job->arena.release_all();
     cudaStreamSynchronize(job->st);
     cudaStreamDestroy(job->st);
+    if (job->copy_st) cudaStreamDestroy(job->copy_st);
     delete job;
 }
 
@@ -432,8 +464,7 @@ int mp_job_reset(mp_job *j)
     j->d_parent = j->d_size = nullptr;
     j->d_filtered = nullptr;
     j->d_out = nullptr;
-    j->kc_off = j->kc_lo = nullptr;
-    j->kc_hi = nullptr;
+    j->kc.clear();
     j->kc_k = 0;
     j->partitioned = j->output_ready = false;
     return 0;
@@ -466,8 +497,8 @@ int mp_job_count(mp_job *j, int k, int min3, const uint64_t *chunk_starts, int n
     {
         StageTimer tm(j->st, &j->stage_ms[1]);
         const bool kc = j->kc_on && !min3 && make_kmer_cache(j, k);
-        launch_count(j->d_fq, j->pr, k, min3, d_rec, nchunks, cc, glob, err, j->st, kc ? j->kc_off : nullptr,
-                     kc ? j->kc_lo : nullptr, kc ? j->kc_hi : nullptr);
+        launch_count(j->d_fq, j->pr, k, min3, d_rec, nchunks, cc, glob, err, j->st, kc ? j->kc[0].off : nullptr,
+                     kc ? j->kc[0].lo : nullptr, kc ? j->kc[0].hi : nullptr);
     }
     std::vector<unsigned long long> g(NB);
     uint32_t herr = 0;
@@ -486,6 +517,153 @@ int mp_job_count(mp_job *j, int k, int min3, const uint64_t *chunk_starts, int n
     if (chunk_reads_out)
         for (int c = 0; c < nchunks; c++) chunk_reads_out[c] = rec[c + 1] - rec[c];
     return 0;
+}
+
+namespace {
+
+constexpr int LC_SEGMENTS = 8;  // upload segments of mp_job_load_count
+
+// The pipelined body of mp_job_load_count: segment i's bytes go up on the copy stream while the job
+// stream parses and counts segment i - 1.  Each segment holds whole chunks, so it starts on a record
+// start of the whole input exactly when its own parse succeeds (a segment whose lines are not a multiple
+// of four, or that does not end with a complete record, fails); the segments' record tables then
+// concatenate to the whole input's.  Any failure returns non-zero and the caller reruns the steps one
+// after the other, which report it.
+int load_count_pipelined(mp_job *j, const char *bytes, uint64_t nbytes, const uint64_t *file_sizes, int nfiles,
+                         int interleaved, int k, const std::vector<uint64_t> &seg, const uint64_t *chunk_starts,
+                         int nchunks, uint64_t *hist_out, uint64_t *chunk_reads_out)
+{
+    const int S = (int)seg.size() - 1;
+    j->d_fq = j->arena.alloc_persistent<uint8_t>(nbytes + 64);
+    if (!j->d_fq) return MP_ENOMEM;
+    if (!j->copy_st && cudaStreamCreateWithFlags(&j->copy_st, cudaStreamNonBlocking) != cudaSuccess) {
+        j->copy_st = nullptr;
+        return MP_ECUDA;
+    }
+    std::vector<cudaEvent_t> ev(S + 1);
+    for (auto &e : ev) cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+    struct Guard {  // the copies end before anything below returns (an error path frees the buffer)
+        cudaStream_t cs;
+        std::vector<cudaEvent_t> &ev;
+        ~Guard()
+        {
+            cudaStreamSynchronize(cs);
+            for (auto &e : ev) cudaEventDestroy(e);
+        }
+    } guard{j->copy_st, ev};
+    cudaEventRecord(ev[S], j->st);  // the buffer exists
+    cudaStreamWaitEvent(j->copy_st, ev[S], 0);
+    for (int i = 0; i < S; i++) {
+        if (cudaMemcpyAsync(j->d_fq + seg[i], bytes + seg[i], seg[i + 1] - seg[i], cudaMemcpyHostToDevice, j->copy_st) !=
+            cudaSuccess)
+            return MP_ECUDA;
+        cudaEventRecord(ev[i], j->copy_st);
+    }
+    MP_CUDA(cudaMemsetAsync(j->d_fq + nbytes, 0, 64, j->st));
+    uint64_t tot = 0;
+    for (int f = 0; f < nfiles; f++) tot += file_sizes[f];
+    if (tot != nbytes) return MP_EARG;
+    j->fq_bytes = nbytes;
+    j->interleaved = interleaved;
+    j->stage_ms[0] = j->stage_ms[1] = 0;
+    unsigned long long *glob = j->arena.alloc_persistent<unsigned long long>(NB);
+    uint32_t *err = j->arena.alloc_persistent<uint32_t>(1);
+    if (!glob || !err) return MP_ENOMEM;
+    MP_CUDA(cudaMemsetAsync(glob, 0, NB * 8, j->st));
+    MP_CUDA(cudaMemsetAsync(err, 0, 4, j->st));
+    drop_kmer_cache(j);
+    std::vector<ParsedReads> prs(S);
+    std::vector<uint64_t> R(S + 1, 0);
+    for (int i = 0; i < S; i++) {
+        MP_CUDA(cudaStreamWaitEvent(j->st, ev[i], 0));
+        {
+            StageTimer tm(j->st, &j->stage_ms[0]);
+            if (parse_fastq_range(j->d_fq, seg[i], seg[i + 1], &prs[i], j->arena, j->st)) return MP_EFMT;
+        }
+        R[i + 1] = R[i] + prs[i].n_reads;
+        StageTimer tm(j->st, &j->stage_ms[1]);
+        KcPiece q;
+        if (!make_kc_piece(j, prs[i], R[i], k, &q)) return MP_ENOMEM;
+        j->kc.push_back(q);
+        launch_count(j->d_fq + seg[i], prs[i], k, 0, nullptr, 0, nullptr, glob, err, j->st, q.off, q.lo, q.hi);
+    }
+    j->kc_k = k;
+    const uint64_t N = R[S];
+    if (N >= UMAX32 || (interleaved && (N & 1))) return MP_EFMT;
+    {
+        StageTimer tm(j->st, &j->stage_ms[0]);
+        j->pr.n_reads = N;
+        j->pr.rec_start = j->arena.alloc_persistent<uint64_t>(N + 1);
+        j->pr.seq_off = j->arena.alloc_persistent<uint64_t>(N + 1);
+        j->pr.seq_len = j->arena.alloc_persistent<uint32_t>(N + 1);
+        if (!j->pr.rec_start || !j->pr.seq_off || !j->pr.seq_len) return MP_ENOMEM;
+        for (int i = 0; i < S; i++) concat_records(prs[i], seg[i], j->pr, R[i], j->st);
+    }
+    for (auto &p : prs) {
+        j->arena.free_persistent(p.rec_start);
+        j->arena.free_persistent(p.seq_off);
+        j->arena.free_persistent(p.seq_len);
+    }
+    // the checks of the load (files end on record ends) and of the count (chunks start on records)
+    std::vector<uint64_t> ends;
+    uint64_t acc = 0;
+    for (int f = 0; f + 1 < nfiles; f++) ends.push_back(acc += file_sizes[f]);
+    if (!ends.empty()) {
+        std::vector<uint64_t> rec(ends.size());
+        if (records_at_offsets(&j->pr, ends.data(), (int)ends.size(), rec.data(), j->arena, j->st)) return MP_EFMT;
+    }
+    std::vector<uint64_t> rec;
+    if (chunk_records(j, chunk_starts, nchunks, rec)) return MP_EFMT;
+    std::vector<unsigned long long> g(NB);
+    uint32_t herr = 0;
+    MP_CUDA(cudaMemcpyAsync(g.data(), glob, NB * 8, cudaMemcpyDeviceToHost, j->st));
+    MP_CUDA(cudaMemcpyAsync(&herr, err, 4, cudaMemcpyDeviceToHost, j->st));
+    MP_CUDA(cudaStreamSynchronize(j->st));
+    MP_CUDA(cudaGetLastError());
+    j->arena.free_persistent(glob);
+    j->arena.free_persistent(err);
+    j->arena.release_scratch();
+    if (herr) return MP_EUNSUP;
+    hist_out[0] = 0;
+    for (uint32_t b = 1; b <= NB; b++) hist_out[b] = hist_out[b - 1] + g[b - 1];
+    if (chunk_reads_out)
+        for (int c = 0; c < nchunks; c++) chunk_reads_out[c] = rec[c + 1] - rec[c];
+    return 0;
+}
+
+}  // namespace
+
+int mp_job_load_count(mp_job *j, const char *bytes, uint64_t nbytes, const uint64_t *file_sizes, int nfiles,
+                      int interleaved, int k, int min3, const uint64_t *chunk_starts, int nchunks, uint64_t *hist_out,
+                      uint64_t *chunk_reads_out)
+{
+    if (!j || !bytes || !file_sizes || nfiles < 1 || !chunk_starts || !hist_out || nchunks < 1)
+        return set_error(MP_EARG, "bad argument");
+    if (k < 11 || k > 31) return set_error(MP_EARG, "k must be in [11, 31]");
+    MP_CUDA(cudaSetDevice(j->ctx->device));
+    if (j->d_fq) return set_error(MP_EARG, "the job already holds reads");
+    auto one_by_one = [&]() -> int {
+        int rc = mp_job_load_fastq(j, bytes, nbytes, file_sizes, nfiles, interleaved);
+        return rc ? rc : mp_job_count(j, k, min3, chunk_starts, nchunks, hist_out, nullptr, chunk_reads_out);
+    };
+    // pinned input (asynchronous copies), the k-mer cache variant, ascending chunks over the whole input
+    cudaPointerAttributes pa{};
+    const bool pinned = cudaPointerGetAttributes(&pa, bytes) == cudaSuccess && pa.type == cudaMemoryTypeHost;
+    cudaGetLastError();
+    bool ok = pinned && !min3 && j->kc_on && nchunks >= 2 && chunk_starts[0] == 0 && chunk_starts[nchunks] == nbytes;
+    for (int c = 0; ok && c < nchunks; c++) ok = chunk_starts[c] <= chunk_starts[c + 1];
+    if (!ok) return one_by_one();
+    std::vector<uint64_t> seg = {0};
+    for (int c = 1; c < nchunks; c++)
+        if (chunk_starts[c] > seg.back() && chunk_starts[c] >= (uint64_t)((double)nbytes * seg.size() / LC_SEGMENTS))
+            seg.push_back(chunk_starts[c]);
+    seg.push_back(nbytes);
+    if (seg.size() < 3) return one_by_one();
+    if (load_count_pipelined(j, bytes, nbytes, file_sizes, nfiles, interleaved, k, seg, chunk_starts, nchunks, hist_out,
+                             chunk_reads_out) == 0)
+        return 0;
+    int rc = mp_job_reset(j);
+    return rc ? rc : one_by_one();
 }
 
 int mp_job_partition(mp_job *j, const mp_part_params *p, const uint64_t *chunk_starts, const uint64_t *chunk_first_read,
@@ -551,7 +729,7 @@ int mp_job_partition(mp_job *j, const mp_part_params *p, const uint64_t *chunk_s
     MP_CUDA(cudaMemcpyAsync(d_hist, hist, (NB + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, j->st));
     uint32_t *cnt_all = nullptr, *d_b = nullptr;
     // the count pass's k-mer cache serves this partition when it holds the same k (plain variant)
-    const bool use_kc = j->kc_lo && j->kc_k == k && !p->min3 && S <= 8;
+    const bool use_kc = !j->kc.empty() && j->kc_k == k && !p->min3 && S <= 8;
     {
         bool mono = !p->min3 && S <= 8;
         for (int s = 0; s < S && mono; s++) mono = scanR[s] <= scanR[s + 1];
@@ -562,8 +740,12 @@ int mp_job_partition(mp_job *j, const mp_part_params *p, const uint64_t *chunk_s
             std::vector<uint32_t> hb(scanR.begin(), scanR.end());
             StageTimer tm(j->st, &j->stage_ms[2]);
             MP_CUDA(cudaMemcpyAsync(d_b, hb.data(), (S + 1) * 4, cudaMemcpyHostToDevice, j->st));
-            const int lrc = use_kc ? launch_kc_count_scans(j->kc_off, j->kc_lo, j->kc_hi, N, k, d_b, S, cnt_all, N + 1, err, j->st)
-                                   : launch_enum_count_scans(j->d_fq, j->pr, k, d_b, S, cnt_all, N + 1, err, j->st);
+            int lrc = 0;
+            if (use_kc)
+                for (const KcPiece &q : j->kc)
+                    lrc |= q.n ? launch_kc_count_scans(q.off, q.lo, q.hi, q.n, k, d_b, S, cnt_all + q.r0, N + 1, err, j->st) : 0;
+            else
+                lrc = launch_enum_count_scans(j->d_fq, j->pr, k, d_b, S, cnt_all, N + 1, err, j->st);
             if (lrc) return set_error(MP_EARG, "enumeration count over %d scans", S);
             for (int s = 0; s < S; s++) MP_CUDA(cudaMemsetAsync(cnt_all + (size_t)s * (N + 1) + N, 0, 4, j->st));
         }
@@ -605,8 +787,9 @@ int mp_job_partition(mp_job *j, const mp_part_params *p, const uint64_t *chunk_s
                     return set_error(MP_ENOMEM, "device memory for %llu tuples", (unsigned long long)n);
             }
             if (use_kc && cnt_all)
-                launch_kc_write(j->kc_off, j->kc_lo, j->kc_hi, N, k, (uint32_t)lo, (uint32_t)hi, s ? j->d_parent : nullptr,
-                                off, sb.lo[0], sb.hi[0], sb.id[0], j->st);
+                for (const KcPiece &q : j->kc)
+                    launch_kc_write(q.off, q.lo, q.hi, q.r0, q.n, k, (uint32_t)lo, (uint32_t)hi, s ? j->d_parent : nullptr,
+                                    off, sb.lo[0], sb.hi[0], sb.id[0], j->st);
             else
                 launch_enum_write(j->d_fq, j->pr, k, p->min3, (uint32_t)lo, (uint32_t)hi, s ? j->d_parent : nullptr, off,
                                   sb.lo[0], sb.hi[0], sb.id[0], err, j->st);
@@ -723,6 +906,8 @@ int mp_job_output(mp_job *j, char *out, uint64_t capacity, uint64_t *file_sizes,
     }
     return 0;
 }
+
+int mp_job_kmer_cache_pieces(const mp_job *j) { return j ? (int)j->kc.size() : 0; }
 
 int mp_job_set_kmer_cache(mp_job *j, int enable)
 {

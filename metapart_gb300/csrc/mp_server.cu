@@ -105,11 +105,9 @@ void run_request(mp_server *s, mp_job *job, Request &rq, mp_result &res)
     if (!rc) {
         starts.assign(ofs.begin(), ofs.begin() + nrec);
         starts[nrec - 1] = rq.nbytes;
-        rc = mp_job_load_fastq(job, rq.fastq, rq.nbytes, &rq.nbytes, 1, p.interleaved);
-    }
-    if (!rc) {
         std::vector<uint64_t> reads(C);
-        rc = mp_job_count(job, p.k, p.min3, starts.data(), C, hist.data(), nullptr, reads.data());
+        rc = mp_job_load_count(job, rq.fastq, rq.nbytes, &rq.nbytes, 1, p.interleaved, p.k, p.min3, starts.data(), C,
+                               hist.data(), reads.data());
         first[0] = 0;
         for (int c = 0; c < C && !rc; c++) first[c + 1] = first[c] + reads[c];
     }

@@ -51,6 +51,9 @@ def lib():
         L.mp_job_num_reads.argtypes = [C.c_void_p]
         L.mp_job_num_reads.restype = C.c_uint64
         L.mp_job_count.argtypes = [C.c_void_p, C.c_int, C.c_int, u64p, C.c_int, u64p, u32p, u64p]
+        L.mp_job_kmer_cache_pieces.argtypes = [C.c_void_p]
+        L.mp_job_load_count.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64, u64p, C.c_int, C.c_int, C.c_int, C.c_int,
+                                        u64p, C.c_int, u64p, u64p]
         L.mp_job_partition.argtypes = [C.c_void_p, C.c_void_p, u64p, u64p, C.c_int, u64p, u64p]
         L.mp_job_labels.argtypes = [C.c_void_p, u32p]
         L.mp_job_output.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64, u64p, u64p]
@@ -199,6 +202,22 @@ class Job:
         ccp = cc.ctypes.data_as(C.POINTER(C.c_uint32)) if cc is not None else None
         _check(lib().mp_job_count(self.h, k, int(min3), _p64(starts), nch, _p64(hist), ccp, _p64(reads)), "count")
         return CountResult(hist, reads, cc)
+
+    def load_count(self, host_ptr: int, nbytes: int, k: int, chunk_starts, min3: bool = False,
+                   interleaved: bool = False, file_sizes=None) -> CountResult:
+        """load_ptr followed by count, the upload overlapped with parsing and counting (pinned host bytes)."""
+        fs = np.array(file_sizes if file_sizes is not None else [nbytes], dtype=np.uint64)
+        starts = np.ascontiguousarray(chunk_starts, dtype=np.uint64)
+        nch = len(starts) - 1
+        hist = np.zeros(NB + 1, dtype=np.uint64)
+        reads = np.zeros(nch, dtype=np.uint64)
+        _check(lib().mp_job_load_count(self.h, C.c_void_p(host_ptr), nbytes, _p64(fs), len(fs), int(interleaved), k,
+                                       int(min3), _p64(starts), nch, _p64(hist), _p64(reads)), "load_count")
+        return CountResult(hist, reads, None)
+
+    @property
+    def kmer_cache_pieces(self) -> int:
+        return int(lib().mp_job_kmer_cache_pieces(self.h))
 
     def partition(self, k: int, num_scans: int, num_threads: int, chunk_starts, chunk_first_read, hist,
                   min3: bool = False) -> np.ndarray:
