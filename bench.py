@@ -220,7 +220,7 @@ def main():
         st = native.chunk_starts_of(f, o, [nbytes])
         cnt = job.load_count(host_in.data_ptr(), nbytes, args.k, st, min3)
         job.partition(args.k, args.scans, args.threads, st, cnt.chunk_first_read, cnt.hist, min3)
-        _, total = job.prepare_output()
+        _, total = job.output_plan()
         if out_host is None or out_host.numel() < total:
             out_host = torch.empty(total + 16, dtype=torch.uint8, pin_memory=True)
         return job.output_to(out_host.data_ptr(), out_host.numel())
@@ -482,7 +482,7 @@ def batch_mode(args, dist):
                 st = native.chunk_starts_of(f, ofs, [t.numel()])
                 cnt = job.load_count(t.data_ptr(), t.numel(), p.k, st)
                 bnd = job.partition(p.k, p.num_scans, p.num_threads, st, cnt.chunk_first_read, cnt.hist)
-                job.prepare_output()
+                job.output_plan()
                 sizes.append((job.output_to(o.data_ptr(), o.numel()), bnd.tolist()))
         finally:
             job.close()

@@ -125,8 +125,14 @@ int mp_job_labels(mp_job *job, uint32_t *out);
 
 /* Partition FASTQ output, grouped by file j = partition * num_threads + tid in the order of the
  * reference's FromTid<tid>_ToRank<partition>.paired.fastq files.
- * Replaces writeOutput3 (metapart.c:956-1066).  With out == NULL only file_sizes/total are filled. */
+ * Replaces writeOutput3 (metapart.c:956-1066).  With out == NULL only file_sizes/total are filled (the
+ * files' layout is planned, no bytes move).  With out, the files are built in HBM in batches, each
+ * batch copied down while the next is built. */
 int mp_job_output(mp_job *job, char *out, uint64_t capacity, uint64_t *file_sizes, uint64_t *total);
+
+/* The same files built in HBM (kept by the job until it is reset or partitions again): *d_out their
+ * device address.  For a caller that consumes them on the GPU; no counterpart in the reference. */
+int mp_job_output_device(mp_job *job, const void **d_out, uint64_t *file_sizes, uint64_t *total);
 
 /* Stable sort of k-mer tuples by (k-mer, adjacency byte) on the device (onesweep LSD radix sort).
  * Replaces radixPass and the range-partition + 9-pass driver of sortKmerList (metapart.c:1494-1598,

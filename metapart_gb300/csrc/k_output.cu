@@ -122,10 +122,11 @@ __global__ void k_out_copy(OutCtx c, const uint8_t *fq, const uint32_t *val, con
     if ((uint64_t)lane < l - t0) out[o + t0 + lane] = fq[s + t0 + lane];
 }
 
-int gather_output(const uint8_t *d_fq, const ParsedReads &pr, const uint32_t *d_label, const uint64_t *bounds_host,
-                  const uint64_t *chunk_rec_host, int nchunks, int T, int interleaved, uint8_t **d_out,
-                  uint64_t *total_out, std::vector<uint64_t> &file_sizes, DeviceArena &arena, cudaStream_t st)
+int plan_output(const uint8_t *d_fq, const ParsedReads &pr, const uint32_t *d_label, const uint64_t *bounds_host,
+                const uint64_t *chunk_rec_host, int nchunks, int T, int interleaved, OutputPlan *plan,
+                std::vector<uint64_t> &file_sizes, DeviceArena &arena, cudaStream_t st)
 {
+    (void)d_fq;
     const uint64_t units = interleaved ? pr.n_reads / 2 : pr.n_reads;
     const int nf = 16 * T;
     file_sizes.assign(nf, 0);
@@ -166,24 +167,44 @@ int gather_output(const uint8_t *d_fq, const ParsedReads &pr, const uint32_t *d_
     (mp::count_launch(), k_out_entries<<<gb, 256, 0, st>>>(c, f1, f2, nent, eoff, sb.lo[0], sb.id[0]));
     int rc = radix_sort(sb, n, false, arena, st, nullptr);
     if (rc) return rc;
-    uint64_t *len = arena.alloc<uint64_t>(n + 1), *off = arena.alloc<uint64_t>(n + 1);
+    uint64_t *len = arena.alloc<uint64_t>(n + 1);
+    plan->val = arena.alloc_persistent<uint32_t>(n + 1);
+    plan->off = arena.alloc_persistent<uint64_t>(n + 1);
     size_t tb2 = scan_tmp_bytes(n + 1);
     void *tmp2 = arena.alloc<uint8_t>(tb2);
-    if (!len || !off || !tmp2) return set_error(MP_ENOMEM, "device memory for the output offsets");
+    if (!len || !plan->val || !plan->off || !tmp2) return set_error(MP_ENOMEM, "device memory for the output offsets");
     const unsigned ge = (unsigned)((n + 255) / 256);
     (mp::count_launch(), k_out_len<<<ge, 256, 0, st>>>(c, sb.id[sb.cur], n, len, sb.lo[sb.cur], fbytes));
-    scan_u64(len, off, n, ntot, tmp2, tb2, st);
+    scan_u64(len, plan->off, n, ntot, tmp2, tb2, st);
+    MP_CUDA(cudaMemcpyAsync(plan->val, sb.id[sb.cur], n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, st));
     uint64_t total = 0;
     MP_CUDA(cudaMemcpyAsync(&total, ntot, sizeof total, cudaMemcpyDeviceToHost, st));
     MP_CUDA(cudaMemcpyAsync(file_sizes.data(), fbytes, nf * sizeof(uint64_t), cudaMemcpyDeviceToHost, st));
     MP_CUDA(cudaStreamSynchronize(st));
-    uint8_t *out = arena.alloc_persistent<uint8_t>(total + 16);
-    if (!out) return set_error(MP_ENOMEM, "device memory for the output bytes");
-    if (n) (mp::count_launch(), k_out_copy<<<(unsigned)((n * 32 + 255) / 256), 256, 0, st>>>(c, d_fq, sb.id[sb.cur], off, n, out));
     MP_CUDA(cudaGetLastError());
-    *d_out = out;
-    *total_out = total;
+    plan->n = n;
+    plan->total = total;
+    plan->rec_start = pr.rec_start;
+    plan->interleaved = interleaved;
     return 0;
+}
+
+int copy_output_range(const OutputPlan &plan, uint64_t e0, uint64_t e1, const uint8_t *d_fq, uint8_t *dst,
+                      cudaStream_t st)
+{
+    if (e1 <= e0) return 0;
+    OutCtx c{};
+    c.rec_start = plan.rec_start;
+    c.interleaved = plan.interleaved;
+    (mp::count_launch(), k_out_copy<<<(unsigned)(((e1 - e0) * 32 + 255) / 256), 256, 0, st>>>(
+        c, d_fq, plan.val + e0, plan.off + e0, e1 - e0, dst));
+    MP_CUDA(cudaGetLastError());
+    return 0;
+}
+
+int copy_output(const OutputPlan &plan, const uint8_t *d_fq, uint8_t *dst, cudaStream_t st)
+{
+    return copy_output_range(plan, 0, plan.n, d_fq, dst, st);
 }
 
 }  // namespace mp

@@ -5,10 +5,25 @@
 
 namespace mp {
 
-// Builds the concatenated partition files in device memory (persistent allocation of the arena).
-// file_sizes: 16 * T byte counts in file order j = partition * T + tid.
-int gather_output(const uint8_t *d_fq, const ParsedReads &pr, const uint32_t *d_label, const uint64_t *bounds_host,
-                  const uint64_t *chunk_rec_host, int nchunks, int T, int interleaved, uint8_t **d_out,
-                  uint64_t *total_out, std::vector<uint64_t> &file_sizes, DeviceArena &arena, cudaStream_t st);
+// Where every record goes in the concatenated partition files (file j = partition * T + tid): the
+// entries' units in file order (val), their byte offsets (off), the total; persistent arena arrays.
+struct OutputPlan {
+    uint32_t *val = nullptr;
+    uint64_t *off = nullptr;
+    uint64_t n = 0, total = 0;
+    const uint64_t *rec_start = nullptr;
+    int interleaved = 0;
+};
+
+// The plan; file_sizes: 16 * T byte counts in file order.
+int plan_output(const uint8_t *d_fq, const ParsedReads &pr, const uint32_t *d_label, const uint64_t *bounds_host,
+                const uint64_t *chunk_rec_host, int nchunks, int T, int interleaved, OutputPlan *plan,
+                std::vector<uint64_t> &file_sizes, DeviceArena &arena, cudaStream_t st);
+
+// The records' bytes to dst (plan.total bytes, 4-byte aligned device memory); _range: the entries
+// [e0, e1) only (their bytes [off[e0], off[e1]) of dst).
+int copy_output(const OutputPlan &plan, const uint8_t *d_fq, uint8_t *dst, cudaStream_t st);
+int copy_output_range(const OutputPlan &plan, uint64_t e0, uint64_t e1, const uint8_t *d_fq, uint8_t *dst,
+                      cudaStream_t st);
 
 }  // namespace mp

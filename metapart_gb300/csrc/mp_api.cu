@@ -84,7 +84,8 @@ struct mp_job {
     uint8_t *d_out = nullptr;
     uint64_t out_total = 0;
     std::vector<uint64_t> out_sizes;
-    bool output_ready = false;
+    bool output_ready = false;  // out_plan holds the partition files' layout
+    OutputPlan out_plan;
     std::string dump_dir;
     double stage_ms[8] = {0};
     SortStats sort_stats;
@@ -464,6 +465,7 @@ int mp_job_reset(mp_job *j)
     j->d_parent = j->d_size = nullptr;
     j->d_filtered = nullptr;
     j->d_out = nullptr;
+    j->out_plan = OutputPlan{};
     j->kc.clear();
     j->kc_k = 0;
     j->partitioned = j->output_ready = false;
@@ -711,6 +713,9 @@ int mp_job_partition(mp_job *j, const mp_part_params *p, const uint64_t *chunk_s
     if (j->d_size) { j->arena.free_persistent(j->d_size); j->d_size = nullptr; }
     if (j->d_filtered) { j->arena.free_persistent(j->d_filtered); j->d_filtered = nullptr; }
     if (j->d_out) { j->arena.free_persistent(j->d_out); j->d_out = nullptr; }
+    j->arena.free_persistent(j->out_plan.val);
+    j->arena.free_persistent(j->out_plan.off);
+    j->out_plan = OutputPlan{};
     j->d_parent = j->arena.alloc_persistent<uint32_t>(N + 1);
     j->d_size = j->arena.alloc_persistent<uint32_t>(N + 1);
     j->d_filtered = j->arena.alloc_persistent<uint8_t>(N + 1);
@@ -884,26 +889,112 @@ int mp_job_labels(mp_job *j, uint32_t *out)
     return 0;
 }
 
+namespace {
+
+// The partition files' layout (once per partition).
+int plan_job_output(mp_job *j)
+{
+    if (j->output_ready) return 0;
+    StageTimer tm(j->st, &j->stage_ms[7]);
+    j->stage_ms[7] = 0;
+    int rc = plan_output(j->d_fq, j->pr, j->d_parent, j->bounds, j->chunk_rec.data(), j->nchunks, j->T, j->interleaved,
+                         &j->out_plan, j->out_sizes, j->arena, j->st);
+    j->arena.release_scratch();
+    if (rc) return rc;
+    j->out_total = j->out_plan.total;
+    j->output_ready = true;
+    return 0;
+}
+
+// The partition files in HBM (once per partition).
+int materialize_output(mp_job *j)
+{
+    if (j->d_out) return 0;
+    StageTimer tm(j->st, &j->stage_ms[7]);
+    j->d_out = j->arena.alloc_persistent<uint8_t>(j->out_total + 16);
+    if (!j->d_out) return set_error(MP_ENOMEM, "device memory for the output bytes");
+    return copy_output(j->out_plan, j->d_fq, j->d_out, j->st);
+}
+
+// The files built in HBM in batches of entries; each batch's bytes go down on the copy stream while the
+// next batch is built (copying records straight into mapped host memory from the kernel was slower: the
+// small writes use the host link worse than the copy engine).
+int materialize_and_download(mp_job *j, uint8_t *out)
+{
+    constexpr int K = 8;
+    const OutputPlan &pl = j->out_plan;
+    if (pl.n < (uint64_t)K * 1024 || pl.total == 0) {
+        int rc = materialize_output(j);
+        if (rc) return rc;
+        MP_CUDA(cudaMemcpyAsync(out, j->d_out, j->out_total, cudaMemcpyDeviceToHost, j->st));
+        MP_CUDA(cudaStreamSynchronize(j->st));
+        return 0;
+    }
+    if (!j->copy_st && cudaStreamCreateWithFlags(&j->copy_st, cudaStreamNonBlocking) != cudaSuccess) {
+        j->copy_st = nullptr;
+        return set_error(MP_ECUDA, "cannot create a stream");
+    }
+    uint64_t e[K + 1], o[K + 1];
+    for (int b = 0; b <= K; b++) e[b] = pl.n * (uint64_t)b / K;
+    for (int b = 0; b < K; b++) MP_CUDA(cudaMemcpyAsync(&o[b], pl.off + e[b], 8, cudaMemcpyDeviceToHost, j->st));
+    o[K] = pl.total;
+    j->d_out = j->arena.alloc_persistent<uint8_t>(pl.total + 16);
+    if (!j->d_out) return set_error(MP_ENOMEM, "device memory for the output bytes");
+    MP_CUDA(cudaStreamSynchronize(j->st));
+    cudaEvent_t ev[K];
+    for (auto &x : ev) cudaEventCreateWithFlags(&x, cudaEventDisableTiming);
+    int rc = 0;
+    {
+        StageTimer tm(j->st, &j->stage_ms[7]);
+        for (int b = 0; b < K && !rc; b++) {
+            rc = copy_output_range(pl, e[b], e[b + 1], j->d_fq, j->d_out, j->st);
+            cudaEventRecord(ev[b], j->st);
+            cudaStreamWaitEvent(j->copy_st, ev[b], 0);
+            if (!rc && cudaMemcpyAsync(out + o[b], j->d_out + o[b], o[b + 1] - o[b], cudaMemcpyDeviceToHost, j->copy_st) !=
+                           cudaSuccess)
+                rc = set_error(MP_ECUDA, "copy of the partition files");
+        }
+    }
+    cudaStreamSynchronize(j->copy_st);
+    cudaStreamSynchronize(j->st);
+    for (auto &x : ev) cudaEventDestroy(x);
+    MP_CUDA(cudaGetLastError());
+    return rc;
+}
+
+}  // namespace
+
 int mp_job_output(mp_job *j, char *out, uint64_t capacity, uint64_t *file_sizes, uint64_t *total)
 {
     if (!j || !j->partitioned) return set_error(MP_EARG, "no partition result in this job");
     MP_CUDA(cudaSetDevice(j->ctx->device));
-    if (!j->output_ready) {
-        StageTimer tm(j->st, &j->stage_ms[7]);
-        j->stage_ms[7] = 0;
-        int rc = gather_output(j->d_fq, j->pr, j->d_parent, j->bounds, j->chunk_rec.data(), j->nchunks, j->T,
-                               j->interleaved, &j->d_out, &j->out_total, j->out_sizes, j->arena, j->st);
-        j->arena.release_scratch();
-        if (rc) return rc;
-        j->output_ready = true;
-    }
+    int rc = plan_job_output(j);
+    if (rc) return rc;
     if (file_sizes) memcpy(file_sizes, j->out_sizes.data(), j->out_sizes.size() * 8);
     if (total) *total = j->out_total;
     if (out) {
         if (capacity < j->out_total) return set_error(MP_EARG, "output buffer too small");
-        MP_CUDA(cudaMemcpyAsync(out, j->d_out, j->out_total, cudaMemcpyDeviceToHost, j->st));
-        MP_CUDA(cudaStreamSynchronize(j->st));
+        if (j->d_out) {
+            MP_CUDA(cudaMemcpyAsync(out, j->d_out, j->out_total, cudaMemcpyDeviceToHost, j->st));
+            MP_CUDA(cudaStreamSynchronize(j->st));
+        } else if ((rc = materialize_and_download(j, (uint8_t *)out))) {
+            return rc;
+        }
     }
+    return 0;
+}
+
+int mp_job_output_device(mp_job *j, const void **d_out, uint64_t *file_sizes, uint64_t *total)
+{
+    if (!j || !j->partitioned) return set_error(MP_EARG, "no partition result in this job");
+    MP_CUDA(cudaSetDevice(j->ctx->device));
+    int rc = plan_job_output(j);
+    if (!rc) rc = materialize_output(j);
+    if (rc) return rc;
+    MP_CUDA(cudaStreamSynchronize(j->st));
+    if (d_out) *d_out = j->d_out;
+    if (file_sizes) memcpy(file_sizes, j->out_sizes.data(), j->out_sizes.size() * 8);
+    if (total) *total = j->out_total;
     return 0;
 }
 

@@ -57,6 +57,7 @@ def lib():
         L.mp_job_partition.argtypes = [C.c_void_p, C.c_void_p, u64p, u64p, C.c_int, u64p, u64p]
         L.mp_job_labels.argtypes = [C.c_void_p, u32p]
         L.mp_job_output.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64, u64p, u64p]
+        L.mp_job_output_device.argtypes = [C.c_void_p, C.POINTER(C.c_void_p), u64p, u64p]
         L.mp_job_set_dump_dir.argtypes = [C.c_void_p, C.c_char_p]
         L.mp_job_set_kmer_cache.argtypes = [C.c_void_p, C.c_int]
         L.mp_job_stage_ms.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.c_int]
@@ -164,6 +165,14 @@ class Job:
 
     def prepare_output(self):
         """Builds the partition files in device memory; returns (file sizes, total bytes)."""
+        sizes = np.zeros(16 * self.num_threads, dtype=np.uint64)
+        total = C.c_uint64()
+        ptr = C.c_void_p()
+        _check(lib().mp_job_output_device(self.h, C.byref(ptr), _p64(sizes), C.byref(total)), "output_device")
+        return sizes, total.value
+
+    def output_plan(self):
+        """The partition files' sizes (file sizes, total bytes); no bytes move."""
         sizes = np.zeros(16 * self.num_threads, dtype=np.uint64)
         total = C.c_uint64()
         _check(lib().mp_job_output(self.h, None, 0, _p64(sizes), C.byref(total)), "output")

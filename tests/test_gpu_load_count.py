@@ -142,3 +142,23 @@ def test_chunk_start_off_a_record(ctx):
     st = _starts([data], 16, False)
     st[5] += 1
     _both_fail_alike(ctx, data, st)
+
+
+def test_output_into_pinned_memory(ctx):
+    """Partition files built batch by batch, each batch copied down while the next is built, equal those
+    built whole and copied at once."""
+    import torch
+    data = synth.fastq_bytes(synth.workload("interleaved_small", 20000, seed=36))
+    job, _, _ = native.run_pipeline(ctx, data, 27, 8, 2, 2, interleaved=True)
+    try:
+        sizes, total = job.output_plan()
+        pinned = torch.zeros(total + 16, dtype=torch.uint8).pin_memory()
+        assert job.output_to(pinned.data_ptr(), pinned.numel()) == total
+        via_hbm, sizes2 = job.output()  # the files already in HBM: one copy
+        assert bytes(pinned[:total].numpy()) == bytes(via_hbm) and np.array_equal(sizes, sizes2)
+        job.prepare_output()
+        again = torch.zeros(total + 16, dtype=torch.uint8).pin_memory()
+        job.output_to(again.data_ptr(), again.numel())
+        assert bytes(again[:total].numpy()) == bytes(via_hbm)
+    finally:
+        job.close()
