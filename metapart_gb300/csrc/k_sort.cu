@@ -395,13 +395,14 @@ constexpr int SS_ITEMS = 12;
 constexpr int SS_CAP = SS_THREADS * SS_ITEMS;  // 12288 tuples per unit
 constexpr int SS_WARPS = SS_THREADS / 32;
 constexpr uint32_t SS_MAXB = 4096;             // buckets per unit
-constexpr int SS_MAXBITS = 10;                 // widest digit of the unit sort
+constexpr int SS_MAXBITS = 9;                  // widest digit of the unit sort (53 varying bits: six passes)
 constexpr int SS_BINS = 1 << SS_MAXBITS;
 
 struct SegSmem {
     uint64_t key[SS_CAP];                // 96 KB
     uint16_t perm[2][SS_CAP];            // 48 KB
-    uint16_t whist[SS_WARPS][SS_BINS];   // 64 KB: digit counts per warp, then each (warp, digit)'s offset in the digit
+    uint32_t ids[SS_CAP];                // 48 KB: the unit's ids, loaded with the keys
+    uint16_t whist[SS_WARPS][SS_BINS];   // 32 KB: digit counts per warp, then each (warp, digit)'s offset in the digit
     uint16_t dstart[SS_BINS];            // first position of each digit
     uint32_t wsum[SS_WARPS];
     unsigned long long kor, kand;
@@ -518,12 +519,13 @@ __global__ void __launch_bounds__(SS_THREADS) k_segsort(const uint64_t *__restri
         }
         // all loads of the unit in flight at once
         uint64_t lr[SS_ITEMS];
-        uint32_t hr[SS_ITEMS];
+        uint32_t hr[SS_ITEMS], ir[SS_ITEMS];
 #pragma unroll
         for (int j = 0; j < SS_ITEMS; j++) {
             const uint32_t e = threadIdx.x + j * SS_THREADS;
             lr[j] = e < cnt ? lo_in[start + e] : 0ull;
             hr[j] = (hi_in && e < cnt) ? (uint32_t)hi_in[start + e] : 0u;
+            ir[j] = e < cnt ? id_in[start + e] : 0u;
         }
         __syncthreads();
         unsigned long long kor = 0, kand = ~0ull;
@@ -534,6 +536,7 @@ __global__ void __launch_bounds__(SS_THREADS) k_segsort(const uint64_t *__restri
                 const uint64_t km = (lr[j] >> 8) | ((uint64_t)hr[j] << 56);
                 const uint64_t key = ((uint64_t)((uint32_t)(km >> bsh) - b0) << lowbits) | (lr[j] & lowmask);
                 sm.key[e] = key;
+                sm.ids[e] = ir[j];
                 kor |= key;
                 kand &= key;
             }
@@ -566,23 +569,12 @@ __global__ void __launch_bounds__(SS_THREADS) k_segsort(const uint64_t *__restri
             }
         }
         const long long t2 = clock64();
-        for (uint32_t e0 = threadIdx.x; e0 < cnt; e0 += 4 * SS_THREADS) {  // four id gathers in flight
-            uint32_t sidx[4], idv[4];
-#pragma unroll
-            for (int q = 0; q < 4; q++) {
-                const uint32_t e = e0 + q * SS_THREADS;
-                sidx[q] = e < cnt ? (cur < 0 ? e : (uint32_t)sm.perm[cur][e]) : 0u;
-                idv[q] = e < cnt ? id_in[start + sidx[q]] : 0u;
-            }
-#pragma unroll
-            for (int q = 0; q < 4; q++) {
-                const uint32_t e = e0 + q * SS_THREADS;
-                if (e >= cnt) break;
-                const uint64_t key = sm.key[sidx[q]];
-                const uint64_t bucket = b0 + (key >> lowbits);
-                lo_out[start + e] = (bucket << lowbits) | (key & lowmask);
-                id_out[start + e] = idv[q];
-            }
+        for (uint32_t e = threadIdx.x; e < cnt; e += SS_THREADS) {
+            const uint32_t sidx = cur < 0 ? e : (uint32_t)sm.perm[cur][e];
+            const uint64_t key = sm.key[sidx];
+            const uint64_t bucket = b0 + (key >> lowbits);
+            lo_out[start + e] = (bucket << lowbits) | (key & lowmask);
+            id_out[start + e] = sm.ids[sidx];
         }
         __syncthreads();  // the next unit reuses the shared arrays
         cyc[0] += (unsigned long long)(t1 - t0);
