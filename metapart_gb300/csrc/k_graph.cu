@@ -497,57 +497,83 @@ __device__ __forceinline__ unsigned long long resv_key(uint32_t round, uint32_t 
 
 // The round kernels read their list lengths from device memory (written by the previous kernel),
 // so the host launches several rounds between synchronisations; grid-stride loops cover any length.
+// The loops step whole warps (lanes past the list end idle), so a warp appends its entries to a list
+// with one atomic (the order of a list's entries does not matter: a commit is decided by the round's
+// reservations, not by list position).
+
+// Appends v (where pred) to list; all 32 lanes call it.
+__device__ __forceinline__ void warp_append(uint32_t *list, unsigned int *count, bool pred, uint32_t v, int lane)
+{
+    const uint32_t m = __ballot_sync(FULLW, pred);
+    uint32_t base = 0;
+    if (lane == 0 && m) base = atomicAdd(count, (unsigned int)__popc(m));
+    base = __shfl_sync(FULLW, base, 0);
+    if (pred) list[base + __popc(m & ((1u << lane) - 1))] = v;
+}
+
 __global__ void k_pe_reserve(uint32_t *parent, const uint32_t *size, const uint32_t *act, const unsigned int *nact_p,
                              uint32_t *act2, unsigned int *nact2, uint32_t *pra, uint32_t *prb, uint32_t *psa,
                              uint32_t *psb, unsigned long long *resv, uint32_t round, uint32_t limit)
 {
     const uint32_t nact = *nact_p;
-    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < nact; t += gridDim.x * blockDim.x) {
-        const uint32_t j = act[t];
-        const uint32_t ra = uf_find(parent, 2 * j), rb = uf_find(parent, 2 * j + 1);
-        if (ra == rb) continue;
-        const uint32_t za = size[ra], zb = size[rb];
-        const bool sa = za <= limit, sb = zb <= limit;
-        if (!sa && !sb) continue;
-        pra[j] = ra;
-        prb[j] = rb;
-        psa[j] = za;  // sizes at the start of the round: the commit kernel changes sizes while it runs
-        psb[j] = zb;
-        act2[atomicAdd(nact2, 1u)] = j;
-        const unsigned long long key = resv_key(round, j);
-        if (sa) atomicMax(&resv[ra], key);
-        if (sb) atomicMax(&resv[rb], key);
+    const int lane = threadIdx.x & 31;
+    for (uint32_t w0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); w0 < nact; w0 += gridDim.x * blockDim.x) {
+        const uint32_t t = w0 + lane;
+        bool keep = false, sa = false, sb = false;
+        uint32_t j = 0, ra = 0, rb = 0;
+        if (t < nact) {
+            j = act[t];
+            ra = 2 * j;
+            rb = 2 * j + 1;
+            uf_find2(parent, ra, rb);
+            if (ra != rb) {
+                const uint32_t za = size[ra], zb = size[rb];
+                sa = za <= limit;
+                sb = zb <= limit;
+                keep = sa || sb;
+                if (keep) {
+                    pra[j] = ra;
+                    prb[j] = rb;
+                    psa[j] = za;  // sizes at the start of the round: the commit kernel changes sizes while it runs
+                    psb[j] = zb;
+                }
+            }
+        }
+        warp_append(act2, nact2, keep, j, lane);
+        if (keep) {
+            const unsigned long long key = resv_key(round, j);
+            if (sa) atomicMax(&resv[ra], key);
+            if (sb) atomicMax(&resv[rb], key);
+        }
     }
 }
 
-__device__ __forceinline__ void pe_commit_one(uint32_t *parent, uint32_t *size, uint32_t j, uint32_t *next,
-                                              unsigned int *nnext, uint32_t *pra, uint32_t *prb, const uint32_t *psa,
-                                              const uint32_t *psb, const unsigned long long *resv, unsigned long long *gmax,
-                                              unsigned long long *gadd, uint32_t *bigsmall, unsigned int *nbig,
-                                              uint32_t round, uint32_t limit)
+// The commit of pair j: 0 = committed a small-small merge, 1 = back to the next round's list,
+// 2 = a small root under a large one (to k_pe_bigsmall).
+__device__ __forceinline__ int pe_commit_one(uint32_t *parent, uint32_t *size, uint32_t j, uint32_t *pra, uint32_t *prb,
+                                             const uint32_t *psa, const uint32_t *psb, const unsigned long long *resv,
+                                             unsigned long long *gmax, unsigned long long *gadd, uint32_t round,
+                                             uint32_t limit)
 {
     const uint32_t ra = pra[j], rb = prb[j];
     const uint32_t za = psa[j], zb = psb[j];
     const bool sa = za <= limit, sb = zb <= limit;
     const unsigned long long key = resv_key(round, j);
     const bool own = (!sa || resv[ra] == key) && (!sb || resv[rb] == key);
-    if (!own) {
-        next[atomicAdd(nnext, 1u)] = j;
-        return;
-    }
+    if (!own) return 1;
     if (sa && sb) {
         const uint32_t hi = ra > rb ? ra : rb, lo = ra > rb ? rb : ra;
         parent[lo] = hi;
         size[hi] = za + zb;
         size[lo] = 0;
-        return;
+        return 0;
     }
     const uint32_t g = sa ? rb : ra, x = sa ? ra : rb;
     atomicMax(&gmax[g], ((unsigned long long)round << 32) | x);
     atomicAdd(&gadd[g], (unsigned long long)(sa ? za : zb));
     pra[j] = g;  // k_pe_bigsmall reads the roles from here: sizes change while it runs
     prb[j] = x;
-    bigsmall[atomicAdd(nbig, 1u)] = j;
+    return 2;
 }
 
 __global__ void k_pe_commit(uint32_t *parent, uint32_t *size, const uint32_t *act, const unsigned int *nact_p, uint32_t *next,
@@ -556,8 +582,18 @@ __global__ void k_pe_commit(uint32_t *parent, uint32_t *size, const uint32_t *ac
                             uint32_t *bigsmall, unsigned int *nbig, uint32_t round, uint32_t limit)
 {
     const uint32_t nact = *nact_p;
-    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < nact; t += gridDim.x * blockDim.x)
-        pe_commit_one(parent, size, act[t], next, nnext, pra, prb, psa, psb, resv, gmax, gadd, bigsmall, nbig, round, limit);
+    const int lane = threadIdx.x & 31;
+    for (uint32_t w0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); w0 < nact; w0 += gridDim.x * blockDim.x) {
+        const uint32_t t = w0 + lane;
+        int r = -1;
+        uint32_t j = 0;
+        if (t < nact) {
+            j = act[t];
+            r = pe_commit_one(parent, size, j, pra, prb, psa, psb, resv, gmax, gadd, round, limit);
+        }
+        warp_append(next, nnext, r == 1, j, lane);
+        warp_append(bigsmall, nbig, r == 2, j, lane);
+    }
 }
 
 __device__ __forceinline__ void pe_bigsmall_one(uint32_t *parent, uint32_t *size, uint32_t j, const uint32_t *pra,
