@@ -269,13 +269,19 @@ __device__ __forceinline__ uint32_t uf_find(uint32_t *parent, uint32_t x)
 }
 
 // uf_find of x and of y advanced together (the same steps and path halving), so the parent loads of
-// the two walks are in flight at the same time.
+// the two walks are in flight at the same time.  When the walks meet (the same node on both) the two
+// are in one component: x and y come back equal without the rest of the walk (callers use the results
+// as roots only when they differ).
 __device__ __forceinline__ void uf_find2(uint32_t *parent, uint32_t &x, uint32_t &y)
 {
     bool dx = false, dy = false;
     for (;;) {
         const uint32_t px = dx ? x : parent[x];
         const uint32_t py = dy ? y : parent[y];
+        if (px == py && px != BAD) {
+            x = y = px;
+            return;
+        }
         dx = dx || px == x || px == BAD;
         dy = dy || py == y || py == BAD;
         if (dx && dy) return;
