@@ -139,9 +139,23 @@ __global__ void __launch_bounds__(256) k_filter_warp(const uint64_t *lo, const u
     }
     uint64_t nlv = c0 + lane < n ? lo[c0 + lane] : 0;  // next window's words, loaded one window ahead
     uint8_t nhv = (hi && c0 + lane < n) ? hi[c0 + lane] : 0;
+    // range ends: the warp's windows advance in order, so a cursor over the sorted ends gives each window
+    // the ends in [p, p + 32] as a bit mask (bit e - p)
+    int ne = 0;
+    {
+        int lo_i = 0, hi_i = T;  // first end >= c0
+        while (lo_i < hi_i) {
+            const int m = (lo_i + hi_i) >> 1;
+            if (ends[m] < c0) lo_i = m + 1; else hi_i = m;
+        }
+        ne = lo_i;
+    }
     for (uint64_t p = c0;; p += 32) {
         const bool owned = p < c1;
         if (!owned && !open) break;
+        uint64_t emask = 0;
+        while (ne < T && ends[ne] < p + 32) emask |= 1ull << (ends[ne++] - p);
+        if (ne < T && ends[ne] == p + 32) emask |= 1ull << 32;
         const uint64_t i = p + lane;
         const bool valid = i < n;
         const uint64_t lv = nlv;
@@ -202,7 +216,7 @@ __global__ void __launch_bounds__(256) k_filter_warp(const uint64_t *lo, const u
             if (fh < 32 || arr_end) {
                 const uint64_t re = fh < 32 ? p + fh : n;
                 open = false;
-                if (!at_range_end(ends, T, re)) {
+                if (!((emask >> (re - p)) & 1u)) {
                     const uint32_t J = judge_run(cb, ca, deg);
                     if (J & J_ANY)
                         for (uint64_t q = rs + lane; q < re; q += 32) mark_tuple(J, q, (uint32_t)(lo[q] & 0xFF), id, parent, filtered, z);
@@ -223,7 +237,7 @@ __global__ void __launch_bounds__(256) k_filter_warp(const uint64_t *lo, const u
 #pragma unroll
                 for (int c = 0; c < 7; c++) { b[c] = __popc(Bm[c] & m); a[c] = __popc(Am[c] & m); }
                 const uint64_t re = nh < 32 ? p + nh : n;
-                if (!at_range_end(ends, T, re)) J = judge_run(b, a, __popc(m));
+                if (!((emask >> (re - p)) & 1u)) J = judge_run(b, a, __popc(m));
             }
         }
         const uint32_t Js = __shfl_sync(FULLW, J, s < 0 ? 0 : s);
