@@ -99,17 +99,9 @@ __global__ void k_out_len(OutCtx c, const uint32_t *val, uint64_t n, uint64_t *l
     if (v && lane == last) atomicAdd(&file_bytes[f], (unsigned long long)(incl - (first > 0 ? before : 0)));
 }
 
-// A warp per record: bytes up to the first 4-byte boundary of the destination, then aligned 4-byte
-// words assembled from two aligned source words by a funnel shift, then the tail bytes.  Source
-// words may reach 3 bytes past the record; the FASTQ buffer carries 64 bytes of padding.
-__global__ void k_out_copy(OutCtx c, const uint8_t *fq, const uint32_t *val, const uint64_t *off, uint64_t n, uint8_t *out)
+// One record (l bytes at fq + s) to out + o by a warp.
+__device__ __forceinline__ void copy_record(const uint8_t *fq, uint64_t s, uint64_t l, uint64_t o, uint8_t *out, int lane)
 {
-    const uint64_t w = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
-    if (w >= n) return;
-    const uint64_t u = val[w];
-    const uint64_t r0 = c.interleaved ? 2 * u : u, r1 = c.interleaved ? 2 * u + 2 : u + 1;
-    const uint64_t s = c.rec_start[r0], l = c.rec_start[r1] - s, o = off[w];
     const uint64_t head = min(l, (uint64_t)((4 - (o & 3)) & 3));
     if ((uint64_t)lane < head) out[o + lane] = fq[s + lane];
     const uint64_t words = (l - head) >> 2;
@@ -120,6 +112,33 @@ __global__ void k_out_copy(OutCtx c, const uint8_t *fq, const uint32_t *val, con
     for (uint64_t j = lane; j < words; j += 32) dst[j] = __funnelshift_r(src[j], src[j + 1], a);
     const uint64_t t0 = head + (words << 2);
     if ((uint64_t)lane < l - t0) out[o + t0 + lane] = fq[s + t0 + lane];
+}
+
+constexpr int OC_PER_WARP = 8;  // records per warp in k_out_copy
+
+// A warp copies OC_PER_WARP records: lanes fetch the records' source ranges and destinations in one
+// round, then for each record: bytes up to the first 4-byte boundary of the destination, aligned
+// 4-byte words assembled from two aligned source words by a funnel shift, the tail bytes.  Source
+// words may reach 3 bytes past the record; the FASTQ buffer carries 64 bytes of padding.
+__global__ void k_out_copy(OutCtx c, const uint8_t *fq, const uint32_t *val, const uint64_t *off, uint64_t n, uint8_t *out)
+{
+    const uint64_t w0 = (((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * OC_PER_WARP;
+    const int lane = threadIdx.x & 31;
+    if (w0 >= n) return;
+    uint64_t my_s = 0, my_l = 0, my_o = 0;  // lane q < OC_PER_WARP: record w0 + q
+    if (lane < OC_PER_WARP && w0 + lane < n) {
+        const uint64_t u = val[w0 + lane];
+        const uint64_t r0 = c.interleaved ? 2 * u : u, r1 = c.interleaved ? 2 * u + 2 : u + 1;
+        my_s = c.rec_start[r0];
+        my_l = c.rec_start[r1] - my_s;
+        my_o = off[w0 + lane];
+    }
+    const int nrec = (int)min((uint64_t)OC_PER_WARP, n - w0);
+    for (int q = 0; q < nrec; q++) {
+        const uint64_t s = __shfl_sync(0xFFFFFFFFu, my_s, q), l = __shfl_sync(0xFFFFFFFFu, my_l, q),
+                       o = __shfl_sync(0xFFFFFFFFu, my_o, q);
+        copy_record(fq, s, l, o, out, lane);
+    }
 }
 
 int plan_output(const uint8_t *d_fq, const ParsedReads &pr, const uint32_t *d_label, const uint64_t *bounds_host,
@@ -196,7 +215,8 @@ int copy_output_range(const OutputPlan &plan, uint64_t e0, uint64_t e1, const ui
     OutCtx c{};
     c.rec_start = plan.rec_start;
     c.interleaved = plan.interleaved;
-    (mp::count_launch(), k_out_copy<<<(unsigned)(((e1 - e0) * 32 + 255) / 256), 256, 0, st>>>(
+    const uint64_t warps = (e1 - e0 + OC_PER_WARP - 1) / OC_PER_WARP;
+    (mp::count_launch(), k_out_copy<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, st>>>(
         c, d_fq, plan.val + e0, plan.off + e0, e1 - e0, dst));
     MP_CUDA(cudaGetLastError());
     return 0;
