@@ -360,8 +360,14 @@ __global__ void __launch_bounds__(256) k_kc_count_scans(const uint64_t *kc_off, 
     const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
     const int sh = 2 * (k - 10);
     const uint32_t b_lo = sb[0], b_hi = sb[S];
-    for (uint64_t r = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < n_reads; r += nw) {
-        const uint64_t p0 = kc_off[r], np = kc_off[r + 1] - p0;
+    uint64_t r = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    uint64_t n0 = r < n_reads ? kc_off[r] : 0, n1 = r < n_reads ? kc_off[r + 1] : 0;  // the read's offsets, a read ahead
+    for (; r < n_reads; r += nw) {
+        const uint64_t p0 = n0, np = n1 - n0;
+        if (r + nw < n_reads) {
+            n0 = kc_off[r + nw];
+            n1 = kc_off[r + nw + 1];
+        }
         uint32_t packed = 0;
         if (np > 300) {  // L - k >= 300 (enumerateKmers.c:155)
             if (lane == 0) atomicOr(err, DERR_LONG_READ);
@@ -407,16 +413,30 @@ __global__ void __launch_bounds__(256) k_kc_write(const uint64_t *kc_off, const 
     const int lane = threadIdx.x & 31;
     const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
     const int sh = 2 * (k - 10);
-    for (uint64_t r = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < n_reads; r += nw) {
-        const uint64_t p0 = kc_off[r], np = kc_off[r + 1] - p0;
-        if (np == 0 || np > 300) continue;
+    uint64_t r = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    // the read's offsets, label and output offset, loaded a read ahead
+    uint64_t n0 = 0, n1 = 0, nb = 0;
+    uint32_t nl = 0;
+    if (r < n_reads) {
+        n0 = kc_off[r];
+        n1 = kc_off[r + 1];
+        nb = out_off[r0 + r];
+        nl = label ? label[r0 + r] : 0u;
+    }
+    for (; r < n_reads; r += nw) {
+        const uint64_t p0 = n0, np = n1 - n0;
         const uint64_t gr = r0 + r;
-        uint32_t id = (uint32_t)gr;
-        if (label) {
-            const uint32_t p = label[gr];
-            id = (p == BAD) ? (uint32_t)gr : p;  // findRoot after full compression (metapart.c:543-568)
+        uint64_t base = nb;
+        const uint32_t lab = nl;
+        if (r + nw < n_reads) {
+            n0 = kc_off[r + nw];
+            n1 = kc_off[r + nw + 1];
+            nb = out_off[gr + nw];
+            if (label) nl = label[gr + nw];
         }
-        uint64_t base = out_off[gr];
+        if (np == 0 || np > 300) continue;
+        uint32_t id = (uint32_t)gr;
+        if (label) id = (lab == BAD) ? (uint32_t)gr : lab;  // findRoot after full compression (metapart.c:543-568)
         // every position of the read (at most 300: 10 per lane) loaded at once
         uint64_t lv[KC_PER_LANE];
         uint32_t hv[KC_PER_LANE];
