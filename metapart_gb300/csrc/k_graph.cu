@@ -269,23 +269,11 @@ __global__ void k_apply_zero(uint64_t *lo, uint8_t *hi, uint64_t n, const uint32
 
 // ---------------------------------------------------------- union-find
 
-__device__ __forceinline__ uint32_t uf_find(uint32_t *parent, uint32_t x)
-{
-    uint32_t p = parent[x];
-    while (p != x && p != BAD) {
-        const uint32_t gp = parent[p];
-        if (gp == p || gp == BAD) return p;
-        parent[x] = gp;  // path halving: gp is an ancestor of x
-        x = gp;
-        p = parent[x];
-    }
-    return x;
-}
-
-// uf_find of x and of y advanced together (the same steps and path halving), so the parent loads of
-// the two walks are in flight at the same time.  When the walks meet (the same node on both) the two
-// are in one component: x and y come back equal without the rest of the walk (callers use the results
-// as roots only when they differ).
+// The roots of x and of y, the two walks advanced together so that their parent loads are in flight at
+// the same time.  A walk stops at a node that is its own parent or whose parent is BAD (a BAD read is
+// its own root, unionfind.h:25-32), and halves its path as it goes (a node is pointed at its
+// grandparent).  When the walks meet (the same node on both) the two are in one component: x and y come
+// back equal without the rest of the walk (callers use the results as roots only when they differ).
 __device__ __forceinline__ void uf_find2(uint32_t *parent, uint32_t &x, uint32_t &y)
 {
     bool dx = false, dy = false;
