@@ -162,3 +162,26 @@ def test_output_into_pinned_memory(ctx):
         assert bytes(again[:total].numpy()) == bytes(via_hbm)
     finally:
         job.close()
+
+
+def _edge_reads(n, seed, k):
+    """The golden set's edge-case reads: lengths around k up to the longest read, N runs, poly-A/T,
+    palindromes, duplicates, lowercase and IUPAC bytes."""
+    import importlib.util
+    from pathlib import Path
+    spec = importlib.util.spec_from_file_location("make_golden", Path(__file__).resolve().parent / "golden" /
+                                                  "make_golden.py")
+    mg = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mg)
+    return mg.edge_fastq(n, seed, k, False)
+
+
+@pytest.mark.parametrize("k", [31, 21])
+def test_edge_reads(ctx, tmp_path, k):
+    data = _edge_reads(6000, 40 + k, k)
+    a = _run(ctx, [data], k, 16, 2, 2, False, "pinned", tmp_path / "a")
+    b = _run(ctx, [data], k, 16, 2, 2, False, "steps", tmp_path / "b")
+    assert a["pieces"] > 1
+    _same(a, b)
+    for f in sorted(p.name for p in (tmp_path / "a").iterdir()):
+        assert (tmp_path / "a" / f).read_bytes() == (tmp_path / "b" / f).read_bytes(), f
