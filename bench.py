@@ -197,7 +197,8 @@ def main():
     starts = native.chunk_starts_of(fno, ofs, [nbytes])
     host_in = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
     host_in.numpy()[:] = np.frombuffer(fq, dtype=np.uint8)
-    dev_in = host_in.to(f"cuda:{dev}")
+    dev_in = torch.zeros(nbytes + 64, dtype=torch.uint8, device=f"cuda:{dev}")  # 64 readable bytes past the reads
+    dev_in[:nbytes].copy_(host_in)
     del fq
     ctx = native.Context(dev)
     job = native.Job(ctx)
@@ -206,7 +207,7 @@ def main():
 
     def device_step():
         job.reset()
-        job.load_device(dev_in.data_ptr(), nbytes)
+        job.load_device_inplace(dev_in.data_ptr(), nbytes)  # the reads already in HBM, used where they are
         cnt = job.count(args.k, starts, min3)
         job.partition(args.k, args.scans, args.threads, starts, cnt.chunk_first_read, cnt.hist, min3)
         job.prepare_output()

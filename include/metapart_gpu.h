@@ -65,6 +65,11 @@ int mp_job_load_fastq(mp_job *job, const char *bytes, uint64_t nbytes, const uin
 /* Same, for bytes already in device memory (copied into the job). */
 int mp_job_load_fastq_device(mp_job *job, const void *dev_bytes, uint64_t nbytes, const uint64_t *file_sizes,
                              int nfiles, int interleaved);
+/* Same, using bytes already in device memory in place (no copy): they must start on a 16-byte boundary,
+ * be followed by 64 readable bytes, and stay unchanged until the job is reset or destroyed.  For a caller
+ * whose reads are already in HBM; no counterpart in the reference. */
+int mp_job_load_fastq_device_inplace(mp_job *job, const void *dev_bytes, uint64_t nbytes, const uint64_t *file_sizes,
+                                     int nfiles, int interleaved);
 uint64_t mp_job_num_reads(const mp_job *job);
 
 /* Releases the job's reads and stage state (device memory) and keeps its stream, so one job can

@@ -451,6 +451,17 @@ int mp_job_load_fastq_device(mp_job *j, const void *dev_bytes, uint64_t nbytes, 
     return load_common(j, nbytes, file_sizes, nfiles, interleaved);
 }
 
+int mp_job_load_fastq_device_inplace(mp_job *j, const void *dev_bytes, uint64_t nbytes, const uint64_t *file_sizes,
+                                     int nfiles, int interleaved)
+{
+    if (!j || !dev_bytes || !file_sizes || nfiles < 1) return set_error(MP_EARG, "null argument");
+    if ((uintptr_t)dev_bytes & 15) return set_error(MP_EARG, "the FASTQ bytes must start on a 16-byte boundary");
+    MP_CUDA(cudaSetDevice(j->ctx->device));
+    if (j->d_fq) return set_error(MP_EARG, "the job already holds reads");
+    j->d_fq = (uint8_t *)dev_bytes;  // borrowed: not the arena's, so a reset drops it without freeing it
+    return load_common(j, nbytes, file_sizes, nfiles, interleaved);
+}
+
 uint64_t mp_job_num_reads(const mp_job *j) { return j ? j->pr.n_reads : 0; }
 
 int mp_job_reset(mp_job *j)

@@ -44,6 +44,7 @@ def lib():
         L.mp_job_destroy.argtypes = [C.c_void_p]
         L.mp_job_load_fastq.argtypes = [C.c_void_p, C.c_char_p, C.c_uint64, u64p, C.c_int, C.c_int]
         L.mp_job_load_fastq_device.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64, u64p, C.c_int, C.c_int]
+        L.mp_job_load_fastq_device_inplace.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64, u64p, C.c_int, C.c_int]
         L.mp_job_reset.argtypes = [C.c_void_p]
         L.mp_job_stream.argtypes = [C.c_void_p]
         L.mp_job_stream.restype = C.c_void_p
@@ -156,6 +157,13 @@ class Job:
         fs = np.array(file_sizes if file_sizes is not None else [nbytes], dtype=np.uint64)
         _check(lib().mp_job_load_fastq_device(self.h, C.c_void_p(dev_ptr), nbytes, _p64(fs), len(fs), int(interleaved)),
                "load_device")
+
+    def load_device_inplace(self, dev_ptr: int, nbytes: int, file_sizes=None, interleaved: bool = False):
+        """Uses FASTQ bytes already in device memory in place: 16-byte aligned, followed by 64 readable
+        bytes, unchanged until the job is reset."""
+        fs = np.array(file_sizes if file_sizes is not None else [nbytes], dtype=np.uint64)
+        _check(lib().mp_job_load_fastq_device_inplace(self.h, C.c_void_p(dev_ptr), nbytes, _p64(fs), len(fs),
+                                                      int(interleaved)), "load_device_inplace")
 
     def load_ptr(self, host_ptr: int, nbytes: int, interleaved: bool = False):
         """Upload from a host address (pinned memory for full copy bandwidth)."""

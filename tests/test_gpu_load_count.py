@@ -185,3 +185,36 @@ def test_edge_reads(ctx, tmp_path, k):
     _same(a, b)
     for f in sorted(p.name for p in (tmp_path / "a").iterdir()):
         assert (tmp_path / "a" / f).read_bytes() == (tmp_path / "b" / f).read_bytes(), f
+
+
+def test_device_bytes_used_in_place(ctx):
+    """Reads already in device memory used where they are give the results of an upload."""
+    import torch
+    data = synth.fastq_bytes(synth.workload("plain_small", 20000, seed=37))
+    starts = _starts([data], 8, False)
+    dev = torch.zeros(len(data) + 64, dtype=torch.uint8, device="cuda")
+    dev[:len(data)].copy_(torch.frombuffer(bytearray(data), dtype=torch.uint8))
+    res = []
+    for inplace in (True, False):
+        job = native.Job(ctx)
+        try:
+            if inplace:
+                job.load_device_inplace(dev.data_ptr(), len(data))
+            else:
+                job.load(data)
+            cnt = job.count(31, starts)
+            bounds = job.partition(31, 2, 2, starts, cnt.chunk_first_read, cnt.hist)
+            out, sizes = job.output()
+            res.append((cnt.hist.copy(), bytes(out), sizes.copy(), bounds.copy(), job.labels()))
+        finally:
+            job.close()
+    assert np.array_equal(res[0][0], res[1][0]) and res[0][1] == res[1][1]
+    for x, y in zip(res[0][2:], res[1][2:]):
+        assert np.array_equal(x, y)
+    assert torch.count_nonzero(dev[len(data):]) == 0  # the caller's bytes are untouched
+    job = native.Job(ctx)
+    try:
+        with pytest.raises(native.MetapartError):
+            job.load_device_inplace(dev.data_ptr() + 1, len(data) - 1)  # not 16-byte aligned
+    finally:
+        job.close()
