@@ -15,6 +15,7 @@
 #include <cstdlib>
 #include <cstdio>
 #include <mutex>
+#include <string>
 #include <vector>
 
 #include "k_sort.cuh"
@@ -96,17 +97,21 @@ __device__ __forceinline__ uint32_t digit_of(uint64_t lo, uint32_t hi, int shift
     return (uint32_t)((((lo >> 8) | ((uint64_t)hi << 56)) >> shift) & 0xFF);
 }
 
-template <int SRC>
+// W: ballots per tuple in the ranking, at least the digit's width w (digits are masked to w bits, so
+// the planes above w are zero in every lane and filter nothing).
+template <int SRC, int W = 8>
 __global__ void __launch_bounds__(ST, 3) k_onesweep(const uint64_t *__restrict__ in_lo, const uint8_t *__restrict__ in_hi,
                                                     const uint32_t *__restrict__ in_id, uint64_t *__restrict__ out_lo,
                                                     uint8_t *__restrict__ out_hi, uint32_t *__restrict__ out_id, uint64_t n,
-                                                    int shift, const uint64_t *__restrict__ dbase,
-                                                    unsigned long long *status, uint32_t *tile_ctr, uint32_t epoch,
-                                                    uint32_t *err, uint32_t pf_tiles, unsigned long long *trace)
+                                                    int shift, int w, const uint64_t *__restrict__ dbase,
+                                                    const uint32_t *__restrict__ nzmask, unsigned long long *status,
+                                                    uint32_t *tile_ctr, uint32_t epoch, uint32_t *err, uint32_t pf_tiles,
+                                                    unsigned long long *trace)
 {
     extern __shared__ __align__(16) unsigned char smraw[];
     SortSmem &sm = *reinterpret_cast<SortSmem *>(smraw);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t dmask = (1u << w) - 1;
     long long ts[5];  // thread 0's clock at the phase boundaries (trace only)
     ts[0] = clock64();
     for (int i = threadIdx.x; i < SW * 256; i += ST) (&sm.whist[0][0])[i] = 0;
@@ -138,10 +143,10 @@ __global__ void __launch_bounds__(ST, 3) k_onesweep(const uint64_t *__restrict__
         key[j] = v ? in_lo[idx] : 0ull;
         const uint32_t h = (has_hi && v) ? (uint32_t)in_hi[idx] : 0u;
         hv[j >> 2] |= h << (8 * (j & 3));
-        rd[j] = (v ? digit_of<SRC>(key[j], h, shift) : 256u) << 16;
+        rd[j] = (v ? digit_of<SRC>(key[j], h, shift) & dmask : 256u) << 16;
     }
     // warp-level multi-split: stable rank of each tuple among equal digits of its warp.  First every
-    // tuple's peers (the lanes holding its digit, from eight bit-plane ballots), packed into rd as the
+    // tuple's peers (the lanes holding its digit, from W bit-plane ballots), packed into rd as the
     // peers below its lane (bits 0-4), their number (5-10) and whether it leads them (11); no memory
     // is touched, so the ballots of all tuples issue back to back.  Then one read-modify-write of the
     // warp's running digit count per tuple.
@@ -151,7 +156,7 @@ __global__ void __launch_bounds__(ST, 3) k_onesweep(const uint64_t *__restrict__
         const uint32_t d = rd[j] >> 16;
         uint32_t peers = __ballot_sync(FULLM, d < 256);
 #pragma unroll
-        for (int b = 0; b < 8; b++) {
+        for (int b = 0; b < W; b++) {
             const uint32_t bb = __ballot_sync(FULLM, (d >> b) & 1u);
             peers &= ((d >> b) & 1u) ? bb : ~bb;
         }
@@ -177,9 +182,11 @@ __global__ void __launch_bounds__(ST, 3) k_onesweep(const uint64_t *__restrict__
     }
     __syncthreads();
     ts[2] = clock64();
-    // threads 0..255 own one digit each: warp prefixes, the tile count, its look-back
+    // threads 0..255 own one digit each: warp prefixes, the tile count, its look-back (skipped, with the
+    // status word, for a digit that no tuple of the input has: bit clear in nzmask)
     const uint32_t d = threadIdx.x;
     const bool dig = d < 256;
+    const bool walk = dig && (!nzmask || ((nzmask[d >> 5] >> (d & 31)) & 1u));
     uint32_t cnt = 0, x = 0;
     if (dig) {
 #pragma unroll
@@ -189,7 +196,7 @@ __global__ void __launch_bounds__(ST, 3) k_onesweep(const uint64_t *__restrict__
             cnt += t;
         }
         const unsigned long long E = (unsigned long long)epoch << 60, PF = 1ull << 59;
-        st_relaxed(status + tile * 256 + d, tile == 0 ? (E | PF | cnt) : (E | cnt));
+        if (walk) st_relaxed(status + tile * 256 + d, tile == 0 ? (E | PF | cnt) : (E | cnt));
         // tile-local exclusive scan of the digit counts (warps 0..7 are all digit owners)
         x = cnt;
 #pragma unroll
@@ -220,7 +227,7 @@ __global__ void __launch_bounds__(ST, 3) k_onesweep(const uint64_t *__restrict__
         }
     }
     uint32_t lb_steps = 0, lb_waits = 0;  // thread 0's look-back: status words summed, polls that found none posted
-    if (dig) {
+    if (walk) {
         // decoupled look-back for digit d
         const unsigned long long E = (unsigned long long)epoch << 60, PF = 1ull << 59, CM = PF - 1;
         unsigned long long excl = 0;
@@ -269,7 +276,7 @@ __global__ void __launch_bounds__(ST, 3) k_onesweep(const uint64_t *__restrict__
     const uint32_t nv = sm.nvalid;
     for (uint32_t s = threadIdx.x; s < nv; s += ST) {
         const uint64_t kk = sm.keys[s];
-        const uint32_t dd = digit_of<SRC>(kk, has_hi ? sm.his[s] : 0u, shift);
+        const uint32_t dd = digit_of<SRC>(kk, has_hi ? sm.his[s] : 0u, shift) & dmask;
         const uint64_t g = sm.gbase[dd] + (s - sm.tstart[dd]);
         if (g >= n) continue;  // only after a failed look-back (err is set)
         out_lo[g] = kk;
@@ -344,11 +351,11 @@ int radix_sort(SortBufs &b, uint64_t n, bool has_hi, DeviceArena &arena, cudaStr
         uint8_t *oh = has_hi ? b.hi[dst] : nullptr;
         if (dgt < 8)
             (mp::count_launch(), k_onesweep<0><<<(unsigned)tiles, ST, sizeof(SortSmem), st>>>(b.lo[src], ih, b.id[src], b.lo[dst], oh,
-                                                                         b.id[dst], n, 8 * dgt, dbase + dgt * 256, status,
+                                                                         b.id[dst], n, 8 * dgt, 8, dbase + dgt * 256, nullptr, status,
                                                                          ctr + pi, (uint32_t)(pi + 1), err, pf, nullptr));
         else
             (mp::count_launch(), k_onesweep<1><<<(unsigned)tiles, ST, sizeof(SortSmem), st>>>(b.lo[src], ih, b.id[src], b.lo[dst], oh,
-                                                                         b.id[dst], n, 0, dbase + dgt * 256, status,
+                                                                         b.id[dst], n, 0, 8, dbase + dgt * 256, nullptr, status,
                                                                          ctr + pi, (uint32_t)(pi + 1), err, pf, nullptr));
         cudaEventRecord(ev[pi + 1], st);
         b.cur = dst;
@@ -618,9 +625,15 @@ __global__ void k_big_scatter(const uint64_t *__restrict__ bstart, const uint32_
 // ---- planning of one scan's bucket sort on the device, from the .kmerHist prefix (d_hist, 1048577 u64)
 
 
-// Digit counts of the three bucket bytes (weighted by the bucket counts) and the populated-bucket flags.
-__global__ void k_bp_count(const uint64_t *__restrict__ hist, uint64_t lo, uint64_t nbk, unsigned long long *dcnt,
-                           uint32_t *pop)
+// The bucket-digit passes of one scan: pass p sorts by the bucket bits [sh[p], sh[p] + w[p]), w <= 8.
+struct BucketPasses {
+    int np;
+    int sh[3], w[3];
+};
+
+// Digit counts of the passes (weighted by the bucket counts) and the populated-bucket flags.
+__global__ void k_bp_count(const uint64_t *__restrict__ hist, uint64_t lo, uint64_t nbk, BucketPasses bp,
+                           unsigned long long *dcnt, uint32_t *pop)
 {
     __shared__ unsigned long long h[3 * 256];
     for (int i = threadIdx.x; i < 3 * 256; i += blockDim.x) h[i] = 0;
@@ -630,33 +643,44 @@ __global__ void k_bp_count(const uint64_t *__restrict__ hist, uint64_t lo, uint6
         pop[i] = c ? 1u : 0u;
         if (!c) continue;
 #pragma unroll
-        for (int d = 0; d < 3; d++) atomicAdd(&h[d * 256 + ((b >> (8 * d)) & 0xFF)], (unsigned long long)c);
+        for (int p = 0; p < 3; p++)
+            if (p < bp.np) atomicAdd(&h[p * 256 + ((b >> bp.sh[p]) & ((1u << bp.w[p]) - 1))], (unsigned long long)c);
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < 3 * 256; i += blockDim.x)
+    for (int i = threadIdx.x; i < bp.np * 256; i += blockDim.x)
         if (h[i]) atomicAdd(&dcnt[i], h[i]);
 }
 
-// Exclusive digit offsets; konst[d] = 1 when digit d takes one value for all n tuples.  One block of 256.
-__global__ void k_bp_digits(const unsigned long long *dcnt, uint64_t n, uint64_t *dbase, uint32_t *konst)
+// Per pass (one block of 256): exclusive digit offsets, the mask of digits that occur, the largest
+// digit count (a digit holding every tuple is constant: no pass) and the total.
+__global__ void __launch_bounds__(256) k_bp_digits(const unsigned long long *dcnt, uint64_t *dbase, uint32_t *dnz,
+                                                   unsigned long long *dmax, unsigned long long *dtot)
 {
     __shared__ unsigned long long ws[8];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (int d = 0; d < 3; d++) {
-        const unsigned long long c = dcnt[d * 256 + threadIdx.x];
-        unsigned long long x = c;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, p = blockIdx.x;
+    const unsigned long long c = dcnt[p * 256 + threadIdx.x];
+    unsigned long long x = c, m = c;
 #pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const unsigned long long y = __shfl_up_sync(FULLM, x, o);
-            if (lane >= o) x += y;
-        }
-        if (lane == 31) ws[warp] = x;
-        __syncthreads();
-        unsigned long long before = 0;
-        for (int w = 0; w < warp; w++) before += ws[w];
-        dbase[d * 256 + threadIdx.x] = before + x - c;
-        const int one = __syncthreads_or(c == n);  // also keeps ws intact until every warp has read it
-        if (threadIdx.x == 0) konst[d] = (uint32_t)one;
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned long long y = __shfl_up_sync(FULLM, x, o);
+        if (lane >= o) x += y;
+        m = max(m, __shfl_xor_sync(FULLM, m, o));
+    }
+    const uint32_t nzw = __ballot_sync(FULLM, c != 0);
+    if (lane == 0) dnz[p * 8 + warp] = nzw;
+    if (lane == 31) ws[warp] = x;
+    __syncthreads();
+    unsigned long long before = 0;
+    for (int q = 0; q < warp; q++) before += ws[q];
+    dbase[p * 256 + threadIdx.x] = before + x - c;
+    if (threadIdx.x == 255) dtot[p] = before + x;
+    __syncthreads();
+    if (lane == 0) ws[warp] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long mm = 0;
+        for (int q = 0; q < 8; q++) mm = max(mm, ws[q]);
+        dmax[p] = mm;
     }
 }
 
@@ -740,6 +764,14 @@ static int unit_sort_max_bits()
     return v < 5 ? 5 : (v > SS_MAXBITS ? SS_MAXBITS : v);
 }
 
+// MP_SORT_BUCKET_DIGITS=bytes: the bucket sort's digit passes take the bucket's bytes (three passes
+// over a 20-bit bucket) instead of the scan's varying bits in passes of near-equal width.
+static bool byte_bucket_digits()
+{
+    const char *e = getenv("MP_SORT_BUCKET_DIGITS");
+    return e && std::string(e) == "bytes";
+}
+
 static int sm_count()
 {
     int dev = 0, n = 0;
@@ -767,7 +799,10 @@ static void sort_kernel_attrs()
     std::call_once(once[dev & 63], [] {
         cudaFuncSetAttribute(k_onesweep<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SortSmem));
         cudaFuncSetAttribute(k_onesweep<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SortSmem));
-        cudaFuncSetAttribute(k_onesweep<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SortSmem));
+        cudaFuncSetAttribute(k_onesweep<2, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SortSmem));
+        cudaFuncSetAttribute(k_onesweep<2, 7>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SortSmem));
+        cudaFuncSetAttribute(k_onesweep<2, 6>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SortSmem));
+        cudaFuncSetAttribute(k_onesweep<2, 5>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SortSmem));
         cudaFuncSetAttribute(k_segsort, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SegSmem));
     });
 }
@@ -781,33 +816,53 @@ int bucket_sort(SortBufs &b, uint64_t n, bool has_hi, int k, const uint64_t *d_h
     if (scan_hi <= scan_lo) return set_error(MP_EFMT, "the histogram does not match the scan's tuples");
     const int bsh = 2 * (k - 10), lowbits = 2 * (k - 10) + 8;
     const uint64_t nbk = scan_hi - scan_lo;
-    // ---- plan on the device: digit offsets of the bucket bytes, populated buckets
-    unsigned long long *dcnt = arena.alloc<unsigned long long>(3 * 256);
+    // ---- plan on the device: digit offsets of the passes, populated buckets.  The scan's varying bucket
+    // bits (those of scan_lo ^ (scan_hi - 1)) are split into the fewest passes of at most 8 bits, of
+    // near-equal widths (19 bits: 7 + 6 + 6), so no pass ranks or looks back over digits that cannot occur;
+    // MP_SORT_BUCKET_DIGITS=bytes takes the bucket's bytes instead.
+    BucketPasses bpl{};
+    {
+        int vb = 0;
+        for (uint64_t v = scan_lo ^ (scan_hi - 1); v; v >>= 1) vb++;
+        if (byte_bucket_digits()) {
+            bpl.np = 3;
+            for (int p = 0; p < 3; p++) bpl.sh[p] = 8 * p, bpl.w[p] = 8;
+        } else {
+            bpl.np = vb ? (vb + 7) / 8 : 1;
+            const int wb = vb / bpl.np, extra = vb % bpl.np;
+            for (int p = 0, at = 0; p < bpl.np; p++) {
+                bpl.w[p] = wb + (p < extra ? 1 : 0);
+                if (bpl.w[p] < 1) bpl.w[p] = 1;
+                bpl.sh[p] = at;
+                at += bpl.w[p];
+            }
+        }
+    }
+    unsigned long long *dcnt = arena.alloc<unsigned long long>(3 * 256), *dmax = arena.alloc<unsigned long long>(6);
     uint64_t *dbase = arena.alloc<uint64_t>(3 * 256), *tot = arena.alloc<uint64_t>(4), *popoff = arena.alloc<uint64_t>(nbk + 2);
-    uint32_t *konst = arena.alloc<uint32_t>(4), *pop = arena.alloc<uint32_t>(nbk + 1);
+    uint32_t *dnz = arena.alloc<uint32_t>(3 * 8), *pop = arena.alloc<uint32_t>(nbk + 1);
     const size_t tbp = scan_tmp_bytes(nbk + 1);
     void *tmp = arena.alloc<uint8_t>(tbp);
-    if (!dcnt || !dbase || !tot || !popoff || !konst || !pop || !tmp) return set_error(MP_ENOMEM, "device memory for the bucket sort");
+    if (!dcnt || !dmax || !dbase || !tot || !popoff || !dnz || !pop || !tmp)
+        return set_error(MP_ENOMEM, "device memory for the bucket sort");
     MP_CUDA(cudaMemsetAsync(dcnt, 0, 3 * 256 * sizeof(unsigned long long), st));
     MP_CUDA(cudaMemsetAsync(pop + nbk, 0, sizeof(uint32_t), st));
     {
         const unsigned g = (unsigned)std::min<uint64_t>((nbk + 255) / 256, 152u * 8u);
-        (mp::count_launch(), k_bp_count<<<g, 256, 0, st>>>(d_hist, scan_lo, nbk, dcnt, pop));
+        (mp::count_launch(), k_bp_count<<<g, 256, 0, st>>>(d_hist, scan_lo, nbk, bpl, dcnt, pop));
     }
-    (mp::count_launch(), k_bp_digits<<<1, 256, 0, st>>>(dcnt, n, dbase, konst));
+    (mp::count_launch(), k_bp_digits<<<bpl.np, 256, 0, st>>>(dcnt, dbase, dnz, dmax, dmax + 3));
     scan_u32_to_u64(pop, popoff, nbk + 1, tot, tmp, tbp, st);
-    uint64_t hd[3] = {0, 0, 0};  // populated buckets; digit 0's last count and offset
-    uint32_t hk[4] = {0, 0, 0, 0};
-    MP_CUDA(cudaMemcpyAsync(&hd[0], tot, 8, cudaMemcpyDeviceToHost, st));
-    MP_CUDA(cudaMemcpyAsync(&hd[1], dcnt + 255, 8, cudaMemcpyDeviceToHost, st));
-    MP_CUDA(cudaMemcpyAsync(&hd[2], dbase + 255, 8, cudaMemcpyDeviceToHost, st));
-    MP_CUDA(cudaMemcpyAsync(hk, konst, 3 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    uint64_t hd = 0;                   // populated buckets
+    unsigned long long hm[6] = {};     // per pass: largest digit count, then the totals
+    MP_CUDA(cudaMemcpyAsync(&hd, tot, 8, cudaMemcpyDeviceToHost, st));
+    MP_CUDA(cudaMemcpyAsync(hm, dmax, sizeof hm, cudaMemcpyDeviceToHost, st));
     MP_CUDA(cudaStreamSynchronize(st));
-    if (hd[1] + hd[2] != n) return set_error(MP_EFMT, "the histogram does not match the scan's tuples");
-    const uint64_t np = hd[0];
+    if (hm[3] != n) return set_error(MP_EFMT, "the histogram does not match the scan's tuples");
+    const uint64_t np = hd;
     std::vector<int> passes;
-    for (int d = 0; d < 3; d++)
-        if (!hk[d]) passes.push_back(d);
+    for (int d = 0; d < bpl.np; d++)
+        if (hm[d] != n) passes.push_back(d);
     const uint64_t tiles = (n + STILE - 1) / STILE;
     uint32_t *ctr = arena.alloc<uint32_t>(8), *err = arena.alloc<uint32_t>(1);
     unsigned long long *trace = arena.alloc<unsigned long long>(16);  // [0..3] unit sort, [8..12] digit passes
@@ -825,9 +880,12 @@ int bucket_sort(SortBufs &b, uint64_t n, bool has_hi, int k, const uint64_t *d_h
     for (size_t pi = 0; pi < passes.size(); pi++) {
         const int d = passes[pi];
         const int src = b.cur, dst = b.cur ^ 1;
-        (mp::count_launch(), k_onesweep<2><<<(unsigned)tiles, ST, sizeof(SortSmem), st>>>(
+        const int w = bpl.w[d];
+        auto kern = w >= 8 ? k_onesweep<2, 8> : w == 7 ? k_onesweep<2, 7> : w == 6 ? k_onesweep<2, 6> : k_onesweep<2, 5>;
+        (mp::count_launch(), kern<<<(unsigned)tiles, ST, sizeof(SortSmem), st>>>(
             b.lo[src], has_hi ? b.hi[src] : nullptr, b.id[src], b.lo[dst], has_hi ? b.hi[dst] : nullptr, b.id[dst], n,
-            bsh + 8 * d, dbase + d * 256, status, ctr + pi, (uint32_t)(pi + 1), err, pf, trace + 8));
+            bsh + bpl.sh[d], bpl.w[d], dbase + d * 256, dnz + d * 8, status, ctr + pi, (uint32_t)(pi + 1), err, pf,
+            trace + 8));
         b.cur = dst;
     }
     cudaEventRecord(ev[1], st);
@@ -1048,11 +1106,11 @@ int sort_tuples_noalloc(const uint64_t *lo_in, const uint8_t *hi_in, const uint3
         const int dgt = passes[i];
         if (dgt < 8)
             (mp::count_launch(), k_onesweep<0><<<(unsigned)tiles, ST, sizeof(SortSmem), st>>>(
-                src_lo, src_hi, src_id, d_lo, d_hi, d_id, n, 8 * dgt, S->dbase + dgt * 256, S->status, S->ctr + i,
+                src_lo, src_hi, src_id, d_lo, d_hi, d_id, n, 8 * dgt, 8, S->dbase + dgt * 256, nullptr, S->status, S->ctr + i,
                 (uint32_t)(i + 1), &S->err, 0u, nullptr));
         else
             (mp::count_launch(), k_onesweep<1><<<(unsigned)tiles, ST, sizeof(SortSmem), st>>>(
-                src_lo, src_hi, src_id, d_lo, d_hi, d_id, n, 0, S->dbase + dgt * 256, S->status, S->ctr + i,
+                src_lo, src_hi, src_id, d_lo, d_hi, d_id, n, 0, 8, S->dbase + dgt * 256, nullptr, S->status, S->ctr + i,
                 (uint32_t)(i + 1), &S->err, 0u, nullptr));
         src_lo = d_lo;
         src_hi = d_hi;

@@ -74,3 +74,11 @@ NARROW = [
 @pytest.mark.parametrize("name,n,p", NARROW, ids=[f"{c[0]}-k{c[2].k}" for c in NARROW])
 def test_gpu_unit_sort_digit_width(tmp_path, built_gpu, name, n, p, bits):
     _compare(tmp_path, name, n, p, env_extra={"MP_UNIT_SORT_MAX_BITS": str(bits)})
+
+
+# The bucket's bytes as digits (three passes for a scan over half the bucket range) instead of the wide
+# passes of up to 10 bits that the sort takes by default.
+@pytest.mark.parametrize("name,n,p", NARROW + [CASES[2], CASES[10]],
+                         ids=[f"{c[0]}-k{c[2].k}-s{c[2].scans}" for c in NARROW + [CASES[2], CASES[10]]])
+def test_gpu_byte_bucket_digits(tmp_path, built_gpu, name, n, p):
+    _compare(tmp_path, name, n, p, env_extra={"MP_SORT_BUCKET_DIGITS": "bytes"})
