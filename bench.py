@@ -277,6 +277,7 @@ def main():
     e1.record(stream)
     e1.synchronize()
     dist.barrier()
+    e2e_pieces = job.scan_pieces
     e2e_ms = dist.max(e0.elapsed_time(e1) / args.steps)
     e2e_value = dist.world * bases / (e2e_ms / 1e3)
 
@@ -306,7 +307,8 @@ def main():
                    "chunks": args.chunks, "bases_per_step": bases, "fastq_bytes": nbytes,
                    "l2": "inputs larger than L2 (FASTQ and tuple arrays are GBs)", "parallelism": "replicas"},
         "e2e": {"value": round(e2e_value, 1), "unit": "bases/s", "ms_per_step": round(e2e_ms, 3),
-                "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": int(out_bytes) + 8 * (1 << 20) + 8},
+                "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": int(out_bytes) + 8 * (1 << 20) + 8,
+                "scan_pieces": e2e_pieces},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
                      "kernel": "k_onesweep (radix digit pass)",

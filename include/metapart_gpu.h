@@ -222,6 +222,18 @@ void mp_server_destroy(mp_server *s);
  * separate processes. */
 int mp_job_set_kmer_cache(mp_job *job, int enable);
 
+/* Most tuples one scan of mp_job_partition holds in HBM at once (0, the default: what the context's
+ * budget, or the device, has left at about 32 bytes per tuple; the environment variable
+ * MP_SCAN_PIECE_TUPLES overrides both).  A scan of the plain variant with more tuples runs in pieces of
+ * consecutive m-mer buckets, swept twice (sort and mischief filter of every piece, then sort and union of
+ * every piece), with the same results as the whole scan at once.  The reference has no counterpart: its
+ * scans are what bounds its memory (numScans, metapart.c:3720-3791), and a different numScans changes
+ * the partitions; pieces inside a scan do not. */
+int mp_job_set_scan_piece_tuples(mp_job *job, uint64_t max_tuples);
+/* Bucket-range pieces the last mp_job_partition ran its scans in, summed over the scans (numScans when
+ * no scan was split).  Tracing only. */
+int mp_job_scan_pieces(const mp_job *job);
+
 /* Optional stage dumps in the reference's formats (the files oracle/ref_hooks.c writes),
  * for parity testing.  NULL disables. */
 int mp_job_set_dump_dir(mp_job *job, const char *dir);

@@ -704,6 +704,51 @@ int union_scan(Tuples &tp, const std::vector<uint64_t> &range_bounds, uint32_t *
     return 0;
 }
 
+int union_piece(Tuples &tp, const std::vector<uint64_t> &bounds, const std::vector<uint8_t> &seen, uint64_t init_kmer,
+                uint32_t init_min, bool init_min_ok, uint32_t *parent, const uint8_t *filtered, DeviceArena &arena,
+                cudaStream_t st, std::vector<uint8_t> &has_valid)
+{
+    const uint64_t n = tp.n;
+    const int T = (int)bounds.size() - 1;
+    has_valid.assign(T, 0);
+    if (n == 0 || T < 1) return 0;
+    uint32_t *err = arena.alloc<uint32_t>(1);
+    uint64_t *d_bounds = arena.alloc<uint64_t>(T + 1), *first = arena.alloc<uint64_t>(T);
+    if (!err || !d_bounds || !first) return set_error(MP_ENOMEM, "device memory for union-find");
+    MP_CUDA(cudaMemsetAsync(err, 0, sizeof *err, st));
+    MP_CUDA(cudaMemcpyAsync(d_bounds, bounds.data(), (T + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, st));
+    (mp::count_launch(), k_range_first_valid<<<blocks_for(T, 64), 64, 0, st>>>(tp.lo, tp.hi, tp.id, tp.z, d_bounds, T, parent,
+                                                                              first));
+    // a range whose first valid tuple lies in an earlier piece has none here: the quirk is that tuple's alone
+    std::vector<uint64_t> hf(T);
+    MP_CUDA(cudaMemcpyAsync(hf.data(), first, T * sizeof(uint64_t), cudaMemcpyDeviceToHost, st));
+    MP_CUDA(cudaStreamSynchronize(st));
+    for (int t = 0; t < T; t++) {
+        has_valid[t] = hf[t] != ~0ull;
+        if (seen[t]) hf[t] = ~0ull;
+    }
+    MP_CUDA(cudaMemcpyAsync(first, hf.data(), T * sizeof(uint64_t), cudaMemcpyHostToDevice, st));
+    EdgeCtx c;
+    c.lo = tp.lo; c.hi = tp.hi; c.id = tp.id; c.z = tp.z; c.n = n;
+    c.first_valid = first; c.range_bounds = d_bounds; c.T = T; c.parent = parent; c.filtered = filtered; c.err = err;
+    c.init_kmer = init_kmer;
+    c.init_min = init_min;
+    c.init_min_ok = init_min_ok ? 1u : 0u;
+    const uint64_t warps = (n + SEG - 1) / SEG;
+    (mp::count_launch(), k_edges_warp<<<blocks_for(warps * 32, 256), 256, 0, st>>>(c));
+    uint32_t herr = 0;
+    MP_CUDA(cudaMemcpyAsync(&herr, err, sizeof herr, cudaMemcpyDeviceToHost, st));
+    MP_CUDA(cudaStreamSynchronize(st));
+    MP_CUDA(cudaGetLastError());
+    if (herr) return set_error(MP_EDEVICE, "union-find retry limit reached (flags 0x%x)", herr);
+    return 0;
+}
+
+void compress_parents(uint32_t *parent, uint64_t n_reads, cudaStream_t st)
+{
+    (mp::count_launch(), k_compress<<<blocks_for(n_reads, 256), 256, 0, st>>>(parent, n_reads));
+}
+
 int mate_union_and_plan(uint32_t *parent, uint64_t n_reads, uint32_t *size, uint64_t *bounds_out, DeviceArena &arena,
                         cudaStream_t st, int *rounds_out)
 {

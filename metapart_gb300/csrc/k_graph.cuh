@@ -20,6 +20,16 @@ int filter_scan(Tuples &tp, const std::vector<uint64_t> &range_bounds, uint32_t 
 // K5: unionFindPar2 + unionFind + printStats compression for the scan.
 int union_scan(Tuples &tp, const std::vector<uint64_t> &range_bounds, uint32_t *parent, const uint8_t *filtered,
                uint64_t n_reads, DeviceArena &arena, cudaStream_t st);
+// K5 for one piece of a scan split by bucket ranges (the scan's tuples do not fit at once): the sweep of
+// unionFindPar2 over the piece's part of the thread ranges.  bounds: T' + 1 tuple bounds of those parts;
+// seen[t] = 1 when part t's thread range had a valid tuple in an earlier piece; init_*: the scan's initial
+// sweep state (its last tuple's k-mer after the filter, its first tuple's read, whether that read was BAD
+// when the scan's unions began).  On return has_valid[t] = 1 when part t holds a valid tuple.  No
+// compression (compress_parents, once the scan's last piece is done).
+int union_piece(Tuples &tp, const std::vector<uint64_t> &bounds, const std::vector<uint8_t> &seen, uint64_t init_kmer,
+                uint32_t init_min, bool init_min_ok, uint32_t *parent, const uint8_t *filtered, DeviceArena &arena,
+                cudaStream_t st, std::vector<uint8_t> &has_valid);
+void compress_parents(uint32_t *parent, uint64_t n_reads, cudaStream_t st);
 // K6: sizes, unionFindPeReads(1000), final compression and the 17 partition bounds (host).
 int mate_union_and_plan(uint32_t *parent, uint64_t n_reads, uint32_t *size, uint64_t *bounds_out, DeviceArena &arena,
                         cudaStream_t st, int *rounds_out);

@@ -96,6 +96,8 @@ struct mp_job {
     uint64_t units_total = 0, big_buckets_total = 0, big_tuples_total = 0;
     uint64_t unit_passes_total = 0, phase_total[3] = {0, 0, 0}, pass_cycles_total[7] = {};
     int pe_rounds = 0;
+    uint64_t piece_tuples = 0;  // most tuples a scan holds in HBM at once (0: from the free device memory)
+    int pieces_total = 0;       // bucket-range pieces of the last partition, over all scans
 };
 
 // ------------------------------------------------------------------ helpers
@@ -124,9 +126,9 @@ struct StageTimer {
     }
 };
 
-int write_file(const std::string &path, const void *buf, size_t n)
+int write_file(const std::string &path, const void *buf, size_t n, bool append = false)
 {
-    FILE *f = fopen(path.c_str(), "wb");
+    FILE *f = fopen(path.c_str(), append ? "ab" : "wb");
     if (!f) return set_error(MP_EIO, "cannot write %s", path.c_str());
     size_t w = n ? fwrite(buf, 1, n, f) : 0;
     fclose(f);
@@ -134,8 +136,10 @@ int write_file(const std::string &path, const void *buf, size_t n)
     return 0;
 }
 
-// Dump of tuples in the reference's 14-byte record format (enumerateKmers.c:352-365).
-int dump_tuples(mp_job *j, const char *name, const uint64_t *lo, const uint8_t *hi, const uint32_t *id, uint64_t n)
+// Dump of tuples in the reference's 14-byte record format (enumerateKmers.c:352-365); append: after the
+// file's earlier pieces.
+int dump_tuples(mp_job *j, const char *name, const uint64_t *lo, const uint8_t *hi, const uint32_t *id, uint64_t n,
+                bool append = false)
 {
     if (j->dump_dir.empty()) return 0;
     std::vector<uint64_t> hl(n);
@@ -155,7 +159,7 @@ int dump_tuples(mp_job *j, const char *name, const uint64_t *lo, const uint8_t *
         memcpy(&b[i * 14 + 8], &w4, 2);
         memcpy(&b[i * 14 + 10], &hid[i], 4);
     }
-    return write_file(j->dump_dir + "/" + name, b.data(), b.size());
+    return write_file(j->dump_dir + "/" + name, b.data(), b.size(), append);
 }
 
 // Parent (5-byte encoding, BAD = 0xBADBADBAD) and sizes, as printStats leaves them.
@@ -679,6 +683,240 @@ int mp_job_load_count(mp_job *j, const char *bytes, uint64_t nbytes, const uint6
     return rc ? rc : one_by_one();
 }
 
+static void add_sort_stats(mp_job *j, const SortStats &ss, uint64_t n)
+{
+    j->sort_stats = ss;
+    j->sort_passes_total += ss.passes;
+    j->sort_ms_total += ss.pass_ms;
+    j->sort_bytes_total += ss.bytes;
+    j->sort_tuples_total += n;
+    j->seg_ms_total += ss.seg_ms;
+    j->big_ms_total += ss.big_ms;
+    j->units_total += ss.units;
+    j->big_buckets_total += ss.big_buckets;
+    j->big_tuples_total += ss.big_tuples;
+    j->unit_passes_total += ss.unit_passes;
+    for (int q = 0; q < 3; q++) j->phase_total[q] += ss.phase_cycles[q];
+    for (int q = 0; q < 7; q++) j->pass_cycles_total[q] += ss.pass_cycles[q];
+}
+
+// Most tuples one scan may hold in HBM at once: MP_SCAN_PIECE_TUPLES, else the job's setting, else what
+// the context's budget (or the device, counting the pool's cached memory) has left at ~32 B per tuple
+// (two tuple buffers of 13 B, the sort's status and plans, the filter's marks).
+static uint64_t scan_piece_cap(mp_job *j)
+{
+    const char *e = getenv("MP_SCAN_PIECE_TUPLES");
+    if (e && *e) return std::max<uint64_t>(1, strtoull(e, nullptr, 10));
+    if (j->piece_tuples) return j->piece_tuples;
+    size_t fr = 0, tot = 0;
+    uint64_t avail = cudaMemGetInfo(&fr, &tot) == cudaSuccess ? fr : 0;
+    cudaMemPool_t pool;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+        uint64_t rsv = 0, used = 0;
+        if (cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReservedMemCurrent, &rsv) == cudaSuccess &&
+            cudaMemPoolGetAttribute(pool, cudaMemPoolAttrUsedMemCurrent, &used) == cudaSuccess && rsv > used)
+            avail += rsv - used;
+    }
+    cudaGetLastError();
+    if (j->arena.budget_used && j->arena.budget_limit != ~0ull) {
+        const uint64_t u = j->arena.budget_used->load();
+        avail = std::min<uint64_t>(avail, u < j->arena.budget_limit ? j->arena.budget_limit - u : 0);
+    }
+    return std::max<uint64_t>(1, avail / 32);
+}
+
+// Bucket-range pieces of the scan [lo, hi): consecutive buckets while their tuples stay within cap (a bucket
+// above cap ends a piece of its own, with the empty buckets before it).  Returns the piece bounds, lo first
+// and hi last.
+static std::vector<uint64_t> plan_pieces(const uint64_t *hist, uint64_t lo, uint64_t hi, uint64_t cap)
+{
+    std::vector<uint64_t> b{lo};
+    uint64_t start = lo;
+    for (uint64_t x = lo + 1; x < hi; x++)
+        if (hist[x + 1] - hist[start] > cap && hist[x] > hist[start]) {
+            b.push_back(x);
+            start = x;
+        }
+    b.push_back(hi);
+    return b;
+}
+
+// One scan whose tuples do not fit HBM at once, in bucket-range pieces (the sorted scan is the pieces'
+// sorted tuples one after the other).  Inside a scan every BAD mark is final before the first union
+// (metapart.c:3961-3964), so the pieces are swept twice: enumerate, sort and filter each (its zero marks
+// kept), then enumerate and sort each again and run its unions.  The enumeration of scans after the first
+// carries each read's root as the scan began (SCAN_OPT, metapart.c:543-568), from a copy of the parents
+// taken before the first sweep.  A thread range's last run is exempt from the filter only where the range
+// ends, and each range's sweep starts from the scan's own initial state (metapart.c:2539-2548), however
+// the pieces cut it.
+static int scan_in_pieces(mp_job *j, int s, int k, bool has_hi, uint64_t lo, uint64_t hi, const std::vector<uint64_t> &pcs,
+                          const std::vector<uint64_t> &rb, const uint64_t *hist, const uint64_t *d_hist, bool use_kc,
+                          uint32_t *err)
+{
+    const uint64_t N = j->pr.n_reads, scan0 = hist[lo];
+    const int P = (int)pcs.size() - 1, T = (int)rb.size() - 1;
+    int rc = 0;
+    char name[64];
+    uint64_t maxn = 0;
+    for (int i = 0; i < P; i++) maxn = std::max<uint64_t>(maxn, hist[pcs[i + 1]] - hist[pcs[i]]);
+    uint32_t *roots = nullptr;
+    if (s) {
+        roots = j->arena.alloc<uint32_t>(N + 1);
+        if (!roots) return set_error(MP_ENOMEM, "device memory for the scan's roots");
+        MP_CUDA(cudaMemcpyAsync(roots, j->d_parent, (N + 1) * 4, cudaMemcpyDeviceToDevice, j->st));
+    }
+    uint32_t *cnt = j->arena.alloc<uint32_t>(N + 1), *d_b = j->arena.alloc<uint32_t>(2 * P);
+    uint64_t *off = j->arena.alloc<uint64_t>(N + 2), *ntot = j->arena.alloc<uint64_t>(1);
+    const size_t tb = scan_tmp_bytes(N + 1);
+    void *tmp = j->arena.alloc<uint8_t>(tb);
+    SortBufs sb0;
+    for (int b = 0; b < 2; b++) {
+        sb0.lo[b] = j->arena.alloc<uint64_t>(maxn + 1);
+        sb0.id[b] = j->arena.alloc<uint32_t>(maxn + 1);
+        sb0.hi[b] = has_hi ? j->arena.alloc<uint8_t>(maxn + 1) : nullptr;
+        if (!sb0.lo[b] || !sb0.id[b] || (has_hi && !sb0.hi[b]))
+            return set_error(MP_ENOMEM, "device memory for %llu tuples", (unsigned long long)maxn);
+    }
+    if (!cnt || !d_b || !off || !ntot || !tmp) return set_error(MP_ENOMEM, "device memory for enumeration offsets");
+    {
+        std::vector<uint32_t> hb(2 * P);
+        for (int i = 0; i < P; i++) hb[2 * i] = (uint32_t)pcs[i], hb[2 * i + 1] = (uint32_t)pcs[i + 1];
+        MP_CUDA(cudaMemcpyAsync(d_b, hb.data(), hb.size() * 4, cudaMemcpyHostToDevice, j->st));
+    }
+    // piece i's tuples in enumeration order into sb0.*[0], then sorted; tp views the sorted piece
+    auto piece_tuples = [&](int i, Tuples &tp) -> int {
+        const uint64_t b0 = pcs[i], b1 = pcs[i + 1], expect = hist[b1] - hist[b0];
+        SortBufs sb = sb0;
+        uint64_t n = 0;
+        {
+            StageTimer tm(j->st, &j->stage_ms[2]);
+            int lrc = 0;
+            if (use_kc)
+                for (const KcPiece &q : j->kc)
+                    lrc |= q.n ? launch_kc_count_scans(q.off, q.lo, q.hi, q.n, k, d_b + 2 * i, 1, cnt + q.r0, N + 1, err, j->st) : 0;
+            else
+                launch_enum_count(j->d_fq, j->pr, k, 0, (uint32_t)b0, (uint32_t)b1, cnt, err, j->st);
+            if (lrc) return set_error(MP_EARG, "enumeration count of a scan piece");
+            MP_CUDA(cudaMemsetAsync(cnt + N, 0, 4, j->st));
+            scan_u32_to_u64(cnt, off, N + 1, ntot, tmp, tb, j->st);
+            MP_CUDA(cudaMemcpyAsync(&n, ntot, 8, cudaMemcpyDeviceToHost, j->st));
+            MP_CUDA(cudaStreamSynchronize(j->st));
+            if (n != expect)
+                return set_error(MP_EFMT, "scan %d piece %d: %llu tuples but the histogram holds %llu", s, i,
+                                 (unsigned long long)n, (unsigned long long)expect);
+            if (use_kc)
+                for (const KcPiece &q : j->kc)
+                    launch_kc_write(q.off, q.lo, q.hi, q.r0, q.n, k, (uint32_t)b0, (uint32_t)b1, roots, off, sb.lo[0],
+                                    sb.hi[0], sb.id[0], j->st);
+            else
+                launch_enum_write(j->d_fq, j->pr, k, 0, (uint32_t)b0, (uint32_t)b1, roots, off, sb.lo[0], sb.hi[0],
+                                  sb.id[0], err, j->st);
+        }
+        uint32_t herr = 0;
+        MP_CUDA(cudaMemcpyAsync(&herr, err, 4, cudaMemcpyDeviceToHost, j->st));
+        MP_CUDA(cudaStreamSynchronize(j->st));
+        if (herr) return set_error(MP_EDEVICE, "enumeration flags 0x%x", herr);
+        int lo_buf = 0, hi_buf = 0;
+        {
+            StageTimer tm(j->st, &j->stage_ms[3]);
+            SortStats ss;
+            int r = bucket_sort(sb, n, has_hi, k, d_hist, b0, b1, j->arena, j->st, &ss, &lo_buf, &hi_buf);
+            if (r) return r;
+            add_sort_stats(j, ss, n);
+        }
+        tp = Tuples{};
+        tp.lo = sb.lo[lo_buf];
+        tp.hi = has_hi ? sb.hi[hi_buf] : nullptr;
+        tp.id = sb.id[lo_buf];
+        tp.n = n;
+        return 0;
+    };
+    // ---- sweep 1: the filter over every piece
+    std::vector<uint32_t *> zs(P);
+    uint32_t first_id = 0;
+    uint64_t last_kmer = 0;
+    bool have_first = false;
+    for (int i = 0; i < P; i++) {
+        Tuples tp;
+        if ((rc = piece_tuples(i, tp))) return rc;
+        const uint64_t p0 = hist[pcs[i]] - scan0, p1 = hist[pcs[i + 1]] - scan0;
+        snprintf(name, sizeof name, "scan%d_sorted.bin", s);
+        if ((rc = dump_tuples(j, name, tp.lo, tp.hi, tp.id, tp.n, i > 0))) return rc;
+        std::vector<uint64_t> ends{0};  // the thread ranges ending inside the piece or at its end
+        for (int t = 1; t <= T; t++)
+            if (rb[t] > p0 && rb[t] <= p1) ends.push_back(rb[t] - p0);
+        {
+            StageTimer tm(j->st, &j->stage_ms[4]);
+            if ((rc = filter_scan(tp, ends, j->d_parent, j->d_filtered, j->arena, j->st, !j->dump_dir.empty()))) return rc;
+        }
+        zs[i] = tp.z;
+        snprintf(name, sizeof name, "scan%d_filtered.bin", s);
+        if ((rc = dump_tuples(j, name, tp.lo, tp.hi, tp.id, tp.n, i > 0))) return rc;
+        if (tp.n && !have_first) {  // the scan's first tuple
+            MP_CUDA(cudaMemcpyAsync(&first_id, tp.id, 4, cudaMemcpyDeviceToHost, j->st));
+            have_first = true;
+        }
+        if (tp.n) {  // the scan's last tuple, once the last piece that holds one is done
+            uint64_t l = 0;
+            uint8_t h = 0;
+            uint32_t zw = 0;
+            MP_CUDA(cudaMemcpyAsync(&l, tp.lo + (tp.n - 1), 8, cudaMemcpyDeviceToHost, j->st));
+            if (tp.hi) MP_CUDA(cudaMemcpyAsync(&h, tp.hi + (tp.n - 1), 1, cudaMemcpyDeviceToHost, j->st));
+            MP_CUDA(cudaMemcpyAsync(&zw, tp.z + ((tp.n - 1) >> 5), 4, cudaMemcpyDeviceToHost, j->st));
+            MP_CUDA(cudaStreamSynchronize(j->st));
+            last_kmer = ((zw >> ((tp.n - 1) & 31)) & 1u) ? 0 : ((l >> 8) | ((uint64_t)h << 56));
+        }
+        MP_CUDA(cudaStreamSynchronize(j->st));
+    }
+    if (!j->dump_dir.empty()) {
+        std::vector<uint8_t> f(N);
+        MP_CUDA(cudaMemcpyAsync(f.data(), j->d_filtered, N, cudaMemcpyDeviceToHost, j->st));
+        MP_CUDA(cudaStreamSynchronize(j->st));
+        snprintf(name, sizeof name, "scan%d_bad.bin", s);
+        if ((rc = write_file(j->dump_dir + "/" + name, f.data(), N))) return rc;
+    }
+    // ---- sweep 2: the unions, piece by piece, from the scan's initial state
+    uint32_t first_parent = 0;
+    MP_CUDA(cudaMemcpyAsync(&first_parent, j->d_parent + first_id, 4, cudaMemcpyDeviceToHost, j->st));
+    MP_CUDA(cudaStreamSynchronize(j->st));
+    std::vector<uint8_t> seen(T, 0);
+    for (int i = 0; i < P; i++) {
+        Tuples tp;
+        if ((rc = piece_tuples(i, tp))) return rc;
+        tp.z = zs[i];
+        const uint64_t p0 = hist[pcs[i]] - scan0, p1 = hist[pcs[i + 1]] - scan0;
+        std::vector<uint64_t> bounds;  // the piece's parts of the thread ranges, and which range each is
+        std::vector<int> which;
+        for (int t = 0; t < T; t++) {
+            const uint64_t a = std::max(rb[t], p0), b = std::min(rb[t + 1], p1);
+            if (a < b) {
+                bounds.push_back(a - p0);
+                which.push_back(t);
+            }
+        }
+        bounds.push_back(p1 - p0);
+        std::vector<uint8_t> part_seen(which.size()), has_valid;
+        for (size_t q = 0; q < which.size(); q++) part_seen[q] = seen[which[q]];
+        {
+            StageTimer tm(j->st, &j->stage_ms[5]);
+            if ((rc = union_piece(tp, bounds, part_seen, last_kmer, first_id, first_parent != BAD, j->d_parent,
+                                  j->d_filtered, j->arena, j->st, has_valid)))
+                return rc;
+        }
+        for (size_t q = 0; q < which.size(); q++) seen[which[q]] |= has_valid[q];
+    }
+    {
+        StageTimer tm(j->st, &j->stage_ms[5]);
+        compress_parents(j->d_parent, N, j->st);
+        MP_CUDA(cudaStreamSynchronize(j->st));
+        MP_CUDA(cudaGetLastError());
+    }
+    j->pieces_total += P;
+    return 0;
+}
+
 int mp_job_partition(mp_job *j, const mp_part_params *p, const uint64_t *chunk_starts, const uint64_t *chunk_first_read,
                      int nchunks, const uint64_t *hist, uint64_t *bounds_out)
 {
@@ -766,9 +1004,37 @@ int mp_job_partition(mp_job *j, const mp_part_params *p, const uint64_t *chunk_s
             for (int s = 0; s < S; s++) MP_CUDA(cudaMemsetAsync(cnt_all + (size_t)s * (N + 1) + N, 0, 4, j->st));
         }
     }
+    j->pieces_total = 0;
+    const uint64_t piece_cap = p->min3 ? ~0ull : scan_piece_cap(j);  // the 3-minimizer choice depends on the range
     for (int s = 0; s < S; s++) {
         const uint64_t lo = scanR[s], hi = scanR[s + 1];
         const uint64_t expect = hist[hi] - hist[lo];
+        if (expect > piece_cap) {
+            const std::vector<uint64_t> pcs = plan_pieces(hist, lo, hi, piece_cap);
+            if (pcs.size() > 2) {
+                {  // the per-read checks of the whole scan (its counts, when the pass over all scans did not make them)
+                    uint32_t cerr = 0, *c1 = cnt_all ? nullptr : j->arena.alloc<uint32_t>(N + 1);
+                    if (!cnt_all && !c1) return set_error(MP_ENOMEM, "device memory for enumeration counts");
+                    if (c1) launch_enum_count(j->d_fq, j->pr, k, 0, (uint32_t)lo, (uint32_t)hi, c1, err, j->st);
+                    MP_CUDA(cudaMemcpyAsync(&cerr, err, 4, cudaMemcpyDeviceToHost, j->st));
+                    MP_CUDA(cudaStreamSynchronize(j->st));
+                    j->arena.free_scratch(c1);
+                    if (cerr & DERR_LONG_READ) return set_error(MP_EUNSUP, "a read has 300 or more k-mer positions");
+                    if (cerr & DERR_TOO_MANY)
+                        return set_error(MP_EUNSUP, "a read has 256 or more k-mers in scan %d (the reference counts "
+                                                    "them in 8 bits, enumerateKmers.c:152)", s);
+                    if (cerr) return set_error(MP_EDEVICE, "enumeration flags 0x%x", cerr);
+                }
+                std::vector<uint64_t> rb;
+                if ((rc = range_bounds(hist, thrR.data() + (size_t)s * T, T, lo, hi, rb))) return rc;
+                if ((rc = scan_in_pieces(j, s, k, has_hi, lo, hi, pcs, rb, hist, d_hist, use_kc, err))) return rc;
+                j->arena.release_scratch();
+                snprintf(name, sizeof name, "stats%d_parent.bin", s);
+                if ((rc = dump_state(j, name, nullptr))) return rc;
+                continue;
+            }
+        }
+        j->pieces_total += 1;
         uint32_t *cnt = cnt_all ? cnt_all + (size_t)s * (N + 1) : j->arena.alloc<uint32_t>(N + 1);
         uint64_t *off = j->arena.alloc<uint64_t>(N + 2), *ntot = j->arena.alloc<uint64_t>(1);
         size_t tb = scan_tmp_bytes(N + 1);
@@ -824,19 +1090,7 @@ int mp_job_partition(mp_job *j, const mp_part_params *p, const uint64_t *chunk_s
             StageTimer tm(j->st, &j->stage_ms[3]);
             SortStats ss;
             if ((rc = bucket_sort(sb, n, has_hi, k, d_hist, lo, hi, j->arena, j->st, &ss, &lo_buf, &hi_buf))) return rc;
-            j->sort_stats = ss;
-            j->sort_passes_total += ss.passes;
-            j->sort_ms_total += ss.pass_ms;
-            j->sort_bytes_total += ss.bytes;
-            j->sort_tuples_total += n;
-            j->seg_ms_total += ss.seg_ms;
-            j->big_ms_total += ss.big_ms;
-            j->units_total += ss.units;
-            j->big_buckets_total += ss.big_buckets;
-            j->big_tuples_total += ss.big_tuples;
-            j->unit_passes_total += ss.unit_passes;
-            for (int q = 0; q < 3; q++) j->phase_total[q] += ss.phase_cycles[q];
-            for (int q = 0; q < 7; q++) j->pass_cycles_total[q] += ss.pass_cycles[q];
+            add_sort_stats(j, ss, n);
         }
         Tuples tp;
         tp.lo = sb.lo[lo_buf];
@@ -1018,6 +1272,15 @@ int mp_job_set_kmer_cache(mp_job *j, int enable)
     if (!j->kc_on) drop_kmer_cache(j);
     return 0;
 }
+
+int mp_job_set_scan_piece_tuples(mp_job *j, uint64_t max_tuples)
+{
+    if (!j) return set_error(MP_EARG, "null job");
+    j->piece_tuples = max_tuples;
+    return 0;
+}
+
+int mp_job_scan_pieces(const mp_job *j) { return j ? j->pieces_total : 0; }
 
 int mp_job_set_dump_dir(mp_job *j, const char *dir)
 {

@@ -61,6 +61,8 @@ def lib():
         L.mp_job_output_device.argtypes = [C.c_void_p, C.POINTER(C.c_void_p), u64p, u64p]
         L.mp_job_set_dump_dir.argtypes = [C.c_void_p, C.c_char_p]
         L.mp_job_set_kmer_cache.argtypes = [C.c_void_p, C.c_int]
+        L.mp_job_set_scan_piece_tuples.argtypes = [C.c_void_p, C.c_uint64]
+        L.mp_job_scan_pieces.argtypes = [C.c_void_p]
         L.mp_job_stage_ms.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.c_int]
         L.mp_job_sort_stats.argtypes = [C.c_void_p, u64p, C.POINTER(C.c_int), C.POINTER(C.c_double), u64p]
         L.mp_job_sort_split.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double),
@@ -207,6 +209,16 @@ class Job:
         """Keep the count pass's k-mers for the next partition of the same k (default on)."""
         _check(lib().mp_job_set_kmer_cache(self.h, int(enable)), "set_kmer_cache")
 
+    def set_scan_piece_tuples(self, max_tuples: int):
+        """Most tuples a scan holds in HBM at once (0: from the free device memory); a larger scan runs in
+        bucket-range pieces with the same results."""
+        _check(lib().mp_job_set_scan_piece_tuples(self.h, int(max_tuples)), "set_scan_piece_tuples")
+
+    @property
+    def scan_pieces(self) -> int:
+        """Bucket-range pieces the last partition ran its scans in (numScans when none was split)."""
+        return int(lib().mp_job_scan_pieces(self.h))
+
     def set_dump_dir(self, d: str | Path | None):
         _check(lib().mp_job_set_dump_dir(self.h, str(d).encode() if d else None), "set_dump_dir")
 
@@ -286,7 +298,8 @@ class Job:
                 "big_buckets": nb.value, "big_tuples": nt.value, "unit_passes": uc[0],
                 "unit_cycles": {"load": uc[1], "passes": uc[2], "store": uc[3]},
                 "pass_cycles": {"tile_id": uc[4], "load_rank": uc[5], "scan": uc[6], "order_lookback": uc[7],
-                                "store": uc[8], "lookback_words": uc[9], "lookback_waits": uc[10]}}
+                                "store": uc[8], "lookback_words": uc[9], "lookback_waits": uc[10]},
+                "scan_pieces": self.scan_pieces}
 
 
 def fastq_index_ptr(num_chunks: int, host_ptr: int, nbytes: int, interleaved: bool = False):
