@@ -389,8 +389,9 @@ int radix_sort(SortBufs &b, uint64_t n, bool has_hi, DeviceArena &arena, cudaStr
 // Sort by m-mer bucket, then within buckets.
 //
 // The tuples of a scan are sorted first by their m-mer bucket (the top 20 bits of the
-// k-mer) with onesweep passes over the bucket's bytes only -- the per-bucket counts are the
-// .kmerHist the scan was planned from, so the digit offsets need no histogram pass -- and
+// k-mer) with onesweep passes over the bucket bits that vary within the scan, in digits of at
+// most 8 bits and near-equal width -- the per-bucket counts are the .kmerHist the scan was
+// planned from, so the digit offsets need no histogram pass -- and
 // then each unit of consecutive buckets (at most SS_CAP tuples) is sorted in shared memory
 // by the rest of the key: (bucket - first bucket of the unit) << lowbits | the low k-mer
 // bits and the adjacency byte.  Buckets larger than a unit are gathered, sorted together
