@@ -398,31 +398,44 @@ int radix_sort(SortBufs &b, uint64_t n, bool has_hi, DeviceArena &arena, cudaStr
 // by the device-wide sort and put back.  Both steps are stable, so the result equals the
 // stable (k-mer, adjacency) order of the enumeration (metapart.c:1496, 2169-2195).
 
-constexpr int SS_THREADS = 1024;
+// Two block shapes sort the units: 512 threads for units of at most SS_SMALL_CAP tuples, two blocks per
+// SM (so one block's barriers and digit scans overlap the other's ranking), and 1024 threads, one block
+// per SM, for single buckets of up to SS_CAP tuples.  Buckets above SS_CAP take the device-wide sort.
 constexpr int SS_ITEMS = 12;
-constexpr int SS_CAP = SS_THREADS * SS_ITEMS;  // 12288 tuples per unit
-constexpr int SS_WARPS = SS_THREADS / 32;
+constexpr int SS_CAP = 1024 * SS_ITEMS;        // 12288: the most tuples a unit holds
+constexpr int SS_SMALL_CAP = 6128;             // 512 x 12 slots; two blocks' shared memory fit one SM
 constexpr uint32_t SS_MAXB = 4096;             // buckets per unit
 constexpr int SS_MAXBITS = 9;                  // widest digit of the unit sort (53 varying bits: six passes)
 constexpr int SS_BINS = 1 << SS_MAXBITS;
 
-struct SegSmem {
-    uint64_t key[SS_CAP];                // 96 KB
-    uint16_t perm[2][SS_CAP];            // 48 KB
-    uint32_t ids[SS_CAP];                // 48 KB: the unit's ids, loaded with the keys
-    uint16_t whist[SS_WARPS][SS_BINS];   // 32 KB: digit counts per warp, then each (warp, digit)'s offset in the digit
+template <int THREADS, int CAP>
+struct SegSmemT {
+    static constexpr int WARPS = THREADS / 32;
+    uint64_t key[CAP];
+    uint16_t perm[2][CAP];
+    uint32_t ids[CAP];                   // the unit's ids, loaded with the keys
+    uint16_t whist[WARPS][SS_BINS];      // digit counts per warp, then each (warp, digit)'s offset in the digit
     uint16_t dstart[SS_BINS];            // first position of each digit
-    uint32_t wsum[SS_WARPS];
+    uint32_t wsum[WARPS];
     unsigned long long kor, kand;
 };
-static_assert(offsetof(SegSmem, whist) % 16 == 0, "histogram rows are cleared with 16-byte stores");
+typedef SegSmemT<1024, SS_CAP> SegSmemL;
+typedef SegSmemT<512, SS_SMALL_CAP> SegSmemS;
+static_assert(offsetof(SegSmemL, whist) % 16 == 0 && offsetof(SegSmemS, whist) % 16 == 0,
+              "histogram rows are cleared with 16-byte stores");
+static_assert(sizeof(SegSmemL) <= 227 * 1024, "one 1024-thread unit block per SM");
+static_assert(2 * (sizeof(SegSmemS) + 1024) <= 228 * 1024, "two 512-thread unit blocks per SM");
+static_assert(SS_SMALL_CAP <= 512 * SS_ITEMS, "a small unit fits its block's slots");
 
 // One stable counting-sort pass over a unit: perm[cur] (or the identity) -> perm[cur ^ 1] by the
 // digit (key >> sh) & mask, nbins = a power of two >= 32 covering the mask.  Items are ranked in
 // warp-blocked order with match_any, so equal digits keep their order.  Every warp's histogram row
 // is zero on entry and on exit: a warp clears its own row once its scatter has read it.
-__device__ void seg_pass(SegSmem &sm, int cur, uint32_t cnt, int sh, uint32_t mask, uint32_t nbins, bool identity)
+template <int THREADS, int CAP>
+__device__ void seg_pass(SegSmemT<THREADS, CAP> &sm, int cur, uint32_t cnt, int sh, uint32_t mask, uint32_t nbins,
+                         bool identity)
 {
+    constexpr int SS_WARPS = THREADS / 32;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t lt = (1u << lane) - 1;
     uint32_t src[SS_ITEMS], rd[SS_ITEMS];  // rd: rank (bits 0-15) | digit (bits 16-27; nbins = none)
@@ -495,15 +508,17 @@ __device__ void seg_pass(SegSmem &sm, int cur, uint32_t cnt, int sh, uint32_t ma
 // low k-mer bits and adjacency, stable LSD over the key's varying bits in digits of at most max_bits
 // (equal widths, so 53 varying bits take six passes).  While a unit is sorted, the next unit of this
 // block is prefetched into L2.  trace (nullable): [0] digit passes, [1..3] SM cycles in load, passes, store.
-__global__ void __launch_bounds__(SS_THREADS) k_segsort(const uint64_t *__restrict__ ustart, const uint32_t *__restrict__ ucount,
+template <int THREADS, int CAP>
+__global__ void __launch_bounds__(THREADS, 1024 / THREADS) k_segsort(const uint64_t *__restrict__ ustart, const uint32_t *__restrict__ ucount,
                                                          const uint32_t *__restrict__ ubucket, uint32_t nunits,
                                                          const uint64_t *__restrict__ lo_in, const uint8_t *__restrict__ hi_in,
                                                          const uint32_t *__restrict__ id_in, uint64_t *__restrict__ lo_out,
                                                          uint32_t *__restrict__ id_out, int bsh, int lowbits, int max_bits,
                                                          unsigned long long *trace)
 {
+    constexpr int SS_THREADS = THREADS;
     extern __shared__ __align__(16) unsigned char smraw[];
-    SegSmem &sm = *reinterpret_cast<SegSmem *>(smraw);
+    SegSmemT<THREADS, CAP> &sm = *reinterpret_cast<SegSmemT<THREADS, CAP> *>(smraw);
     const int lane = threadIdx.x & 31;
     const uint64_t lowmask = (1ull << lowbits) - 1;
     unsigned long long cyc[3] = {0, 0, 0}, npass = 0;
@@ -693,13 +708,13 @@ __global__ void k_bp_compact(const uint32_t *pop, const uint64_t *popoff, uint64
 
 constexpr int BP_BLOCK = 256;  // populated buckets packed greedily by one thread
 
-// Greedy packing of consecutive populated buckets into units (at most SS_CAP tuples, SS_MAXB buckets),
-// one thread per block of BP_BLOCK populated buckets; buckets above SS_CAP are listed apart.  Units never
+// Greedy packing of consecutive populated buckets into units (at most cap tuples, SS_MAXB buckets),
+// one thread per block of BP_BLOCK populated buckets; buckets above cap are listed apart.  Units never
 // cross a block, so each block ends with one partial unit.  Block g writes its units from g * BP_BLOCK
 // into the staging arrays and their counts to nu_blk[g], nb_blk[g].
 __global__ void k_bp_greedy(const uint32_t *P, uint64_t np, const uint64_t *__restrict__ hist, uint64_t lo,
                             uint64_t *sus, uint32_t *suc, uint32_t *sub, uint64_t *sbs, uint32_t *sbc, uint32_t *sbb,
-                            uint32_t *nu_blk, uint32_t *nb_blk)
+                            uint32_t *nu_blk, uint32_t *nb_blk, uint32_t cap)
 {
     const uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const uint64_t i0 = g * BP_BLOCK;
@@ -710,7 +725,7 @@ __global__ void k_bp_greedy(const uint32_t *P, uint64_t np, const uint64_t *__re
     bool have = false;
     for (uint64_t i = i0; i < i1; i++) {
         const uint64_t bk = P[i], c = hist[bk + 1] - hist[bk], s = hist[bk] - base;
-        if (c > (uint64_t)SS_CAP) {
+        if (c > (uint64_t)cap) {
             if (have) {
                 sus[i0 + nu] = u_start; suc[i0 + nu] = (uint32_t)u_cnt; sub[i0 + nu] = u_b0; nu++;
                 have = false;
@@ -718,7 +733,7 @@ __global__ void k_bp_greedy(const uint32_t *P, uint64_t np, const uint64_t *__re
             sbs[i0 + nb] = s; sbc[i0 + nb] = (uint32_t)c; sbb[i0 + nb] = (uint32_t)bk; nb++;
             continue;
         }
-        if (have && (u_cnt + c > (uint64_t)SS_CAP || bk - u_b0 >= SS_MAXB)) {
+        if (have && (u_cnt + c > (uint64_t)cap || bk - u_b0 >= SS_MAXB)) {
             sus[i0 + nu] = u_start; suc[i0 + nu] = (uint32_t)u_cnt; sub[i0 + nu] = u_b0; nu++;
             have = false;
         }
@@ -804,7 +819,8 @@ static void sort_kernel_attrs()
         cudaFuncSetAttribute(k_onesweep<2, 7>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SortSmem));
         cudaFuncSetAttribute(k_onesweep<2, 6>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SortSmem));
         cudaFuncSetAttribute(k_onesweep<2, 5>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SortSmem));
-        cudaFuncSetAttribute(k_segsort, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SegSmem));
+        cudaFuncSetAttribute(k_segsort<1024, SS_CAP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SegSmemL));
+        cudaFuncSetAttribute(k_segsort<512, SS_SMALL_CAP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SegSmemS));
     });
 }
 
@@ -911,7 +927,8 @@ int bucket_sort(SortBufs &b, uint64_t n, bool has_hi, int k, const uint64_t *d_h
     MP_CUDA(cudaMemsetAsync(nb_blk, 0, (nblk + 1) * sizeof(uint32_t), st));
     if (nblk) {
         (mp::count_launch(), k_bp_greedy<<<(unsigned)((nblk + 127) / 128), 128, 0, st>>>(P, np, d_hist, scan_lo, s_us, s_uc, s_ub,
-                                                                                      s_bs, s_bc, s_bb, nu_blk, nb_blk));
+                                                                                      s_bs, s_bc, s_bb, nu_blk, nb_blk,
+                                                                                      (uint32_t)SS_SMALL_CAP));
     }
     scan_u32_to_u64(nu_blk, uoff, nblk + 1, tot + 1, tmp2, tb2, st);
     scan_u32_to_u64(nb_blk, boff, nblk + 1, tot + 2, tmp3, tb2, st);
@@ -921,19 +938,62 @@ int bucket_sort(SortBufs &b, uint64_t n, bool has_hi, int k, const uint64_t *d_h
     uint64_t hn[2] = {0, 0};
     MP_CUDA(cudaMemcpyAsync(hn, tot + 1, 2 * sizeof(uint64_t), cudaMemcpyDeviceToHost, st));
     MP_CUDA(cudaStreamSynchronize(st));
-    const uint64_t nu = hn[0], nb = hn[1];
+    const uint64_t nu = hn[0];
+    uint64_t nb = hn[1], nm = 0;
     const int in = b.cur, out = b.cur ^ 1;
     if (nu)
-        (mp::count_launch(), k_segsort<<<(unsigned)std::min<uint64_t>(nu, (uint64_t)sm_count()), SS_THREADS, sizeof(SegSmem), st>>>(
+        (mp::count_launch(), k_segsort<512, SS_SMALL_CAP><<<(unsigned)std::min<uint64_t>(nu, 2ull * (uint64_t)sm_count()), 512,
+                                                            sizeof(SegSmemS), st>>>(
             d_us, d_uc, d_ub, (uint32_t)nu, b.lo[in], has_hi ? b.hi[in] : nullptr, b.id[in], b.lo[out], b.id[out], bsh,
             lowbits, unit_sort_max_bits(), trace));
+    // buckets above a small unit: up to SS_CAP tuples each is a unit of its own for the 1024-thread blocks,
+    // the rest take the device-wide sort
+    std::vector<uint32_t> bc;
+    if (nb) {
+        std::vector<uint64_t> hs(nb);
+        std::vector<uint32_t> hc(nb), hk(nb);
+        MP_CUDA(cudaMemcpyAsync(hs.data(), d_bs, nb * 8, cudaMemcpyDeviceToHost, st));
+        MP_CUDA(cudaMemcpyAsync(hc.data(), d_bc, nb * 4, cudaMemcpyDeviceToHost, st));
+        MP_CUDA(cudaMemcpyAsync(hk.data(), d_bb, nb * 4, cudaMemcpyDeviceToHost, st));
+        MP_CUDA(cudaStreamSynchronize(st));
+        std::vector<uint64_t> ms, gs;
+        std::vector<uint32_t> mc, mk, gk;
+        for (uint64_t q = 0; q < nb; q++) {
+            if (hc[q] <= (uint32_t)SS_CAP) {
+                ms.push_back(hs[q]);
+                mc.push_back(hc[q]);
+                mk.push_back(hk[q]);
+            } else {
+                gs.push_back(hs[q]);
+                bc.push_back(hc[q]);
+                gk.push_back(hk[q]);
+            }
+        }
+        nm = ms.size();
+        nb = gs.size();
+        if (nm) {
+            uint64_t *d_ms = arena.alloc<uint64_t>(nm);
+            uint32_t *d_mc = arena.alloc<uint32_t>(nm), *d_mk = arena.alloc<uint32_t>(nm);
+            if (!d_ms || !d_mc || !d_mk) return set_error(MP_ENOMEM, "device memory for sort units");
+            MP_CUDA(cudaMemcpyAsync(d_ms, ms.data(), nm * 8, cudaMemcpyHostToDevice, st));
+            MP_CUDA(cudaMemcpyAsync(d_mc, mc.data(), nm * 4, cudaMemcpyHostToDevice, st));
+            MP_CUDA(cudaMemcpyAsync(d_mk, mk.data(), nm * 4, cudaMemcpyHostToDevice, st));
+            (mp::count_launch(), k_segsort<1024, SS_CAP><<<(unsigned)std::min<uint64_t>(nm, (uint64_t)sm_count()), 1024,
+                                                          sizeof(SegSmemL), st>>>(
+                d_ms, d_mc, d_mk, (uint32_t)nm, b.lo[in], has_hi ? b.hi[in] : nullptr, b.id[in], b.lo[out], b.id[out], bsh,
+                lowbits, unit_sort_max_bits(), trace));
+        }
+        if (nb) {  // the oversized buckets, in order, at the front of the lists
+            MP_CUDA(cudaMemcpyAsync(d_bs, gs.data(), nb * 8, cudaMemcpyHostToDevice, st));
+            MP_CUDA(cudaMemcpyAsync(d_bc, bc.data(), nb * 4, cudaMemcpyHostToDevice, st));
+            MP_CUDA(cudaMemcpyAsync(d_bb, gk.data(), nb * 4, cudaMemcpyHostToDevice, st));
+            MP_CUDA(cudaStreamSynchronize(st));  // gs, bc and gk are host vectors of this block
+        }
+    }
     cudaEventRecord(ev[2], st);
     uint64_t nbig = 0;
     if (nb) {
-        std::vector<uint32_t> bc(nb);
         std::vector<uint64_t> bo(nb);
-        MP_CUDA(cudaMemcpyAsync(bc.data(), d_bc, nb * 4, cudaMemcpyDeviceToHost, st));
-        MP_CUDA(cudaStreamSynchronize(st));
         uint64_t *d_bo = arena.alloc<uint64_t>(nb + 1);
         if (!d_bo) return set_error(MP_ENOMEM, "device memory for oversized buckets");
         // batches of oversized buckets whose index fits above the low key bits
@@ -985,7 +1045,7 @@ int bucket_sort(SortBufs &b, uint64_t n, bool has_hi, int k, const uint64_t *d_h
         stats->bytes = (uint64_t)passes.size() * 2 * (12 + (has_hi ? 1 : 0)) * n;
         stats->seg_ms = bms;
         stats->big_ms = c;
-        stats->units = nu;
+        stats->units = nu + nm;
         stats->big_buckets = nb;
         stats->big_tuples = nbig;
         stats->unit_passes = ht[0];
