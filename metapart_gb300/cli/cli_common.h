@@ -22,14 +22,14 @@ typedef struct {
     int32_t file_no;
 } idx_hdr;
 
-static void cli_die(const char *prog, const char *what, int rc)
+static inline void cli_die(const char *prog, const char *what, int rc)
 {
     fprintf(stderr, "%s: %s%s%s (code %d)\n", prog, what, rc ? ": " : "", rc ? mp_last_error() : "", rc);
     exit(1);
 }
 
 /* Read-only mapping of a whole file. */
-static const char *map_file(const char *path, uint64_t *size)
+static inline const char *map_file(const char *path, uint64_t *size)
 {
     int fd = open(path, O_RDONLY);
     if (fd < 0) return NULL;
@@ -42,7 +42,7 @@ static const char *map_file(const char *path, uint64_t *size)
     return p == MAP_FAILED ? NULL : (const char *)p;
 }
 
-static void hdr_put(unsigned char *r, const idx_hdr *h)
+static inline void hdr_put(unsigned char *r, const idx_hdr *h)
 {
     memset(r, 0, IDX_HDR);
     memcpy(r + 0, &h->offset, 8);
@@ -51,7 +51,7 @@ static void hdr_put(unsigned char *r, const idx_hdr *h)
     memcpy(r + 20, &h->read_id, 4);
     memcpy(r + 24, &h->file_no, 4);
 }
-static void hdr_get(const unsigned char *r, idx_hdr *h)
+static inline void hdr_get(const unsigned char *r, idx_hdr *h)
 {
     memcpy(&h->offset, r + 0, 8);
     memcpy(&h->offset2, r + 8, 8);
@@ -61,7 +61,7 @@ static void hdr_get(const unsigned char *r, idx_hdr *h)
 }
 
 /* Headers of every record of an index file (.idx / .KmerIdx*); returns the record count or -1. */
-static int read_index_headers(const char *path, idx_hdr **out)
+static inline int read_index_headers(const char *path, idx_hdr **out)
 {
     FILE *f = fopen(path, "rb");
     if (!f) return -1;
@@ -88,7 +88,7 @@ typedef struct {
     uint64_t total;
 } fastq_set;
 
-static void load_fastq_set(const char *prog, int nfiles, char **names, fastq_set *fs)
+static inline void load_fastq_set(const char *prog, int nfiles, char **names, fastq_set *fs)
 {
     fs->nfiles = nfiles;
     fs->data = (const char **)calloc((size_t)nfiles, sizeof(char *));
@@ -108,7 +108,7 @@ static void load_fastq_set(const char *prog, int nfiles, char **names, fastq_set
 }
 
 /* The files as one contiguous buffer (the mapping itself for a single file). */
-static const char *fastq_concat(const fastq_set *fs, char **owned)
+static inline const char *fastq_concat(const fastq_set *fs, char **owned)
 {
     *owned = NULL;
     if (fs->nfiles == 1) return fs->data[0];
@@ -119,7 +119,7 @@ static const char *fastq_concat(const fastq_set *fs, char **owned)
     return b;
 }
 
-static int env_device(void)
+static inline int env_device(void)
 {
     const char *d = getenv("MP_DEVICE");
     return d ? atoi(d) : 0;

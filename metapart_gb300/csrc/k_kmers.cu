@@ -485,7 +485,7 @@ __global__ void k_enum_min3(const uint8_t *fq, const uint64_t *seq_off, const ui
         const uint64_t end = WRITE ? out_off[r + 1] : 0;
         uint32_t c = 0;
         min3_read<true>(fq + seq_off[r], (int)L, k, lo, hi, [&](uint64_t v, uint32_t adj) {
-            if (WRITE) {
+            if constexpr (WRITE) {
                 if (pos < end) {
                     o_lo[pos] = (v << 8) | adj;
                     if (o_hi) o_hi[pos] = (uint8_t)(v >> 56);

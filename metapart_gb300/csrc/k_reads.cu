@@ -161,8 +161,6 @@ __global__ void __launch_bounds__(NL_THREADS) k_nl_count(const uint8_t *buf, uin
         }
     }
     uint64_t tot;
-    __shared__ uint64_t dummy;
-    (void)dummy;
     uint64_t x = c;
     for (int o = 16; o; o >>= 1) x += __shfl_xor_sync(0xFFFFFFFFu, x, o);
     __shared__ uint64_t ws[NL_THREADS / 32];

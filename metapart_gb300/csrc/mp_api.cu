@@ -875,7 +875,8 @@ static int scan_in_pieces(mp_job *j, int s, int k, bool has_hi, uint64_t lo, uin
         MP_CUDA(cudaMemcpyAsync(f.data(), j->d_filtered, N, cudaMemcpyDeviceToHost, j->st));
         MP_CUDA(cudaStreamSynchronize(j->st));
         snprintf(name, sizeof name, "scan%d_bad.bin", s);
-        if ((rc = write_file(j->dump_dir + "/" + name, f.data(), N))) return rc;
+        rc = write_file(j->dump_dir + "/" + name, f.data(), N);
+        if (rc) return rc;
     }
     // ---- sweep 2: the unions, piece by piece, from the scan's initial state
     uint32_t first_parent = 0;
@@ -1112,7 +1113,8 @@ int mp_job_partition(mp_job *j, const mp_part_params *p, const uint64_t *chunk_s
             MP_CUDA(cudaMemcpyAsync(f.data(), j->d_filtered, N, cudaMemcpyDeviceToHost, j->st));
             MP_CUDA(cudaStreamSynchronize(j->st));
             snprintf(name, sizeof name, "scan%d_bad.bin", s);
-            if ((rc = write_file(j->dump_dir + "/" + name, f.data(), N))) return rc;
+            rc = write_file(j->dump_dir + "/" + name, f.data(), N);
+            if (rc) return rc;
         }
         {
             StageTimer tm(j->st, &j->stage_ms[5]);
