@@ -213,18 +213,29 @@ def main():
         job.prepare_output()
 
     out_host = None
+    phase = {"index": 0.0, "load_count": 0.0, "partition": 0.0, "output_plan": 0.0, "download": 0.0}
 
     def e2e_step():
         nonlocal out_host
+        t0 = time.perf_counter()
         job.reset()
         f, o = native.fastq_index_ptr(args.chunks, host_in.data_ptr(), nbytes)
         st = native.chunk_starts_of(f, o, [nbytes])
+        t1 = time.perf_counter()
         cnt = job.load_count(host_in.data_ptr(), nbytes, args.k, st, min3)
+        t2 = time.perf_counter()
         job.partition(args.k, args.scans, args.threads, st, cnt.chunk_first_read, cnt.hist, min3)
+        t3 = time.perf_counter()
         _, total = job.output_plan()
         if out_host is None or out_host.numel() < total:
             out_host = torch.empty(total + 16, dtype=torch.uint8, pin_memory=True)
-        return job.output_to(out_host.data_ptr(), out_host.numel())
+        t4 = time.perf_counter()
+        n = job.output_to(out_host.data_ptr(), out_host.numel())
+        t5 = time.perf_counter()
+        for kk, a, b in (("index", t0, t1), ("load_count", t1, t2), ("partition", t2, t3), ("output_plan", t3, t4),
+                         ("download", t4, t5)):
+            phase[kk] += (b - a) * 1e3
+        return n
 
     for _ in range(args.warmup):
         device_step()
@@ -266,20 +277,24 @@ def main():
     value = dist.world * bases / (ms / 1e3)
     # ---- end to end through the C ABI, host buffers
     e2e_step()
+    for kk in phase:
+        phase[kk] = 0.0
     dist.barrier()
     torch.cuda.synchronize(dev)
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
     out_bytes = 0
-    for _ in range(args.steps):
-        out_bytes = e2e_step()
-    e1.record(stream)
-    e1.synchronize()
+    with ClockSampler(dev) as clk_e2e:
+        e0.record(stream)
+        for _ in range(args.steps):
+            out_bytes = e2e_step()
+        e1.record(stream)
+        e1.synchronize()
     dist.barrier()
     e2e_pieces = job.scan_pieces
     e2e_ms = dist.max(e0.elapsed_time(e1) / args.steps)
     e2e_value = dist.world * bases / (e2e_ms / 1e3)
+    link = link_bandwidth(host_in, dev_in[:nbytes], out_host)
 
     peak, peak_kind = measured_peak()
     achieved = (sort_bytes / 1e9) / (sort_ms / 1e3) if sort_ms > 0 else 0.0
@@ -308,7 +323,9 @@ def main():
                    "l2": "inputs larger than L2 (FASTQ and tuple arrays are GBs)", "parallelism": "replicas"},
         "e2e": {"value": round(e2e_value, 1), "unit": "bases/s", "ms_per_step": round(e2e_ms, 3),
                 "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": int(out_bytes) + 8 * (1 << 20) + 8,
-                "scan_pieces": e2e_pieces},
+                "scan_pieces": e2e_pieces,
+                "phase_ms": {kk: round(v / args.steps, 2) for kk, v in phase.items()},
+                "link_gbs": link, "clocks": clk_e2e.summary()},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
                      "kernel": "k_onesweep (radix digit pass)",
@@ -330,6 +347,28 @@ def main():
     if dist.rank == 0:
         print(json.dumps(line), flush=True)
     dist.close()
+
+
+def link_bandwidth(host_in, dev_buf, host_out) -> dict:
+    """Host link rate of plain copies between the pinned buffers and HBM (GB/s, best of three), for
+    reading the e2e phases against.  Blocking copies: the pinned buffers carry no pending events into
+    interpreter shutdown."""
+    import torch
+    n = min(host_in.numel(), dev_buf.numel(), host_out.numel())
+    up = dn = 0.0
+    for _ in range(3):
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        c = torch.cuda.Event(enable_timing=True)
+        a.record()
+        dev_buf[:n].copy_(host_in[:n])
+        b.record()
+        host_out[:n].copy_(dev_buf[:n])
+        c.record()
+        c.synchronize()
+        up = max(up, n / a.elapsed_time(b) / 1e6)
+        dn = max(dn, n / b.elapsed_time(c) / 1e6)
+    return {"h2d": round(up, 1), "d2h": round(dn, 1), "bytes": int(n)}
 
 
 # ------------------------------------------------- request loop and batches

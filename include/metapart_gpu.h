@@ -151,12 +151,14 @@ int mp_sort_tuples(mp_ctx *ctx, const uint64_t *lo_in, const uint8_t *hi_in, con
  * they run: a host that gives this library only buffers from its own device allocator, or a loop that
  * must not call cudaMalloc/cudaFree (they can synchronize the whole device) between its steps.  Same
  * arguments and results as mp_sort_tuples, without a context; it returns after the sort completed on
- * `stream`.  It allocates nothing: its scratch is one fixed device array inside the library (about
- * 14 MB on every GPU that loads the library, held until the process exits), so n is limited to
- * 1,048,576 tuples -- a larger n returns MP_EARG before any GPU work.  The first call on a device looks
- * up that array's device address (cudaGetSymbolAddress); make that first call before any stream
- * capture.  Every call uses the same array: calls that overlap on the GPU (other streams, other host
- * threads) race on it and corrupt each other.  This entry point has no counterpart in the reference. */
+ * `stream`.  Each output array may be its own input array (sorted in place); an output that overlaps any
+ * other input, or its own input only in part, returns MP_EARG.  It allocates nothing: its scratch is one
+ * fixed device array inside the library (about 14 MB on every GPU that loads the library, held until the
+ * process exits), so n is limited to 1,048,576 tuples -- a larger n returns MP_EARG before any GPU work.
+ * The first call on a device looks up that array's device address (cudaGetSymbolAddress); make that
+ * first call before any stream capture.  Every call uses the same array: calls that overlap on the GPU
+ * (other streams, other host threads) race on it and corrupt each other.  This entry point has no
+ * counterpart in the reference. */
 int mp_sort_tuples_noalloc(const uint64_t *lo_in, const uint8_t *hi_in, const uint32_t *id_in, uint64_t *lo_out,
                            uint8_t *hi_out, uint32_t *id_out, uint64_t n, void *stream);
 

@@ -25,7 +25,9 @@ CLI = PKG / "cli"
 BUILD = PKG / "_build"
 ORACLE = ROOT / "oracle"
 ORACLE_BUILD = ORACLE / "_build"
-REFERENCE_ROOT = Path(os.environ.get("MP_REFERENCE_ROOT", "/root/reference"))
+# Where oracle/build_ref.sh found the reference sources it built from (written by the recipe); the
+# reference's own test fixture is read from there.
+REFERENCE_ROOT_FILE = ORACLE / "_ref" / "REFERENCE_ROOT"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC = os.environ.get("NVCC", shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc")
@@ -69,14 +71,29 @@ def build_oracle(force: bool = False) -> None:
 
 
 def build_reference(force: bool = False) -> bool:
-    """Builds the reference programs into oracle/_ref when the reference sources are present."""
-    if not (REFERENCE_ROOT / "src" / "metapart.c").exists():
-        return False
+    """Builds the reference programs into oracle/_ref when the reference sources are present (the recipe
+    oracle/build_ref.sh knows where; MP_REFERENCE_ROOT overrides it).  False when they are absent."""
     marker = ORACLE / "_ref" / "metapart_dumpmin"
     deps = [ORACLE / "build_ref.sh", ORACLE / "ref_hooks.c", ORACLE / "mpi_shim" / "mpi.h"]
-    if force or _stale(marker, deps):
-        _run(["bash", str(ORACLE / "build_ref.sh"), str(REFERENCE_ROOT)])
+    if not (force or _stale(marker, deps)):
+        return True
+    root = os.environ.get("MP_REFERENCE_ROOT")
+    r = subprocess.run(["bash", str(ORACLE / "build_ref.sh"), *([root] if root else [])], stdout=subprocess.PIPE,
+                       stderr=subprocess.STDOUT, text=True)
+    if r.returncode == 2:  # the recipe found no reference sources
+        return False
+    if r.returncode != 0:
+        raise RuntimeError(f"build step failed ({r.returncode}): oracle/build_ref.sh\n{r.stdout}")
     return True
+
+
+def reference_root() -> Path | None:
+    """The reference source tree oracle/_ref was built from, or None where it was not built."""
+    try:
+        p = Path(REFERENCE_ROOT_FILE.read_text().strip())
+    except OSError:
+        return None
+    return p if (p / "src" / "metapart.c").exists() else None
 
 
 def build_synth(force: bool = False) -> None:

@@ -777,7 +777,7 @@ int mate_union_and_plan(uint32_t *parent, uint64_t n_reads, uint32_t *size, uint
     while (nact > 0) {
         if (round + RB > 4000000u) return set_error(MP_EDEVICE, "mate union did not converge");
         // counts only shrink, so nact bounds every list of the batch
-        const unsigned g = (unsigned)std::min<uint64_t>(blocks_for(nact, 256), 152u * 8u);
+        const unsigned g = (unsigned)std::min<uint64_t>(blocks_for(nact, 256), 8ull * (uint64_t)sm_count());
         MP_CUDA(cudaMemsetAsync(cnts, 0, (4 * RB + 4) * sizeof(unsigned int), st));
         MP_CUDA(cudaMemcpyAsync(cnts + 4 * RB + 1, &nact, sizeof(unsigned int), cudaMemcpyHostToDevice, st));
         for (int r = 0; r < RB; r++) {

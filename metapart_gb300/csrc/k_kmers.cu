@@ -506,11 +506,13 @@ __global__ void k_enum_min3(const uint8_t *fq, const uint64_t *seq_off, const ui
 
 // ------------------------------------------------------------- host side
 
-static unsigned grid_for(uint64_t work, int per_block, int max_blocks = 152 * 16)
+// Blocks for `work` items at per_block each, at most `waves` blocks per SM.
+static unsigned grid_for(uint64_t work, int per_block, int waves = 16)
 {
+    const uint64_t max_blocks = (uint64_t)waves * (uint64_t)sm_count();
     uint64_t g = (work + per_block - 1) / per_block;
     if (g < 1) g = 1;
-    if (g > (uint64_t)max_blocks) g = max_blocks;
+    if (g > max_blocks) g = max_blocks;
     return (unsigned)g;
 }
 
@@ -519,7 +521,7 @@ void launch_count(const uint8_t *fq, const ParsedReads &pr, int k, int min3, con
                   uint64_t *kc_lo, uint8_t *kc_hi)
 {
     if (min3)
-        (mp::count_launch(), k_count_min3<<<grid_for(pr.n_reads, 128, 152 * 32), 128, 0, st>>>(fq, pr.seq_off, pr.seq_len, 0, pr.n_reads, k,
+        (mp::count_launch(), k_count_min3<<<grid_for(pr.n_reads, 128, 32), 128, 0, st>>>(fq, pr.seq_off, pr.seq_len, 0, pr.n_reads, k,
                                                                           chunk_rec, nchunks, cc, glob, err));
     else
         (mp::count_launch(), k_count_plain<<<grid_for(pr.n_reads, 8), 256, 0, st>>>(fq, pr.seq_off, pr.seq_len, 0, pr.n_reads, k, chunk_rec,
@@ -531,7 +533,7 @@ void launch_enum_count(const uint8_t *fq, const ParsedReads &pr, int k, int min3
                        uint32_t *cnt, uint32_t *err, cudaStream_t st)
 {
     if (min3)
-        (mp::count_launch(), k_enum_min3<false><<<grid_for(pr.n_reads, 128, 152 * 32), 128, 0, st>>>(
+        (mp::count_launch(), k_enum_min3<false><<<grid_for(pr.n_reads, 128, 32), 128, 0, st>>>(
             fq, pr.seq_off, pr.seq_len, pr.n_reads, k, lo, hi, nullptr, nullptr, cnt, nullptr, nullptr, nullptr, err));
     else
         (mp::count_launch(), k_enum_plain<false><<<grid_for(pr.n_reads, 8), 256, 0, st>>>(fq, pr.seq_off, pr.seq_len, pr.n_reads, k, lo, hi,
@@ -575,7 +577,7 @@ void launch_enum_write(const uint8_t *fq, const ParsedReads &pr, int k, int min3
                        uint32_t *err, cudaStream_t st)
 {
     if (min3)
-        (mp::count_launch(), k_enum_min3<true><<<grid_for(pr.n_reads, 128, 152 * 32), 128, 0, st>>>(
+        (mp::count_launch(), k_enum_min3<true><<<grid_for(pr.n_reads, 128, 32), 128, 0, st>>>(
             fq, pr.seq_off, pr.seq_len, pr.n_reads, k, lo, hi, label, off, nullptr, o_lo, o_hi, o_id, err));
     else
         (mp::count_launch(), k_enum_plain<true><<<grid_for(pr.n_reads, 8), 256, 0, st>>>(fq, pr.seq_off, pr.seq_len, pr.n_reads, k, lo, hi,

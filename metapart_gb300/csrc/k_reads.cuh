@@ -74,6 +74,25 @@ struct DeviceArena {
     }
 };
 
+// CUDA events owned by a scope: destroyed on every return path.
+struct Events {
+    std::vector<cudaEvent_t> ev;
+    explicit Events(size_t n, unsigned flags = cudaEventDefault) : ev(n, nullptr)
+    {
+        for (auto &e : ev)
+            if (cudaEventCreateWithFlags(&e, flags) != cudaSuccess) e = nullptr;
+    }
+    ~Events()
+    {
+        for (auto e : ev)
+            if (e) cudaEventDestroy(e);
+    }
+    Events(const Events &) = delete;
+    Events &operator=(const Events &) = delete;
+    cudaEvent_t &operator[](size_t i) { return ev[i]; }
+    size_t size() const { return ev.size(); }
+};
+
 struct ParsedReads {
     uint64_t n_reads = 0;
     uint64_t *rec_start = nullptr;  // n_reads + 1 record start offsets (last = input size)

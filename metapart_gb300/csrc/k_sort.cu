@@ -86,7 +86,6 @@ __global__ void __launch_bounds__(256) k_hist_upfront(const uint64_t *__restrict
 // 2 = byte of the k-mer value (lo >> 8 | hi << 56) at `shift` (the m-mer bucket digits).
 // Opt-in shared memory sizes of the sort kernels, set once per device (thread-safe).
 static void sort_kernel_attrs();
-static int sm_count();
 static uint32_t onesweep_prefetch_tiles();
 
 template <int SRC>
@@ -309,11 +308,10 @@ int radix_sort(SortBufs &b, uint64_t n, bool has_hi, DeviceArena &arena, cudaStr
     MP_CUDA(cudaMemsetAsync(ctr, 0, 16 * sizeof(uint32_t), st));
     MP_CUDA(cudaMemsetAsync(err, 0, sizeof(uint32_t), st));
     MP_CUDA(cudaMemsetAsync(status, 0, tiles * 256 * sizeof(unsigned long long), st));
-    cudaEvent_t e0, e1;
-    cudaEventCreate(&e0);
-    cudaEventCreate(&e1);
+    Events ht(2);
+    cudaEvent_t e0 = ht[0], e1 = ht[1];
     cudaEventRecord(e0, st);
-    (mp::count_launch(), k_hist_upfront<<<152 * 8, 256, 0, st>>>(b.lo[b.cur], has_hi ? b.hi[b.cur] : nullptr, n, ghist));
+    (mp::count_launch(), k_hist_upfront<<<8 * sm_count(), 256, 0, st>>>(b.lo[b.cur], has_hi ? b.hi[b.cur] : nullptr, n, ghist));
     cudaEventRecord(e1, st);
     std::vector<unsigned long long> h(9 * 256);
     MP_CUDA(cudaMemcpyAsync(h.data(), ghist, h.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
@@ -331,18 +329,13 @@ int radix_sort(SortBufs &b, uint64_t n, bool has_hi, DeviceArena &arena, cudaStr
             if (h[dgt * 256 + v] == n) constant = true;
             acc += h[dgt * 256 + v];
         }
-        if (acc != n) {
-            cudaEventDestroy(e0);
-            cudaEventDestroy(e1);
-            return set_error(MP_EDEVICE, "radix histogram does not add up");
-        }
+        if (acc != n) return set_error(MP_EDEVICE, "radix histogram does not add up");
         if (!constant) passes.push_back(dgt);
     }
     MP_CUDA(cudaMemcpyAsync(dbase, base.data(), base.size() * sizeof(uint64_t), cudaMemcpyHostToDevice, st));
     sort_kernel_attrs();
     const uint32_t pf = onesweep_prefetch_tiles();
-    std::vector<cudaEvent_t> ev(passes.size() + 1);
-    for (auto &e : ev) cudaEventCreate(&e);
+    Events ev(passes.size() + 1);
     cudaEventRecord(ev[0], st);
     for (size_t pi = 0; pi < passes.size(); pi++) {
         const int dgt = passes[pi];
@@ -377,9 +370,6 @@ int radix_sort(SortBufs &b, uint64_t n, bool has_hi, DeviceArena &arena, cudaStr
         stats->bytes = (uint64_t)passes.size() * 2 * elt * n;
         stats->hist_bytes = (8 + (has_hi ? 1 : 0)) * n;
     }
-    for (auto &e : ev) cudaEventDestroy(e);
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
     arena.free_scratch(status);
     if (herr) return set_error(MP_EDEVICE, "radix sort look-back gave up (device error flags 0x%x)", herr);
     return 0;
@@ -788,14 +778,6 @@ static bool byte_bucket_digits()
     return e && std::string(e) == "bytes";
 }
 
-static int sm_count()
-{
-    int dev = 0, n = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-    return n > 0 ? n : 1;
-}
-
 // How far ahead (in tiles) a digit-pass tile prefetches its successor into L2: a number of SM
 // waves (MP_ONESWEEP_PF_WAVES, 0 = no prefetch) times the SM count.  Three tiles are resident per
 // SM; one wave ahead measured best (the bucket-digit passes at 20M reads: 57.8 ms at one wave,
@@ -866,7 +848,7 @@ int bucket_sort(SortBufs &b, uint64_t n, bool has_hi, int k, const uint64_t *d_h
     MP_CUDA(cudaMemsetAsync(dcnt, 0, 3 * 256 * sizeof(unsigned long long), st));
     MP_CUDA(cudaMemsetAsync(pop + nbk, 0, sizeof(uint32_t), st));
     {
-        const unsigned g = (unsigned)std::min<uint64_t>((nbk + 255) / 256, 152u * 8u);
+        const unsigned g = (unsigned)std::min<uint64_t>((nbk + 255) / 256, 8ull * (uint64_t)sm_count());
         (mp::count_launch(), k_bp_count<<<g, 256, 0, st>>>(d_hist, scan_lo, nbk, bpl, dcnt, pop));
     }
     (mp::count_launch(), k_bp_digits<<<bpl.np, 256, 0, st>>>(dcnt, dbase, dnz, dmax, dmax + 3));
@@ -892,8 +874,7 @@ int bucket_sort(SortBufs &b, uint64_t n, bool has_hi, int k, const uint64_t *d_h
     if (status) MP_CUDA(cudaMemsetAsync(status, 0, tiles * 256 * sizeof(unsigned long long), st));
     sort_kernel_attrs();
     const uint32_t pf = onesweep_prefetch_tiles();
-    cudaEvent_t ev[5];
-    for (auto &e : ev) cudaEventCreate(&e);
+    Events ev(5);
     cudaEventRecord(ev[0], st);
     for (size_t pi = 0; pi < passes.size(); pi++) {
         const int d = passes[pi];
@@ -1053,7 +1034,6 @@ int bucket_sort(SortBufs &b, uint64_t n, bool has_hi, int k, const uint64_t *d_h
         for (int q = 0; q < 3; q++) stats->phase_cycles[q] = ht[1 + q];
         for (int q = 0; q < 7; q++) stats->pass_cycles[q] = ht[8 + q];
     }
-    for (auto &e : ev) cudaEventDestroy(e);
     arena.free_scratch(status);
     if (herr) return set_error(MP_EDEVICE, "radix sort look-back gave up (device error flags 0x%x)", herr);
     *out_lo_buf = out;  // lo and id end in the other buffer; hi (constant within a bucket) stays in `in`
@@ -1109,6 +1089,13 @@ static int noalloc_scratch(NoAllocScratch **out)
     return 0;
 }
 
+// [a, a + an) and [b, b + bn) share a byte.
+static bool bytes_overlap(const void *a, uint64_t an, const void *b, uint64_t bn)
+{
+    const uintptr_t x = (uintptr_t)a, y = (uintptr_t)b;
+    return an && bn && x < y + bn && y < x + an;
+}
+
 int sort_tuples_noalloc(const uint64_t *lo_in, const uint8_t *hi_in, const uint32_t *id_in, uint64_t *lo_out,
                         uint8_t *hi_out, uint32_t *id_out, uint64_t n, cudaStream_t st)
 {
@@ -1118,10 +1105,22 @@ int sort_tuples_noalloc(const uint64_t *lo_in, const uint8_t *hi_in, const uint3
     if (n > NOALLOC_MAX_TUPLES)
         return set_error(MP_EARG, "%llu tuples exceed the fixed scratch of the allocation-free sort (%llu tuples)",
                          (unsigned long long)n, (unsigned long long)NOALLOC_MAX_TUPLES);
+    const bool has_hi = hi_in != nullptr;
+    // each output array is either the same array as its input (sorted in place) or apart from every input
+    const void *ins[3] = {lo_in, id_in, hi_in};
+    const uint64_t insz[3] = {n * 8, n * 4, has_hi ? n : 0};
+    const void *outs[3] = {lo_out, id_out, hi_out};
+    bool in_place = false;
+    for (int o = 0; o < 3; o++)
+        for (int i = 0; i < 3; i++) {
+            if (!bytes_overlap(outs[o], insz[o], ins[i], insz[i])) continue;
+            if (o != i || outs[o] != ins[i])
+                return set_error(MP_EARG, "an output array overlaps an input array other than its own in-place input");
+            in_place = true;
+        }
     NoAllocScratch *S = nullptr;
     int rc = noalloc_scratch(&S);
     if (rc) return rc;
-    const bool has_hi = hi_in != nullptr;
     if (n == 0) return 0;
     const uint64_t tiles = (n + STILE - 1) / STILE;
     // the array keeps the previous call's contents: clear what must start at zero
@@ -1129,7 +1128,7 @@ int sort_tuples_noalloc(const uint64_t *lo_in, const uint8_t *hi_in, const uint3
     MP_CUDA(cudaMemsetAsync(S->ctr, 0, sizeof S->ctr, st));
     MP_CUDA(cudaMemsetAsync(&S->err, 0, sizeof S->err, st));
     MP_CUDA(cudaMemsetAsync(S->status, 0, tiles * 256 * sizeof(unsigned long long), st));
-    (mp::count_launch(), k_hist_upfront<<<152 * 2, 256, 0, st>>>(lo_in, hi_in, n, S->ghist));
+    (mp::count_launch(), k_hist_upfront<<<2 * sm_count(), 256, 0, st>>>(lo_in, hi_in, n, S->ghist));
     unsigned long long h[9 * 256];
     MP_CUDA(cudaMemcpyAsync(h, S->ghist, sizeof h, cudaMemcpyDeviceToHost, st));
     MP_CUDA(cudaStreamSynchronize(st));
@@ -1146,20 +1145,29 @@ int sort_tuples_noalloc(const uint64_t *lo_in, const uint8_t *hi_in, const uint3
         if (acc != n) return set_error(MP_EDEVICE, "radix histogram does not add up");
         if (!constant) passes[np++] = dgt;
     }
-    if (np == 0) {  // every digit constant: the input is already in order
-        MP_CUDA(cudaMemcpyAsync(lo_out, lo_in, n * 8, cudaMemcpyDeviceToDevice, st));
-        MP_CUDA(cudaMemcpyAsync(id_out, id_in, n * 4, cudaMemcpyDeviceToDevice, st));
-        if (has_hi) MP_CUDA(cudaMemcpyAsync(hi_out, hi_in, n, cudaMemcpyDeviceToDevice, st));
+    if (np == 0) {  // every digit constant: the input is already in order (nothing to move in place)
+        if (lo_out != lo_in) MP_CUDA(cudaMemcpyAsync(lo_out, lo_in, n * 8, cudaMemcpyDeviceToDevice, st));
+        if (id_out != id_in) MP_CUDA(cudaMemcpyAsync(id_out, id_in, n * 4, cudaMemcpyDeviceToDevice, st));
+        if (has_hi && hi_out != hi_in) MP_CUDA(cudaMemcpyAsync(hi_out, hi_in, n, cudaMemcpyDeviceToDevice, st));
         MP_CUDA(cudaStreamSynchronize(st));
         return 0;
     }
     MP_CUDA(cudaMemcpyAsync(S->dbase, base, sizeof base, cudaMemcpyHostToDevice, st));
     sort_kernel_attrs();
-    // pass i writes the caller's output when (np - 1 - i) is even, the scratch otherwise,
-    // so the last pass always lands in the output
+    // pass i writes the caller's output when (np - 1 - i) is even, the scratch otherwise, so the last
+    // pass always lands in the output.  A pass must not write the array it reads: in place with an odd
+    // pass count, pass 0 would, so the input is first copied to the scratch and pass 0 reads it there.
     const uint64_t *src_lo = lo_in;
     const uint8_t *src_hi = hi_in;
     const uint32_t *src_id = id_in;
+    if (in_place && (np & 1)) {
+        MP_CUDA(cudaMemcpyAsync(S->lo, lo_in, n * 8, cudaMemcpyDeviceToDevice, st));
+        MP_CUDA(cudaMemcpyAsync(S->id, id_in, n * 4, cudaMemcpyDeviceToDevice, st));
+        if (has_hi) MP_CUDA(cudaMemcpyAsync(S->hi, hi_in, n, cudaMemcpyDeviceToDevice, st));
+        src_lo = S->lo;
+        src_id = S->id;
+        src_hi = has_hi ? S->hi : nullptr;
+    }
     for (int i = 0; i < np; i++) {
         const bool to_out = ((np - 1 - i) & 1) == 0;
         uint64_t *d_lo = to_out ? lo_out : S->lo;

@@ -39,6 +39,22 @@ constexpr uint64_t UMAX32 = 4294967295ull;
 static std::atomic<uint64_t> g_launches{0};
 void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
+int sm_count()
+{
+    static std::atomic<int> cached[64];
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::atomic<int> &c = cached[dev & 63];
+    int n = c.load(std::memory_order_relaxed);
+    if (n > 0) return n;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) {
+        cudaGetLastError();
+        n = 1;
+    }
+    c.store(n, std::memory_order_relaxed);
+    return n;
+}
+
 }  // namespace mp
 
 using namespace mp;

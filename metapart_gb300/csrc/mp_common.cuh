@@ -65,6 +65,10 @@ __host__ __device__ __forceinline__ uint32_t adj_rc(uint32_t pa5, uint32_t na5)
 // Process-wide count of kernels this library launched (mp_launch_count).
 void count_launch();
 
+// Streaming multiprocessors of the current device (grids of persistent and grid-stride kernels are sized
+// in multiples of it).
+int sm_count();
+
 // Device-wide exclusive scans (k_reads.cu).
 void scan_u32_to_u64(const uint32_t *in, uint64_t *out, uint64_t n, uint64_t *total_dev, void *tmp, size_t tmp_bytes,
                      cudaStream_t st);

@@ -35,4 +35,5 @@ wait
 for b in genFastqIdx genHistograms_metapart genHistograms_metapartmin metapart metapartmin metapart_dump metapart_dumpmin; do
     test -x "$OUT/$b" || { echo "build_ref: $b missing" >&2; exit 1; }
 done
+(cd "$REF" && pwd) > "$OUT/REFERENCE_ROOT"
 echo "build_ref: ok -> $OUT"

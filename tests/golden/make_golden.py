@@ -11,6 +11,7 @@ used when the reference tree is present; its bytes are not stored, only the dige
 from __future__ import annotations
 
 import hashlib
+import os
 import json
 import random
 import sys
@@ -98,8 +99,8 @@ def make_input(gen, ref_root: Path, k: int, min3: bool = False) -> bytes | None:
     from metapart_gb300 import synth
     name, n, seed = gen
     if name == "bundled":
-        f = ref_root / "data" / "reads.fastq"
-        return f.read_bytes() if f.exists() else None
+        f = ref_root / "data" / "reads.fastq" if ref_root else None
+        return f.read_bytes() if f and f.exists() else None
     if name == "edge":
         return edge_fastq(n, seed, k, min3)
     return synth.fastq_bytes(synth.workload(name, n, seed=seed))
@@ -110,11 +111,13 @@ def params(d: dict) -> pu.Params:
 
 
 def main():
-    ref_root = Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference")
     from metapart_gb300 import build
     build.build_synth()
-    if not build.build_reference():
+    if len(sys.argv) > 1:
+        os.environ["MP_REFERENCE_ROOT"] = sys.argv[1]
+    if not build.build_reference(force=len(sys.argv) > 1):
         raise SystemExit("reference sources not found: cannot regenerate golden digests")
+    ref_root = build.reference_root()
     out = {}
     for name, c in CASES.items():
         data = make_input(c["gen"], ref_root, c["p"]["k"], c["p"].get("min3", False))

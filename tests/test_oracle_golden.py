@@ -17,7 +17,8 @@ def _input(case):
     spec = importlib.util.spec_from_file_location("make_golden", HERE / "golden" / "make_golden.py")
     mg = importlib.util.module_from_spec(spec)
     spec.loader.exec_module(mg)
-    return mg.make_input(tuple(case["gen"]), Path("/root/reference"), case["params"]["k"],
+    from metapart_gb300 import build
+    return mg.make_input(tuple(case["gen"]), build.reference_root(), case["params"]["k"],
                          case["params"].get("min3", False))
 
 
