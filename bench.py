@@ -139,7 +139,7 @@ def traffic_per_tuple():
 
 # ------------------------------------------------------------------ CPU oracle
 
-def cpu_run(sample: Path, k: int, scans: int, threads: int, chunks: int, cores: int) -> float:
+def cpu_run(sample: Path, k: int, scans: int, threads: int, chunks: int, cores: int, min3: bool = False) -> float:
     """Times the oracle's three stages (genFastqIdx, genHistograms, metapart) on a FASTQ file; seconds."""
     from metapart_gb300 import build
     cli = str(build.ORACLE_BUILD / "mpo_cli")
@@ -147,9 +147,10 @@ def cpu_run(sample: Path, k: int, scans: int, threads: int, chunks: int, cores: 
     out = d / "out"
     (out / "Rank0").mkdir(parents=True, exist_ok=True)
     env = dict(os.environ, OMP_NUM_THREADS=str(cores), OMP_STACKSIZE="16M")
+    m3 = ["--min3"] if min3 else []
     cmds = [[cli, "genFastqIdx", str(chunks), "0", "1", "0", sample.name],
-            [cli, "genHistograms", str(k), "0", "1", "0", sample.name],
-            [cli, "metapart", "-o", str(out), str(1 << 40), str(k), str(scans), str(threads), "0", "1", "0",
+            [cli, "genHistograms", *m3, str(k), "0", "1", "0", sample.name],
+            [cli, "metapart", *m3, "-o", str(out), str(1 << 40), str(k), str(scans), str(threads), "0", "1", "0",
              sample.name]]
     t0 = time.perf_counter()
     for c in cmds:
@@ -342,6 +343,7 @@ def main():
     }
     if dist.rank == 0 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(args)
+        line["parity"] = line["cpu_baseline"]["gpu_parity"]["parity"]
     job.close()
     ctx.close()
     if dist.rank == 0:
@@ -574,6 +576,32 @@ def batch_mode(args, dist):
     dist.close()
 
 
+def gpu_parity_on_sample(fq: Path, out_dir: Path, k: int, scans: int, threads: int, chunks: int,
+                         min3: bool = False) -> dict:
+    """Partitions the CPU sample on the GPU through the library with the oracle's parameters and compares
+    every partition file (FromTid<t>_ToRank<p>.paired.fastq) with the oracle's, byte for byte."""
+    import numpy as np
+    from metapart_gb300 import native
+    data = fq.read_bytes()
+    with native.Context(0) as ctx:
+        job, bounds, cnt = native.run_pipeline(ctx, data, k, chunks, scans, threads, min3=min3)
+        try:
+            buf, sizes = job.output()
+        finally:
+            job.close()
+    off = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+    bad = []
+    for p in range(16):
+        for t in range(threads):
+            j = p * threads + t
+            f = out_dir / "Rank0" / f"FromTid{t}_ToRank{p}.paired.fastq"
+            want = f.read_bytes() if f.exists() else b""
+            if bytes(buf[off[j]:off[j + 1]]) != want:
+                bad.append(f.name)
+    return {"parity": not bad, "files": 16 * threads, "files_differing": bad[:8],
+            "compared": "all partition files of the CPU sample, GPU (library) against the oracle, byte for byte"}
+
+
 def cpu_baseline(args) -> dict:
     cores = os.cpu_count() or 1
     n = args.cpu_reads or 400_000
@@ -581,10 +609,13 @@ def cpu_baseline(args) -> dict:
     with tempfile.TemporaryDirectory() as td:
         fq, bases = cpu_sample(args, n, Path(td))
         chunks = cores * max(1, 64 // cores) if cores <= 64 else cores
-        sec = cpu_run(fq, args.k, args.scans, cores, chunks, cores)
+        min3 = args.workload == "min3"
+        sec = cpu_run(fq, args.k, args.scans, cores, chunks, cores, min3)
+        par = gpu_parity_on_sample(fq, fq.parent / "out", args.k, args.scans, cores, chunks, min3)
     return {"value": round(bases / sec, 1), "unit": "bases/s", "cores": cores, "kind": "port",
             "sample": f"{n} reads of the same read set ({bases} bases), numThreads {cores}, {chunks} chunks, "
-                      f"genFastqIdx+genHistograms+metapart wall {sec:.2f} s"}
+                      f"genFastqIdx+genHistograms+metapart wall {sec:.2f} s",
+            "gpu_parity": par}
 
 
 def reference_arm(args, dist):
@@ -603,7 +634,7 @@ def reference_arm(args, dist):
         fq, bases = cpu_sample(args, n, Path(td))
         chunks = cores * max(1, 64 // cores) if cores <= 64 else cores
         for i in range(args.warmup + args.steps):
-            sec = cpu_run(fq, args.k, args.scans, cores, chunks, cores)
+            sec = cpu_run(fq, args.k, args.scans, cores, chunks, cores, args.workload == "min3")
             if i >= args.warmup:
                 times.append(sec)
     sec = statistics.mean(times)

@@ -237,7 +237,8 @@ int mp_job_set_scan_piece_tuples(mp_job *job, uint64_t max_tuples);
 int mp_job_scan_pieces(const mp_job *job);
 
 /* Optional stage dumps in the reference's formats (the files oracle/ref_hooks.c writes),
- * for parity testing.  NULL disables. */
+ * for parity testing.  NULL disables; with the environment variable MP_DUMP_TUPLES=0 only the
+ * per-read dumps (BAD flags, parents, sizes) are written, not the tuple streams. */
 int mp_job_set_dump_dir(mp_job *job, const char *dir);
 
 /* Device time of the last count/partition/output calls per stage, in ms:

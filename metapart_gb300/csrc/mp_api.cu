@@ -158,6 +158,8 @@ int dump_tuples(mp_job *j, const char *name, const uint64_t *lo, const uint8_t *
                 bool append = false)
 {
     if (j->dump_dir.empty()) return 0;
+    const char *tu = getenv("MP_DUMP_TUPLES");  // "0": the per-read dumps only (large inputs)
+    if (tu && strcmp(tu, "0") == 0) return 0;
     std::vector<uint64_t> hl(n);
     std::vector<uint8_t> hh(hi ? n : 0);
     std::vector<uint32_t> hid(n);

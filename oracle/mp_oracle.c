@@ -628,6 +628,8 @@ static void dump(const char *name, const void *buf, size_t bytes)
 static void dump_tuples(const char *name, const tup *t, uint64_t n)
 {
     if (!getenv("MP_DUMP_DIR")) return;
+    const char *tu = getenv("MP_DUMP_TUPLES");  /* "0": the per-read dumps only (large inputs) */
+    if (tu && strcmp(tu, "0") == 0) return;
     unsigned char *b = (unsigned char *)malloc(n * 14 + 1);
     for (uint64_t i = 0; i < n; i++) {
         unsigned char *o = b + i * 14;

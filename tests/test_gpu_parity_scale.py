@@ -1,0 +1,63 @@
+"""GPU parity at the benchmark configurations' own sizes: the drop-in programs against the CPU oracle, byte
+for byte, on read sets with the shapes the numbers are quoted on.
+
+  C1  100k single-end 100 bp reads from 20 genomes of 50 kb, k = 27, one scan (the full configuration),
+      16 threads / 64 chunks and 8 threads / 16 chunks; every stage dump is compared.
+  C2  the 20M-read configuration's read set (200 genomes of 1-5 Mb, log-normal abundance, 1 % errors, N at
+      1e-4) at 400k reads with every stage dump, and at 2M reads with the per-read dumps (BAD flags, parents
+      and sizes after every scan and the mate union) and the partition files; k = 31, 2 scans, 16 threads.
+  C3  the 3-minimizer configuration at its full 5M reads of 250 bp (Zipf abundance, 30 % of every genome
+      from 5 kb repeats shared across genomes: giant components and long runs of equal k-mers), k = 31, one
+      scan, 16 threads; every stage dump.
+
+The oracle is the C restatement of the reference that tests/test_oracle_golden.py pins to the reference's
+own outputs; it runs with every host core.
+"""
+import os
+
+import pytest
+
+import pipeline_util as pu
+from metapart_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+
+CORES = str(os.cpu_count() or 4)
+
+CASES = [
+    # id, workload, reads, params, dump tuple streams
+    ("C1-t16", "plain_small", 100_000, pu.Params(k=27, chunks=64, scans=1, threads=16), True),
+    ("C1-t8", "plain_small", 100_000, pu.Params(k=27, chunks=16, scans=1, threads=8), True),
+    ("C2-400k", "plain_large", 400_000, pu.Params(k=31, chunks=64, scans=2, threads=16), True),
+    ("C2-2M", "plain_large", 2_000_000, pu.Params(k=31, chunks=64, scans=2, threads=16), False),
+    ("C3-5M", "min3", 5_000_000, pu.Params(k=31, chunks=64, scans=1, threads=16, min3=True), True),
+]
+
+
+def _keys(res, p, tuples):
+    ks = [k for k in res if not k.startswith("dump/")]
+    for s in range(p.scans):
+        if tuples:
+            ks += [f"dump/scan{s}_enum.bin", f"dump/scan{s}_sorted.bin", f"dump/scan{s}_filtered.bin"]
+        ks += [f"dump/scan{s}_bad.bin", f"dump/stats{s}_parent.bin"]
+    ks += [f"dump/stats{p.scans}_parent.bin", f"dump/stats{p.scans}_sizes.bin",
+           f"dump/stats{p.scans + 1}_parent.bin", f"dump/stats{p.scans + 1}_sizes.bin"]
+    return ks
+
+
+@pytest.mark.parametrize("name,work,n,p,tuples", CASES, ids=[c[0] for c in CASES])
+def test_gpu_matches_oracle_at_config_size(tmp_path, built_gpu, name, work, n, p, tuples):
+    fq = tmp_path / "in.fastq"
+    synth.write_fastq(synth.workload(work, n, seed=7), fq)
+    env = {"OMP_NUM_THREADS": CORES}
+    if not tuples:
+        env["MP_DUMP_TUPLES"] = "0"
+    do = pu.run("oracle", tmp_path, [fq], p, env_extra=env)
+    dg = pu.run("gpu", tmp_path, [fq], p, env_extra=env)
+    a, b = pu.outputs(do, p, "in.fastq"), pu.outputs(dg, p, "in.fastq")
+    keys = _keys(a, p, tuples)
+    missing = [k for k in keys if k not in a or k not in b]
+    assert not missing, f"missing outputs {missing}"
+    assert sum(1 for k in keys if k.startswith("part/")) == 16 * p.threads
+    diff = pu.diff_keys(a, b, keys)
+    assert not diff, f"GPU output differs from the oracle in {diff}"

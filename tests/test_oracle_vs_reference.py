@@ -14,10 +14,14 @@ CASES = [
     ("plain_large", 4000, 22, pu.Params(k=31, chunks=3, scans=1, threads=3)),
     ("min3", 2000, 23, pu.Params(k=29, chunks=2, scans=1, threads=1, min3=True)),
     ("interleaved_small", 3000, 24, pu.Params(k=17, chunks=4, scans=3, threads=2, interleaved=True)),
+    # the first benchmark configuration at its full size (100k x 100 bp, k = 27, one scan)
+    ("plain_small", 100_000, 7, pu.Params(k=27, chunks=16, scans=1, threads=8)),
+    # the 3-minimizer configuration's shape (shared repeats, Zipf abundance) at 200k reads
+    ("min3", 200_000, 7, pu.Params(k=31, chunks=16, scans=1, threads=8, min3=True)),
 ]
 
 
-@pytest.mark.parametrize("name,n,seed,p", CASES, ids=[c[0] for c in CASES])
+@pytest.mark.parametrize("name,n,seed,p", CASES, ids=[f"{c[0]}-{c[1]}" for c in CASES])
 def test_oracle_equals_reference(tmp_path, built, name, n, seed, p):
     if not REF.exists():
         pytest.skip("reference programs not built here")
