@@ -10,7 +10,11 @@ union, the 16 work partitions and the partition-FASTQ gather.
   roofline -- the radix-sort digit passes (the dominant kernel): algorithmic bytes per pass over their
             CUDA-event time, against the measured HBM copy bandwidth
   cpu_baseline -- the CPU oracle (the reference's algorithm restated in C/OpenMP, all host cores) on a
-            bounded sample of the same read set
+            bounded sample of the same read set; the GPU's partition files of that sample are compared with
+            the oracle's ("parity")
+  batch  -- the batching configuration (64 samples of 50k-5M reads): the samples back to back through one
+            job ("plain") against mp_batch_run ("batched"), both from pinned host FASTQ to partition files
+  serve  -- Poisson arrivals of partition requests into the request loop: p50/p99 job latency
 
 Workload (default): 20M single-end 150 bp reads from 200 synthetic genomes (1-5 Mb, GC 0.3-0.7, log-normal
 abundance sigma 1.5, 1 % substitutions, N at 1e-4, qualities '#'..'J'); k = 31, m = 10 (the only m the
@@ -61,6 +65,9 @@ def parse_args():
     ap.add_argument("--pool", type=int, default=48, help="serve: distinct synthetic requests cycled")
     ap.add_argument("--samples", type=int, default=64, help="batch: samples")
     ap.add_argument("--sample-scale", type=float, default=1.0, help="batch: read-count scale")
+    ap.add_argument("--serve-seconds", type=float, default=15.0,
+                    help="plain mode: seconds of Poisson arrivals for the line's p50/p99 (0: none)")
+    ap.add_argument("--no-batch", action="store_true", help="plain mode: leave out the batched-vs-plain run")
     return ap.parse_args()
 
 
@@ -341,11 +348,25 @@ def main():
         "tuples_sorted_per_s": round(sort_tuples / args.steps / (ms / 1e3), 1),
         "clocks": clk.summary(),
     }
+    job.close()
+    ctx.close()
+    del dev_in
+    torch.cuda.empty_cache()
     if dist.rank == 0 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(args)
         line["parity"] = line["cpu_baseline"]["gpu_parity"]["parity"]
-    job.close()
-    ctx.close()
+    # the metric's other halves: batched against plain on the batching configuration, and job latency
+    # under Poisson arrivals (rank 0 only: each is a single-GPU measurement)
+    if dist.rank == 0 and not args.no_batch:
+        b = batch_measure(args, dev, args.sample_scale)
+        line["batch"] = b
+        for kk in ("plain_bases_per_s", "batched_bases_per_s", "batched_over_plain"):
+            line[kk] = b[kk]
+    if dist.rank == 0 and args.serve_seconds > 0:
+        r = serve_measure(args, dev, args.serve_seconds)
+        line["serve"] = r
+        line["p50_ms"] = r["p50_ms"]
+        line["p99_ms"] = r["p99_ms"]
     if dist.rank == 0:
         print(json.dumps(line), flush=True)
     dist.close()
@@ -386,17 +407,14 @@ def _request_params(args, spec, chunks=None):
     return serve.RequestParams(args.k, 0, 1, args.threads, chunks or args.chunks, 0)
 
 
-def serve_mode(args, dist):
-    """Poisson arrivals of partition requests into the request loop; p50/p99 latency and bases/s."""
+def serve_measure(args, dev: int, duration: float) -> dict:
+    """Poisson arrivals of partition requests into the request loop (continuous admission by HBM footprint);
+    p50/p99 submit-to-done latency and bases/s over the run."""
     import random
 
     import numpy as np
     import torch
     from metapart_gb300 import native, serve, synth
-    if dist.rank != 0:
-        dist.close()
-        return
-    torch.cuda.set_device(dist.local)
     specs = synth.serving_mix(args.pool, seed=11)
     pool = []
     for sp in specs:
@@ -404,7 +422,7 @@ def serve_mode(args, dist):
         out = torch.empty(t.numel() + 64, dtype=torch.uint8, pin_memory=True)
         pool.append((sp, t, out, sp.n_reads * sp.lengths[0]))
     budget = int(args.budget_gb * (1 << 30))
-    ctx = native.Context(dist.local, hbm_budget=budget)
+    ctx = native.Context(dev, hbm_budget=budget)
     srv = serve.Server(ctx, slots=args.slots, hbm_budget=budget)
     params = [_request_params(args, sp) for sp, *_ in pool]
     # warm-up: every slot once
@@ -418,7 +436,7 @@ def serve_mode(args, dist):
     arrivals, at = [], 0.0
     while True:
         at += rng.expovariate(args.rate)
-        if at >= args.duration:
+        if at >= duration:
             break
         arrivals.append(at)
     free = list(range(len(pool)))
@@ -439,7 +457,7 @@ def serve_mode(args, dist):
             free.append(i)
             results.append((i, r))
 
-    with ClockSampler(dist.local) as clk:
+    with ClockSampler(dev) as clk:
         t0 = time.perf_counter()
         for at in arrivals:
             while True:
@@ -468,22 +486,30 @@ def serve_mode(args, dist):
     bases = sum(pool[i][3] for i, _ in results)
     span = (max(r.t_done_ms for _, r in results) - min(r.t_submit_ms for _, r in results)) / 1e3
     dev_ms = sum(r.device_ms for _, r in results)
-    line = {
-        "metric": METRIC, "mode": "serve", "value": round(bases / span, 1), "unit": "bases/s", "n_gpus": 1,
-        "steps": len(results), "warmup": len(wt), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "u64", "data": "synthetic (seeded generator, no real reads)",
-        "config": {"workload": f"Poisson arrivals, mean {args.rate}/s for {args.duration:.0f} s; requests of "
-                               f"10k-2M SE x 150 bp reads (log-uniform) from 5-50 genomes, 1% subs; "
-                               f"{len(pool)} distinct requests cycled",
-                   "k": args.k, "m": 10, "num_scans": 1, "num_threads": args.threads, "chunks": args.chunks,
-                   "slots": args.slots, "hbm_budget_gb": args.budget_gb},
+    return {
+        "workload": f"Poisson arrivals, mean {args.rate}/s for {duration:.0f} s; requests of 10k-2M SE x 150 bp reads "
+                    f"(log-uniform) from 5-50 genomes, 1% subs; {len(pool)} distinct requests cycled; k={args.k}, "
+                    f"1 scan, {args.threads} threads, {args.slots} slots, {args.budget_gb:.0f} GB admission budget",
+        "bases_per_s": round(bases / span, 1), "jobs": len(results), "jobs_per_s": round(len(results) / span, 2),
         "p50_ms": round(float(np.percentile(lat, 50)), 2), "p99_ms": round(float(np.percentile(lat, 99)), 2),
         "mean_ms": round(float(lat.mean()), 2), "queue_p50_ms": round(float(np.percentile(qms, 50)), 2),
-        "queue_p99_ms": round(float(np.percentile(qms, 99)), 2), "jobs": len(results),
-        "jobs_per_s": round(len(results) / span, 2), "device_busy": round(dev_ms / 1e3 / span, 3),
+        "queue_p99_ms": round(float(np.percentile(qms, 99)), 2), "device_busy": round(dev_ms / 1e3 / span, 3),
         "peak_running": st["peak_running"], "peak_reserved_gb": round(st["peak_reserved"] / (1 << 30), 2),
-        "pool_stalls": stalls, "clocks": clk.summary(),
+        "pool_stalls": stalls, "warmup_jobs": len(wt), "clocks": clk.summary(),
     }
+
+
+def serve_mode(args, dist):
+    if dist.rank != 0:
+        dist.close()
+        return
+    import torch
+    torch.cuda.set_device(dist.local)
+    r = serve_measure(args, dist.local, args.duration)
+    line = {"metric": METRIC, "mode": "serve", "value": r["bases_per_s"], "unit": "bases/s", "n_gpus": 1,
+            "steps": r["jobs"], "warmup": r["warmup_jobs"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u64", "data": "synthetic (seeded generator, no real reads)",
+            "config": {"workload": r["workload"]}, **{kk: v for kk, v in r.items() if kk != "workload"}}
     print(json.dumps(line), flush=True)
     dist.close()
 
@@ -498,49 +524,44 @@ def _checksum(t, n: int) -> tuple:
     return int(w.sum()), int(w[::2].sum()), int(w[1::3].sum()), tail
 
 
-def batch_mode(args, dist):
-    """Independent samples partitioned one after another through one job (plain) and queued together in the
-    request loop (batched); both from pinned host FASTQ to partition files on the host."""
+def batch_measure(args, dev: int, scale: float) -> dict:
+    """The batching configuration: independent samples (read counts log-uniform 50k-5M x scale, lengths in
+    {100, 150, 250}) from pinned host FASTQ to partition files in pinned host memory, (a) plain: one after
+    another through one job, every stage per sample, (b) batched: all of them through mp_batch_run.  The two
+    runs' partition files are compared, and two samples' files with the CPU oracle's."""
     import numpy as np
     import torch
-    from metapart_gb300 import native, serve, synth
-    if dist.rank != 0:
-        dist.close()
-        return
-    torch.cuda.set_device(dist.local)
-    specs = synth.batch_mix(args.samples, seed=5, scale=args.sample_scale)
+    from metapart_gb300 import native, synth
+    specs = synth.batch_mix(args.samples, seed=5, scale=scale)
     ins = [synth.fastq_to(sp, _pinned) for sp in specs]
     outs = [torch.empty(t.numel() + 64, dtype=torch.uint8, pin_memory=True) for t in ins]
     bases = sum(sp.n_reads * sp.lengths[0] for sp in specs)
     budget = int(args.budget_gb * (1 << 30))
-    ctx = native.Context(dist.local, hbm_budget=budget)
-    params = [_request_params(args, sp) for sp in specs]
+    ctx = native.Context(dev, hbm_budget=budget)
+    T, chunks = args.threads, args.chunks
+    fsz = [np.zeros(16 * T, dtype=np.uint64) for _ in specs]
 
     def plain_all():
-        job = native.Job(ctx)
-        sizes = []
-        try:
-            for t, o, p in zip(ins, outs, params):
+        res = []
+        with native.Job(ctx) as job:
+            for t, o in zip(ins, outs):
                 job.reset()
-                f, ofs = native.fastq_index_ptr(p.num_chunks, t.data_ptr(), t.numel())
+                f, ofs = native.fastq_index_ptr(chunks, t.data_ptr(), t.numel())
                 st = native.chunk_starts_of(f, ofs, [t.numel()])
-                cnt = job.load_count(t.data_ptr(), t.numel(), p.k, st)
-                bnd = job.partition(p.k, p.num_scans, p.num_threads, st, cnt.chunk_first_read, cnt.hist)
+                cnt = job.load_count(t.data_ptr(), t.numel(), args.k, st)
+                bnd = job.partition(args.k, 1, T, st, cnt.chunk_first_read, cnt.hist)
                 job.output_plan()
-                sizes.append((job.output_to(o.data_ptr(), o.numel()), bnd.tolist()))
-        finally:
-            job.close()
-        return sizes
+                res.append((job.output_to(o.data_ptr(), o.numel()), bnd.tolist()))
+        return res
 
-    def batched_all(srv):
-        tks = [srv.submit(t.data_ptr(), t.numel(), p, o.data_ptr(), o.numel()) for t, o, p in zip(ins, outs, params)]
-        res = [srv.result(x) for x in tks]
-        bad = [r for r in res if r.status]
-        if bad:
-            raise RuntimeError(f"batched sample failed: {bad[0].error}")
-        return [(r.out_total, r.bounds) for r in res]
+    batch = native.Batch(ctx)
+    samples = [native.SampleIn(t.data_ptr(), t.numel(), chunks, T, o.data_ptr(), o.numel(), f)
+               for t, o, f in zip(ins, outs, fsz)]
 
-    with ClockSampler(dist.local) as clk:
+    def batched_all():
+        return [(r["out_total"], r["bounds"].tolist()) for r in batch.run(args.k, samples)]
+
+    with ClockSampler(dev) as clk:
         plain_all()  # warm-up
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -548,30 +569,66 @@ def batch_mode(args, dist):
         torch.cuda.synchronize()
         plain_s = time.perf_counter() - t0
         digest_plain = [_checksum(o, n) for o, (n, _) in zip(outs, want)]
-        with serve.Server(ctx, slots=args.slots, hbm_budget=budget) as srv:
-            batched_all(srv)  # warm-up
-            torch.cuda.synchronize()
-            t0 = time.perf_counter()
-            got = batched_all(srv)
-            torch.cuda.synchronize()
-            batched_s = time.perf_counter() - t0
-            st = srv.stats()
+        batched_all()  # warm-up
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        got = batched_all()
+        torch.cuda.synchronize()
+        batched_s = time.perf_counter() - t0
+    stage = batch.stage_ms()
+    groups = batch.groups
+    ss = batch.sort_stats()
     digest_batched = [_checksum(o, n) for o, (n, _) in zip(outs, got)]
-    same = want == got and digest_plain == digest_batched
+    # two of the smallest samples against the CPU oracle, file by file
+    oracle_ok = []
+    order = sorted(range(len(specs)), key=lambda i: specs[i].n_reads)[:2]
+    for i in order:
+        with tempfile.TemporaryDirectory() as td:
+            d = Path(td)
+            fq = d / "sample.fastq"
+            fq.write_bytes(ins[i].numpy().tobytes())
+            cores = os.cpu_count() or 1
+            cpu_run(fq, args.k, 1, T, chunks, cores)
+            off = np.concatenate([[0], np.cumsum(fsz[i])]).astype(np.int64)
+            ob = outs[i].numpy()
+            same = True
+            for part in range(16):
+                for t in range(T):
+                    j = part * T + t
+                    f = d / "out" / "Rank0" / f"FromTid{t}_ToRank{part}.paired.fastq"
+                    if ob[off[j]:off[j + 1]].tobytes() != (f.read_bytes() if f.exists() else b""):
+                        same = False
+            oracle_ok.append(same)
+    batch.close()
     ctx.close()
-    line = {
-        "metric": METRIC, "mode": "batch", "value": round(bases / batched_s, 1), "unit": "bases/s", "n_gpus": 1,
-        "steps": 1, "warmup": 1, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
-        "data": "synthetic (seeded generator, no real reads)",
-        "config": {"workload": f"{len(specs)} samples, reads log-uniform 50k-5M x {args.sample_scale} (even), "
-                               f"lengths in {{100,150,250}}, 10-100 genomes of 0.5-3 Mb, 1% subs",
-                   "k": args.k, "m": 10, "num_scans": 1, "num_threads": args.threads, "chunks": args.chunks,
-                   "slots": args.slots, "bases": bases, "reads": sum(sp.n_reads for sp in specs)},
+    return {
+        "workload": f"{len(specs)} samples, reads log-uniform 50k-5M x {scale} (even), lengths in {{100,150,250}}, "
+                    f"10-100 genomes of 0.5-3 Mb, log-normal abundance sigma 1.5, 1% subs; k={args.k}, 1 scan, "
+                    f"{T} threads, {chunks} chunks; pinned host FASTQ to pinned host partition files",
+        "bases": bases, "reads": sum(sp.n_reads for sp in specs),
         "plain_bases_per_s": round(bases / plain_s, 1), "batched_bases_per_s": round(bases / batched_s, 1),
         "batched_over_plain": round(plain_s / batched_s, 3), "plain_s": round(plain_s, 3),
-        "batched_s": round(batched_s, 3), "identical_results": bool(same), "peak_running": st["peak_running"],
+        "batched_s": round(batched_s, 3), "groups": groups,
+        "identical_to_plain": bool(want == got and digest_plain == digest_batched),
+        "oracle_samples_identical": oracle_ok,
+        "batched_stage_ms": {kk: round(v, 2) for kk, v in stage.items()},
+        "batched_sort": {"tuples": ss["tuples"], "digit_passes": ss["passes"], "digit_pass_ms": round(ss["pass_ms"], 2),
+                         "digit_pass_gbs": round(ss["bytes"] / 1e9 / (ss["pass_ms"] / 1e3), 1) if ss["pass_ms"] else None},
         "clocks": clk.summary(),
     }
+
+
+def batch_mode(args, dist):
+    if dist.rank != 0:
+        dist.close()
+        return
+    import torch
+    torch.cuda.set_device(dist.local)
+    r = batch_measure(args, dist.local, args.sample_scale)
+    line = {"metric": METRIC, "mode": "batch", "value": r["batched_bases_per_s"], "unit": "bases/s", "n_gpus": 1,
+            "steps": 1, "warmup": 1, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "u64", "data": "synthetic (seeded generator, no real reads)",
+            "config": {"workload": r["workload"]}, **{kk: v for kk, v in r.items() if kk != "workload"}}
     print(json.dumps(line), flush=True)
     dist.close()
 

@@ -162,6 +162,55 @@ int mp_sort_tuples(mp_ctx *ctx, const uint64_t *lo_in, const uint8_t *hi_in, con
 int mp_sort_tuples_noalloc(const uint64_t *lo_in, const uint8_t *hi_in, const uint32_t *id_in, uint64_t *lo_out,
                            uint8_t *hi_out, uint32_t *id_out, uint64_t n, void *stream);
 
+/* ---- Batches: many independent samples partitioned together.
+ * The reference partitions one input per process launch (metapart.c:3544-4150); this has no counterpart
+ * there.  Every sample gets exactly what mp_job_partition + mp_job_output give it alone with numScans = 1
+ * and the plain variant: the same 16 bounds, component labels and partition files.  The samples share
+ * the stages -- one upload of their bytes one after another, per-sample m-mer histograms and scan plans
+ * computed on the device, one enumeration, one sort of every sample's tuples (the sample is the most
+ * significant part of the key), one filter and union sweep over every sample's thread ranges, one mate
+ * union, one output gather -- in groups of samples sized to the context's HBM budget. */
+typedef struct mp_batch mp_batch;
+
+typedef struct {
+    int k;            /* kmerSize of every sample */
+    int interleaved;  /* 1: every sample is interleaved pairs, 0: every sample is single end */
+} mp_batch_params;
+
+typedef struct {
+    const char *fastq;     /* one FASTQ file (pinned host memory lets its upload overlap other work) */
+    uint64_t nbytes;
+    int num_chunks;        /* genFastqIdx chunks */
+    int num_threads;       /* numThreads: a divisor of the chunk count, at most 256 */
+    char *out;             /* nullable: the partition files, grouped as mp_job_output */
+    uint64_t out_cap;
+    uint64_t *file_sizes;  /* nullable: 16 x num_threads file sizes */
+    uint32_t *labels;      /* nullable: the component label of every read (the sample's own ids) */
+    uint64_t labels_cap;
+} mp_batch_sample;
+
+typedef struct {
+    int status;            /* 0 or a negative MP_E* code */
+    char error[256];
+    uint64_t n_reads;
+    uint64_t out_total;    /* partition FASTQ bytes */
+    uint64_t bounds[17];   /* the 16 work partitions' read-id bounds */
+} mp_batch_result;
+
+int mp_batch_create(mp_ctx *ctx, mp_batch **out);
+void mp_batch_destroy(mp_batch *b);
+/* Partitions every sample; returns the first failure (its message names the sample), results[] per sample. */
+int mp_batch_run(mp_batch *b, const mp_batch_params *p, int nsamples, const mp_batch_sample *samples,
+                 mp_batch_result *results);
+/* Device ms of the last run per stage, summed over its groups (the order of mp_job_stage_ms). */
+int mp_batch_stage_ms(const mp_batch *b, double *ms, int n);
+/* Groups the last run went in. */
+int mp_batch_groups(const mp_batch *b);
+/* The batch's bounded device waits, as mp_job_set_wait_limits. */
+int mp_batch_set_wait_limits(mp_batch *b, uint32_t lookback_spins, uint32_t union_retries, uint32_t mate_rounds);
+/* The last run's bucket-digit sort passes: tuples, passes, device ms and algorithmic bytes. */
+int mp_batch_sort_stats(const mp_batch *b, uint64_t *tuples, int *passes, double *pass_ms, uint64_t *bytes);
+
 /* ---- Request loop: continuous admission of partition jobs on one context.
  * The reference runs one input per MPI launch; this loop has no counterpart there.  Worker threads
  * each own one job (one CUDA stream); a request is admitted in arrival order when a worker is free
@@ -232,6 +281,14 @@ int mp_job_set_kmer_cache(mp_job *job, int enable);
  * scans are what bounds its memory (numScans, metapart.c:3720-3791), and a different numScans changes
  * the partitions; pieces inside a scan do not. */
 int mp_job_set_scan_piece_tuples(mp_job *job, uint64_t max_tuples);
+/* Iteration limits of the job's bounded device waits (0 keeps the default): the sort's decoupled
+ * look-back polls of one predecessor's status word (default 2^22), the union-find's hook retries of one
+ * union (2^20), and the mate union's rounds (4,000,000).  A wait that runs out makes the call return
+ * MP_EDEVICE with a message naming it; the job's results are then undefined, the context stays usable
+ * and a reset job runs normally.  The reference's own loops are unbounded (its edge replay,
+ * metapart.c:2736-2800); these limits have no counterpart there. */
+int mp_job_set_wait_limits(mp_job *job, uint32_t lookback_spins, uint32_t union_retries, uint32_t mate_rounds);
+
 /* Bucket-range pieces the last mp_job_partition ran its scans in, summed over the scans (numScans when
  * no scan was split).  Tracing only. */
 int mp_job_scan_pieces(const mp_job *job);

@@ -33,7 +33,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC = os.environ.get("NVCC", shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc")
 CUDA_HOME = Path(NVCC).resolve().parent.parent
 
-CU_SOURCES = ["mp_api.cu", "mp_server.cu", "k_reads.cu", "k_kmers.cu", "k_sort.cu", "k_graph.cu", "k_output.cu"]
+CU_SOURCES = ["mp_api.cu", "mp_batch.cu", "mp_server.cu", "k_reads.cu", "k_kmers.cu", "k_sort.cu", "k_graph.cu", "k_output.cu"]
 CLI_PROGRAMS = {
     "genFastqIdx": ("genFastqIdx.c", []),
     "genHistograms_metapart": ("genHistograms.c", []),

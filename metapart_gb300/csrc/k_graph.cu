@@ -117,9 +117,12 @@ __global__ void __launch_bounds__(256) k_filter_warp(const uint64_t *lo, const u
                                                      uint64_t n, const uint64_t *range_ends, int T, uint32_t *parent,
                                                      uint8_t *filtered, uint32_t *z)
 {
-    __shared__ uint64_t ends[256];
-    for (int t = threadIdx.x; t < T; t += blockDim.x) ends[t] = range_ends[t];
+    __shared__ uint64_t ends_s[256];
+    const bool in_smem = T <= 256;  // many ranges (a batch of samples) are read from global memory
+    if (in_smem)
+        for (int t = threadIdx.x; t < T; t += blockDim.x) ends_s[t] = range_ends[t];
     __syncthreads();
+    const uint64_t *ends = in_smem ? ends_s : range_ends;
     const int lane = threadIdx.x & 31;
     const uint64_t c0 = (((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * SEG;
     if (c0 >= n) return;
@@ -171,7 +174,8 @@ __global__ void __launch_bounds__(256) k_filter_warp(const uint64_t *lo, const u
             pk = prev_km;
             pa = prev_adj;
         }
-        const bool head = valid && (i == 0 || km != pk);
+        // a thread range starts a run whatever the k-mer before it (each range is its own sweep)
+        const bool head = valid && (i == 0 || km != pk || ((emask >> lane) & 1u));
         const uint32_t H = __ballot_sync(FULLW, head), V = __ballot_sync(FULLW, valid);
         const uint32_t D = __ballot_sync(FULLW, valid && !head && adj != pa);
         const uint32_t run_adj = prev_adj;  // byte of a uniform carried run
@@ -311,9 +315,9 @@ __device__ __forceinline__ void uf_find2(uint32_t *parent, uint32_t &x, uint32_t
     }
 }
 
-__device__ __forceinline__ void uf_union(uint32_t *parent, uint32_t a, uint32_t b, uint32_t *err)
+__device__ __forceinline__ void uf_union(uint32_t *parent, uint32_t a, uint32_t b, uint32_t *err, uint32_t cap)
 {
-    for (uint32_t it = 0; it < UF_CAP; it++) {
+    for (uint32_t it = 0; it < cap; it++) {
         uint32_t ra = a, rb = b;
         uf_find2(parent, ra, rb);
         if (ra == rb) return;
@@ -341,15 +345,20 @@ struct EdgeCtx {
     const uint32_t *id;
     const uint32_t *z;             // zero marks of the filter
     uint64_t n;
-    const uint64_t *first_valid;   // per thread range
+    const uint64_t *first_valid;   // per thread range (~0: none)
     const uint64_t *range_bounds;  // T + 1 tuple bounds
     int T;
     uint64_t init_kmer;            // k-mer of the scan's last tuple after the filter (metapart.c:2541)
     uint32_t init_min;             // read id of the scan's first tuple (metapart.c:2543-2545)
     uint32_t init_min_ok;          // that read is not BAD
+    // per thread range instead (a batch of samples, each its own scan); nullable
+    const uint64_t *r_kmer;
+    const uint32_t *r_min;
+    const uint32_t *r_ok;
     uint32_t *parent;
     const uint8_t *filtered;       // BAD flags: during the scans a read's parent is BAD exactly when it is flagged
     uint32_t *err;
+    uint32_t uf_cap;               // hook retries of one union before it gives up (DERR_SPIN)
 };
 
 // unionFindPar2 (metapart.c:2537-2727): in each run of equal k-mers the first valid tuple
@@ -367,6 +376,23 @@ __global__ void __launch_bounds__(256) k_edges_warp(EdgeCtx c)
     const uint32_t le = (lane == 31) ? FULLW : ((2u << lane) - 1);
     bool open = false, has_anchor = false;
     uint32_t anchor = 0;
+    // cursors over the thread ranges: their starts (run heads) and their first valid tuples (the positions
+    // where a range's sweep may take the scan's initial state); both ascend with the range index
+    int nb, nf;
+    {
+        int a = 1, b = c.T;  // first t in [1, T] with range_bounds[t] >= c0 (T when none)
+        while (a < b) {
+            const int m = (a + b) >> 1;
+            if (c.range_bounds[m] < c0) a = m + 1; else b = m;
+        }
+        nb = a;
+        a = 0, b = c.T - 1;  // the range holding c0: ranges before it have their first valid tuple below c0
+        while (a < b) {
+            const int m = (a + b + 1) >> 1;
+            if (c.range_bounds[m] <= c0) a = m; else b = m - 1;
+        }
+        nf = a;
+    }
     uint64_t prev_km = c0 ? kmer_of(c.lo, c.hi, c0 - 1) : 0;
     // the next window's k-mer, read id and zero-mark word (windows start at multiples of 32), loaded one
     // window ahead
@@ -386,9 +412,24 @@ __global__ void __launch_bounds__(256) k_edges_warp(EdgeCtx c)
             }
             nzw = c.z[(p + 32) >> 5];
         }
+        uint32_t smask = 0, fmask = 0;  // lanes at a range start, lanes at a range's first valid tuple
+        int my_t = 0;                   // the range whose first valid tuple this lane holds
+        while (nb < c.T && c.range_bounds[nb] < p + 32) {
+            if (c.range_bounds[nb] >= p) smask |= 1u << (c.range_bounds[nb] - p);
+            nb++;
+        }
+        while (nf < c.T) {
+            const uint64_t f = c.first_valid[nf];
+            if (f != ~0ull && f >= p + 32) break;
+            if (f != ~0ull && f >= p) {
+                fmask |= 1u << (f - p);
+                if ((uint64_t)lane == f - p) my_t = nf;
+            }
+            nf++;
+        }
         uint64_t pk = __shfl_up_sync(FULLW, km, 1);
         if (lane == 0) pk = prev_km;
-        const bool head = valid && (i == 0 || km != pk);
+        const bool head = valid && (i == 0 || km != pk || ((smask >> lane) & 1u));
         const uint32_t H = __ballot_sync(FULLW, head);
         prev_km = __shfl_sync(FULLW, km, 31);
         const bool nz = valid && km != 0 && !((zw >> lane) & 1u);
@@ -409,13 +450,10 @@ __global__ void __launch_bounds__(256) k_edges_warp(EdgeCtx c)
         // quirk check by the lane holding a run's first good tuple when the run has no anchor yet
         uint32_t aval = r;
         bool quirk = false;
-        if (good && lane == fg && !(carried && has_anchor) && km == c.init_kmer && c.init_min_ok) {
-            int lo = 0, hi = c.T - 1;
-            while (lo < hi) {
-                int m = (lo + hi + 1) >> 1;
-                if (c.range_bounds[m] <= i) lo = m; else hi = m - 1;
-            }
-            if (c.first_valid[lo] == i) { quirk = true; aval = c.init_min; }
+        if (good && lane == fg && !(carried && has_anchor) && ((fmask >> lane) & 1u)) {
+            const uint64_t ik = c.r_kmer ? c.r_kmer[my_t] : c.init_kmer;
+            const bool ok = c.r_ok ? c.r_ok[my_t] != 0 : c.init_min_ok != 0;
+            if (km == ik && ok) { quirk = true; aval = c.r_min ? c.r_min[my_t] : c.init_min; }
         }
         const uint32_t av = __shfl_sync(FULLW, aval, fg < 0 ? 0 : fg);
         const bool qk = __shfl_sync(FULLW, quirk, fg < 0 ? 0 : fg);
@@ -431,7 +469,7 @@ __global__ void __launch_bounds__(256) k_edges_warp(EdgeCtx c)
                 if (lane != fg || qk) { do_union = true; target = av; }
             }
         }
-        if (do_union && target != r) uf_union(c.parent, target, r, c.err);
+        if (do_union && target != r) uf_union(c.parent, target, r, c.err, c.uf_cap);
         // carried run bookkeeping
         if (open) {
             if (!has_anchor) {
@@ -690,6 +728,10 @@ int union_scan(Tuples &tp, const std::vector<uint64_t> &range_bounds, uint32_t *
         c.init_kmer = ((zw >> ((n - 1) & 31)) & 1u) ? 0 : ((last_lo >> 8) | ((uint64_t)last_hi << 56));
         c.init_min = first_id;
         c.init_min_ok = first_parent != BAD;
+        c.r_kmer = nullptr;
+        c.r_min = nullptr;
+        c.r_ok = nullptr;
+        c.uf_cap = arena.lim.union_retries;
         (mp::count_launch(), k_range_first_valid<<<blocks_for(T, 64), 64, 0, st>>>(tp.lo, tp.hi, tp.id, tp.z, bounds, T, parent,
                                                                                   first));
         const uint64_t warps = (n + SEG - 1) / SEG;
@@ -734,6 +776,10 @@ int union_piece(Tuples &tp, const std::vector<uint64_t> &bounds, const std::vect
     c.init_kmer = init_kmer;
     c.init_min = init_min;
     c.init_min_ok = init_min_ok ? 1u : 0u;
+    c.r_kmer = nullptr;
+    c.r_min = nullptr;
+    c.r_ok = nullptr;
+    c.uf_cap = arena.lim.union_retries;
     const uint64_t warps = (n + SEG - 1) / SEG;
     (mp::count_launch(), k_edges_warp<<<blocks_for(warps * 32, 256), 256, 0, st>>>(c));
     uint32_t herr = 0;
@@ -751,6 +797,12 @@ void compress_parents(uint32_t *parent, uint64_t n_reads, cudaStream_t st)
 
 int mate_union_and_plan(uint32_t *parent, uint64_t n_reads, uint32_t *size, uint64_t *bounds_out, DeviceArena &arena,
                         cudaStream_t st, int *rounds_out)
+{
+    int rc = mate_union(parent, n_reads, size, arena, st, rounds_out);
+    return rc ? rc : plan_partitions(parent, size, n_reads, bounds_out, arena, st);
+}
+
+int mate_union(uint32_t *parent, uint64_t n_reads, uint32_t *size, DeviceArena &arena, cudaStream_t st, int *rounds_out)
 {
     const uint32_t limit = 1000;
     const uint64_t npairs = n_reads / 2;
@@ -775,7 +827,8 @@ int mate_union_and_plan(uint32_t *parent, uint64_t n_reads, uint32_t *size, uint
     (mp::count_launch(), k_pe_prepare<<<blocks_for(n_reads, 256), 256, 0, st>>>(parent, n_reads, act, npairs));
     uint32_t nact = (uint32_t)npairs, round = 0;
     while (nact > 0) {
-        if (round + RB > 4000000u) return set_error(MP_EDEVICE, "mate union did not converge");
+        if (round + RB > arena.lim.mate_rounds)
+            return set_error(MP_EDEVICE, "mate union did not converge within %u rounds", arena.lim.mate_rounds);
         // counts only shrink, so nact bounds every list of the batch
         const unsigned g = (unsigned)std::min<uint64_t>(blocks_for(nact, 256), 8ull * (uint64_t)sm_count());
         MP_CUDA(cudaMemsetAsync(cnts, 0, (4 * RB + 4) * sizeof(unsigned int), st));
@@ -807,7 +860,7 @@ int mate_union_and_plan(uint32_t *parent, uint64_t n_reads, uint32_t *size, uint
     (mp::count_launch(), k_compress<<<blocks_for(n_reads, 256), 256, 0, st>>>(parent, n_reads));
     MP_CUDA(cudaMemsetAsync(size, 0, n_reads * sizeof(uint32_t), st));
     (mp::count_launch(), k_sizes<<<blocks_for(n_reads, 256), 256, 0, st>>>(parent, n_reads, size));
-    return plan_partitions(parent, size, n_reads, bounds_out, arena, st);
+    return 0;
 }
 
 // Work partitions (metapart.c:4036-4053): bound i = first read id c at which the sizes of
@@ -846,6 +899,115 @@ int plan_partitions(const uint32_t *parent, const uint32_t *size, uint64_t n_rea
     scan_u32_to_u64(w, pre, n_reads + 1, nullptr, tmp, tb, st);
     (mp::count_launch(), k_bounds<<<1, 32, 0, st>>>(pre, n_reads, b));
     MP_CUDA(cudaMemcpyAsync(bounds_host, b, 17 * sizeof(uint64_t), cudaMemcpyDeviceToHost, st));
+    MP_CUDA(cudaStreamSynchronize(st));
+    MP_CUDA(cudaGetLastError());
+    return 0;
+}
+
+// ------------------------------------------------------ batches of samples
+
+// The initial sweep state of every thread range of a batch: its sample's scan's last k-mer (after the
+// filter's zero marks), first read, and whether that read is BAD as the unions begin (metapart.c:2539-2548).
+__global__ void k_seg_union_init(const uint64_t *lo, const uint8_t *hi, const uint32_t *id, const uint32_t *z,
+                                 const uint64_t *seg_tstart, const uint32_t *range_seg, int nranges, const uint32_t *parent,
+                                 uint64_t *r_kmer, uint32_t *r_min, uint32_t *r_ok)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nranges) return;
+    const uint32_t q = range_seg[t];
+    const uint64_t a = seg_tstart[q], b = seg_tstart[q + 1];
+    if (a == b) {  // a sample without tuples: its ranges are empty
+        r_kmer[t] = 0;
+        r_min[t] = 0;
+        r_ok[t] = 0;
+        return;
+    }
+    const uint64_t last = b - 1;
+    r_kmer[t] = zbit(z, last) ? 0ull : kmer_of(lo, hi, last);
+    const uint32_t f = id[a];
+    r_min[t] = f;
+    r_ok[t] = parent[f] != BAD ? 1u : 0u;
+}
+
+int union_segments(Tuples &tp, const std::vector<uint64_t> &range_bounds, const std::vector<uint32_t> &range_seg,
+                   const std::vector<uint64_t> &seg_tstart, uint32_t *parent, const uint8_t *filtered, uint64_t n_reads,
+                   DeviceArena &arena, cudaStream_t st)
+{
+    const uint64_t n = tp.n;
+    const int R = (int)range_bounds.size() - 1, nseg = (int)seg_tstart.size() - 1;
+    uint32_t *err = arena.alloc<uint32_t>(1);
+    if (!err) return set_error(MP_ENOMEM, "device memory");
+    MP_CUDA(cudaMemsetAsync(err, 0, sizeof *err, st));
+    if (n) {
+        uint64_t *bounds = arena.alloc<uint64_t>(R + 1), *first = arena.alloc<uint64_t>(R), *ts = arena.alloc<uint64_t>(nseg + 1);
+        uint64_t *rk = arena.alloc<uint64_t>(R);
+        uint32_t *rs = arena.alloc<uint32_t>(R), *rm = arena.alloc<uint32_t>(R), *ro = arena.alloc<uint32_t>(R);
+        if (!bounds || !first || !ts || !rk || !rs || !rm || !ro) return set_error(MP_ENOMEM, "device memory for union-find");
+        MP_CUDA(cudaMemcpyAsync(bounds, range_bounds.data(), (R + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, st));
+        MP_CUDA(cudaMemcpyAsync(rs, range_seg.data(), R * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+        MP_CUDA(cudaMemcpyAsync(ts, seg_tstart.data(), (nseg + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, st));
+        (mp::count_launch(), k_seg_union_init<<<blocks_for(R, 128), 128, 0, st>>>(tp.lo, tp.hi, tp.id, tp.z, ts, rs, R, parent,
+                                                                                 rk, rm, ro));
+        (mp::count_launch(), k_range_first_valid<<<blocks_for(R, 64), 64, 0, st>>>(tp.lo, tp.hi, tp.id, tp.z, bounds, R, parent,
+                                                                                  first));
+        EdgeCtx c;
+        c.lo = tp.lo; c.hi = tp.hi; c.id = tp.id; c.z = tp.z; c.n = n;
+        c.first_valid = first; c.range_bounds = bounds; c.T = R; c.parent = parent; c.filtered = filtered; c.err = err;
+        c.init_kmer = 0;
+        c.init_min = 0;
+        c.init_min_ok = 0;
+        c.r_kmer = rk;
+        c.r_min = rm;
+        c.r_ok = ro;
+        c.uf_cap = arena.lim.union_retries;
+        const uint64_t warps = (n + SEG - 1) / SEG;
+        (mp::count_launch(), k_edges_warp<<<blocks_for(warps * 32, 256), 256, 0, st>>>(c));
+    }
+    (mp::count_launch(), k_compress<<<blocks_for(n_reads, 256), 256, 0, st>>>(parent, n_reads));
+    uint32_t herr = 0;
+    MP_CUDA(cudaMemcpyAsync(&herr, err, sizeof herr, cudaMemcpyDeviceToHost, st));
+    MP_CUDA(cudaStreamSynchronize(st));
+    MP_CUDA(cudaGetLastError());
+    if (herr) return set_error(MP_EDEVICE, "union-find retry limit reached (flags 0x%x)", herr);
+    return 0;
+}
+
+// The 16 work partitions of every sample of a batch (metapart.c:4036-4053 per sample): bounds in the
+// sample's own read ids, from the prefix of root weights over all reads.
+__global__ void k_seg_bounds(const uint64_t *pre, const uint64_t *srec, int nseg, uint64_t *bounds)
+{
+    const int q = blockIdx.x, i = threadIdx.x;
+    if (q >= nseg || i > 16) return;
+    const uint64_t R = srec[q], N = srec[q + 1] - R;
+    uint64_t *b = bounds + (uint64_t)q * 17;
+    if (i == 0) { b[0] = 0; return; }
+    if (i == 16) { b[16] = N; return; }
+    const uint64_t thr = (uint64_t)i * (N / 16), base = pre[R];
+    uint64_t lo = 0, hi = N;  // smallest c in [0, N] with the weights of reads R .. R + c - 1 reaching thr
+    while (lo < hi) {
+        const uint64_t m = (lo + hi) / 2;
+        if (pre[R + m] - base >= thr) hi = m; else lo = m + 1;
+    }
+    b[i] = lo;
+}
+
+int plan_partitions_segments(const uint32_t *parent, const uint32_t *size, uint64_t n_reads,
+                             const std::vector<uint64_t> &seg_reads, uint64_t *bounds_host, DeviceArena &arena,
+                             cudaStream_t st)
+{
+    const int nseg = (int)seg_reads.size() - 1;
+    uint32_t *w = arena.alloc<uint32_t>(n_reads + 1);
+    uint64_t *pre = arena.alloc<uint64_t>(n_reads + 1), *srec = arena.alloc<uint64_t>(nseg + 1);
+    uint64_t *b = arena.alloc<uint64_t>((size_t)nseg * 17);
+    size_t tb = scan_tmp_bytes(n_reads + 1);
+    void *tmp = arena.alloc<uint8_t>(tb);
+    if (!w || !pre || !srec || !b || !tmp) return set_error(MP_ENOMEM, "device memory for the partition planner");
+    MP_CUDA(cudaMemsetAsync(w + n_reads, 0, sizeof(uint32_t), st));
+    MP_CUDA(cudaMemcpyAsync(srec, seg_reads.data(), (nseg + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, st));
+    (mp::count_launch(), k_root_weight<<<blocks_for(n_reads, 256), 256, 0, st>>>(parent, size, n_reads, w));
+    scan_u32_to_u64(w, pre, n_reads + 1, nullptr, tmp, tb, st);
+    (mp::count_launch(), k_seg_bounds<<<nseg, 32, 0, st>>>(pre, srec, nseg, b));
+    MP_CUDA(cudaMemcpyAsync(bounds_host, b, (size_t)nseg * 17 * sizeof(uint64_t), cudaMemcpyDeviceToHost, st));
     MP_CUDA(cudaStreamSynchronize(st));
     MP_CUDA(cudaGetLastError());
     return 0;

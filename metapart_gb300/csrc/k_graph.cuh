@@ -33,7 +33,21 @@ void compress_parents(uint32_t *parent, uint64_t n_reads, cudaStream_t st);
 // K6: sizes, unionFindPeReads(1000), final compression and the 17 partition bounds (host).
 int mate_union_and_plan(uint32_t *parent, uint64_t n_reads, uint32_t *size, uint64_t *bounds_out, DeviceArena &arena,
                         cudaStream_t st, int *rounds_out);
+// The same without the partition bounds (sizes recounted after the final compression).
+int mate_union(uint32_t *parent, uint64_t n_reads, uint32_t *size, DeviceArena &arena, cudaStream_t st, int *rounds_out);
 int plan_partitions(const uint32_t *parent, const uint32_t *size, uint64_t n_reads, uint64_t *bounds_host,
                     DeviceArena &arena, cudaStream_t st);
+
+// Batches of samples, one after another in the tuple array and the read ids (every sample one scan).
+// K5 for all of them: range_bounds = R + 1 tuple bounds of every sample's thread ranges in order,
+// range_seg[t] = the sample of range t, seg_tstart = nseg + 1 tuple offsets of the samples.
+int union_segments(Tuples &tp, const std::vector<uint64_t> &range_bounds, const std::vector<uint32_t> &range_seg,
+                   const std::vector<uint64_t> &seg_tstart, uint32_t *parent, const uint8_t *filtered, uint64_t n_reads,
+                   DeviceArena &arena, cudaStream_t st);
+// The 16 work partitions of every sample (seg_reads: nseg + 1 read offsets); bounds_host: nseg x 17, in
+// each sample's own read ids.
+int plan_partitions_segments(const uint32_t *parent, const uint32_t *size, uint64_t n_reads,
+                             const std::vector<uint64_t> &seg_reads, uint64_t *bounds_host, DeviceArena &arena,
+                             cudaStream_t st);
 
 }  // namespace mp

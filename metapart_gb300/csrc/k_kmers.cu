@@ -526,7 +526,7 @@ void launch_count(const uint8_t *fq, const ParsedReads &pr, int k, int min3, con
     else
         (mp::count_launch(), k_count_plain<<<grid_for(pr.n_reads, 8), 256, 0, st>>>(fq, pr.seq_off, pr.seq_len, 0, pr.n_reads, k, chunk_rec,
                                                                nchunks, cc, glob, err, kc_off, kc_lo, kc_hi));
-    if (cc) (mp::count_launch(), k_sum_chunks<<<NB / 256, 256, 0, st>>>(cc, nchunks, glob));
+    if (cc && glob) (mp::count_launch(), k_sum_chunks<<<NB / 256, 256, 0, st>>>(cc, nchunks, glob));
 }
 
 void launch_enum_count(const uint8_t *fq, const ParsedReads &pr, int k, int min3, uint32_t lo, uint32_t hi,

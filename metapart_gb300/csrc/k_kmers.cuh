@@ -4,7 +4,7 @@
 namespace mp {
 
 // K1: bucket counts.  cc (nullable): per-chunk u32 counts [nchunks][NB]; glob: u64 counts [NB]
-// (summed from cc when cc is given).
+// (summed from cc when cc is given; nullable with cc).
 // kc_off/kc_lo/kc_hi (nullable, plain variant only): the k-mer cache to fill (see k_kc_*).
 void launch_count(const uint8_t *fq, const ParsedReads &pr, int k, int min3, const uint64_t *chunk_rec, int nchunks,
                   uint32_t *cc, unsigned long long *glob, uint32_t *err, cudaStream_t st, const uint64_t *kc_off = nullptr,

@@ -208,6 +208,154 @@ int plan_output(const uint8_t *d_fq, const ParsedReads &pr, const uint32_t *d_la
     return 0;
 }
 
+// ------------------------------------------------------ batches of samples
+
+// Samples one after another in the read ids; sample q's files are the global files file0[q] + j.
+struct BatchOutCtx {
+    const uint32_t *label;
+    const uint64_t *srec;       // nseg + 1 read offsets
+    const uint64_t *bounds;     // nseg x 17, each sample's own read ids
+    const uint64_t *chunk_rec;  // every sample's nchunks + 1 chunk record starts (its own read ids), one after another
+    const uint32_t *chunk0;     // nseg + 1: where each sample's chunk records start in chunk_rec
+    const uint32_t *T, *per_thread, *file0;  // per sample
+    int nseg, interleaved;
+    uint64_t units;
+};
+
+__device__ __forceinline__ uint32_t seg_of(const uint64_t *srec, int nseg, uint64_t r)
+{
+    int lo = 0, hi = nseg - 1;  // the last sample starting at or below r
+    while (lo < hi) {
+        const int m = (lo + hi + 1) >> 1;
+        if (srec[m] <= r) lo = m; else hi = m - 1;
+    }
+    return (uint32_t)lo;
+}
+
+__global__ void k_outb_dest(BatchOutCtx c, uint32_t *nent, uint32_t *f1, uint32_t *f2)
+{
+    const uint64_t u = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (u >= c.units) return;
+    const uint64_t r = c.interleaved ? 2 * u : u;
+    const uint32_t q = seg_of(c.srec, c.nseg, r);
+    const uint64_t R = c.srec[q], lr = r - R;
+    const uint64_t *cr = c.chunk_rec + c.chunk0[q];
+    int lo = 0, hi = (int)(c.chunk0[q + 1] - c.chunk0[q]) - 2;  // the sample's chunk holding lr
+    while (lo < hi) {
+        const int m = (lo + hi + 1) >> 1;
+        if (cr[m] <= lr) lo = m; else hi = m - 1;
+    }
+    const uint32_t t = (uint32_t)lo / c.per_thread[q], T = c.T[q];
+    const uint64_t *b = c.bounds + (uint64_t)q * 17;
+    const uint32_t pu = c.label[r];
+    f1[u] = c.file0[q] + part_of(b, (uint32_t)(pu - R)) * T + t;
+    uint32_t ne = 1;
+    if (c.interleaved) {
+        const uint32_t pv = c.label[r + 1];
+        if (pu != pv) {
+            f2[u] = c.file0[q] + part_of(b, (uint32_t)(pv - R)) * T + t;
+            ne = 2;
+        }
+    }
+    nent[u] = ne;
+}
+
+int plan_output_batch(const ParsedReads &pr, const uint32_t *d_label, int interleaved, const std::vector<uint64_t> &seg_reads,
+                      const std::vector<uint64_t> &bounds_host, const std::vector<std::vector<uint64_t>> &chunk_rec_host,
+                      const std::vector<int> &T, OutputPlan *plan, std::vector<uint64_t> &file_sizes,
+                      std::vector<uint64_t> &file0, DeviceArena &arena, cudaStream_t st)
+{
+    const int nseg = (int)seg_reads.size() - 1;
+    const uint64_t units = interleaved ? pr.n_reads / 2 : pr.n_reads;
+    std::vector<uint32_t> c0(nseg + 1, 0), hT(nseg), hpt(nseg), hf0(nseg);
+    std::vector<uint64_t> crec;
+    file0.assign(nseg + 1, 0);
+    for (int q = 0; q < nseg; q++) {
+        const int nch = (int)chunk_rec_host[q].size() - 1;
+        if (nch < 1 || T[q] < 1 || nch % T[q]) return set_error(MP_EARG, "sample %d: numThreads must divide its chunks", q);
+        c0[q] = (uint32_t)crec.size();
+        crec.insert(crec.end(), chunk_rec_host[q].begin(), chunk_rec_host[q].end());
+        hT[q] = (uint32_t)T[q];
+        hpt[q] = (uint32_t)(nch / T[q]);
+        hf0[q] = (uint32_t)file0[q];
+        file0[q + 1] = file0[q] + 16ull * (uint64_t)T[q];
+    }
+    c0[nseg] = (uint32_t)crec.size();
+    const uint64_t nf = file0[nseg];
+    file_sizes.assign(nf, 0);
+    uint64_t *srec = arena.alloc<uint64_t>(nseg + 1), *bnd = arena.alloc<uint64_t>((size_t)nseg * 17);
+    uint64_t *dcr = arena.alloc<uint64_t>(crec.size());
+    uint32_t *dc0 = arena.alloc<uint32_t>(nseg + 1), *dT = arena.alloc<uint32_t>(nseg), *dpt = arena.alloc<uint32_t>(nseg),
+             *df0 = arena.alloc<uint32_t>(nseg);
+    uint32_t *nent = arena.alloc<uint32_t>(units + 1), *f1 = arena.alloc<uint32_t>(units + 1),
+             *f2 = arena.alloc<uint32_t>(units + 1);
+    uint64_t *eoff = arena.alloc<uint64_t>(units + 1), *ntot = arena.alloc<uint64_t>(1);
+    unsigned long long *fbytes = arena.alloc<unsigned long long>(nf);
+    size_t tb = scan_tmp_bytes(2 * units + 2);
+    void *tmp = arena.alloc<uint8_t>(tb);
+    if (!srec || !bnd || !dcr || !dc0 || !dT || !dpt || !df0 || !nent || !f1 || !f2 || !eoff || !ntot || !fbytes || !tmp)
+        return set_error(MP_ENOMEM, "device memory for the output gather");
+    MP_CUDA(cudaMemcpyAsync(srec, seg_reads.data(), (nseg + 1) * 8, cudaMemcpyHostToDevice, st));
+    MP_CUDA(cudaMemcpyAsync(bnd, bounds_host.data(), (size_t)nseg * 17 * 8, cudaMemcpyHostToDevice, st));
+    MP_CUDA(cudaMemcpyAsync(dcr, crec.data(), crec.size() * 8, cudaMemcpyHostToDevice, st));
+    MP_CUDA(cudaMemcpyAsync(dc0, c0.data(), (nseg + 1) * 4, cudaMemcpyHostToDevice, st));
+    MP_CUDA(cudaMemcpyAsync(dT, hT.data(), nseg * 4, cudaMemcpyHostToDevice, st));
+    MP_CUDA(cudaMemcpyAsync(dpt, hpt.data(), nseg * 4, cudaMemcpyHostToDevice, st));
+    MP_CUDA(cudaMemcpyAsync(df0, hf0.data(), nseg * 4, cudaMemcpyHostToDevice, st));
+    MP_CUDA(cudaMemsetAsync(fbytes, 0, nf * sizeof(unsigned long long), st));
+    BatchOutCtx bc;
+    bc.label = d_label;
+    bc.srec = srec;
+    bc.bounds = bnd;
+    bc.chunk_rec = dcr;
+    bc.chunk0 = dc0;
+    bc.T = dT;
+    bc.per_thread = dpt;
+    bc.file0 = df0;
+    bc.nseg = nseg;
+    bc.interleaved = interleaved;
+    bc.units = units;
+    OutCtx c{};
+    c.rec_start = pr.rec_start;
+    c.interleaved = interleaved;
+    c.units = units;
+    const unsigned gb = (unsigned)((units + 255) / 256);
+    if (units) (mp::count_launch(), k_outb_dest<<<gb, 256, 0, st>>>(bc, nent, f1, f2));
+    scan_u32_to_u64(nent, eoff, units, ntot, tmp, tb, st);
+    uint64_t n = 0;
+    MP_CUDA(cudaMemcpyAsync(&n, ntot, sizeof n, cudaMemcpyDeviceToHost, st));
+    MP_CUDA(cudaStreamSynchronize(st));
+    SortBufs sb;
+    for (int i = 0; i < 2; i++) {
+        sb.lo[i] = arena.alloc<uint64_t>(n + 1);
+        sb.id[i] = arena.alloc<uint32_t>(n + 1);
+        if (!sb.lo[i] || !sb.id[i]) return set_error(MP_ENOMEM, "device memory for the output entries");
+    }
+    if (units) (mp::count_launch(), k_out_entries<<<gb, 256, 0, st>>>(c, f1, f2, nent, eoff, sb.lo[0], sb.id[0]));
+    int rc = radix_sort(sb, n, false, arena, st, nullptr);
+    if (rc) return rc;
+    uint64_t *len = arena.alloc<uint64_t>(n + 1);
+    plan->val = arena.alloc_persistent<uint32_t>(n + 1);
+    plan->off = arena.alloc_persistent<uint64_t>(n + 1);
+    size_t tb2 = scan_tmp_bytes(n + 1);
+    void *tmp2 = arena.alloc<uint8_t>(tb2);
+    if (!len || !plan->val || !plan->off || !tmp2) return set_error(MP_ENOMEM, "device memory for the output offsets");
+    const unsigned ge = (unsigned)((n + 255) / 256);
+    if (n) (mp::count_launch(), k_out_len<<<ge, 256, 0, st>>>(c, sb.id[sb.cur], n, len, sb.lo[sb.cur], fbytes));
+    scan_u64(len, plan->off, n, ntot, tmp2, tb2, st);
+    if (n) MP_CUDA(cudaMemcpyAsync(plan->val, sb.id[sb.cur], n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, st));
+    uint64_t total = 0;
+    MP_CUDA(cudaMemcpyAsync(&total, ntot, sizeof total, cudaMemcpyDeviceToHost, st));
+    MP_CUDA(cudaMemcpyAsync(file_sizes.data(), fbytes, nf * sizeof(uint64_t), cudaMemcpyDeviceToHost, st));
+    MP_CUDA(cudaStreamSynchronize(st));
+    MP_CUDA(cudaGetLastError());
+    plan->n = n;
+    plan->total = total;
+    plan->rec_start = pr.rec_start;
+    plan->interleaved = interleaved;
+    return 0;
+}
+
 int copy_output_range(const OutputPlan &plan, uint64_t e0, uint64_t e1, const uint8_t *d_fq, uint8_t *dst,
                       cudaStream_t st)
 {

@@ -16,6 +16,7 @@ struct DeviceArena {
     std::atomic<uint64_t> *budget_used = nullptr;  // shared with the context
     uint64_t budget_limit = ~0ull;
     uint64_t peak = 0, live = 0;
+    WaitLimits lim;  // the bounded waits of the kernels this arena's work launches
 
     void *raw(size_t bytes, bool keep)
     {

@@ -27,7 +27,6 @@ constexpr int SI = 16;
 constexpr int STILE = ST * SI;
 constexpr int SW = ST / 32;
 constexpr unsigned FULLM = 0xFFFFFFFFu;
-constexpr uint32_t SPIN_CAP = 1u << 22;
 constexpr int LB = 4;  // look-back: predecessor status words read per round
 
 struct SortSmem {
@@ -40,6 +39,9 @@ struct SortSmem {
     uint32_t wsum[SW];
     uint32_t tile_id;
     uint32_t nvalid;
+    uint32_t seg;         // segment (sample) of the tile
+    uint32_t first_tile;  // the segment's first tile: its look-back stops there
+    uint64_t base;        // the tile's first tuple
 };
 
 __device__ __forceinline__ void prefetch_l2(const void *p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
@@ -98,6 +100,17 @@ __device__ __forceinline__ uint32_t digit_of(uint64_t lo, uint32_t hi, int shift
 
 // W: ballots per tuple in the ranking, at least the digit's width w (digits are masked to w bits, so
 // the planes above w are zero in every lane and filter nothing).
+// Segments (batches of samples): the tuple array holds nseg segments one after another, each sorted on its
+// own -- seg_tstart (nseg + 1 tuple offsets) and seg_tile0 (nseg + 1 tile offsets: a segment's tiles start
+// at its first tuple, so no tile spans two segments); a tile's look-back stops at its segment's first tile
+// and its digit bases are dbase[seg * dstride + digit].  seg_tile0 == nullptr: one segment of n tuples.
+struct Segs {
+    const uint32_t *tile0 = nullptr;
+    const uint64_t *tstart = nullptr;
+    int nseg = 1;
+    uint32_t dstride = 0;
+};
+
 template <int SRC, int W = 8>
 __global__ void __launch_bounds__(ST, 3) k_onesweep(const uint64_t *__restrict__ in_lo, const uint8_t *__restrict__ in_hi,
                                                     const uint32_t *__restrict__ in_id, uint64_t *__restrict__ out_lo,
@@ -105,7 +118,7 @@ __global__ void __launch_bounds__(ST, 3) k_onesweep(const uint64_t *__restrict__
                                                     int shift, int w, const uint64_t *__restrict__ dbase,
                                                     const uint32_t *__restrict__ nzmask, unsigned long long *status,
                                                     uint32_t *tile_ctr, uint32_t epoch, uint32_t *err, uint32_t pf_tiles,
-                                                    unsigned long long *trace)
+                                                    unsigned long long *trace, Segs sg, uint32_t spin_cap)
 {
     extern __shared__ __align__(16) unsigned char smraw[];
     SortSmem &sm = *reinterpret_cast<SortSmem *>(smraw);
@@ -114,13 +127,33 @@ __global__ void __launch_bounds__(ST, 3) k_onesweep(const uint64_t *__restrict__
     long long ts[5];  // thread 0's clock at the phase boundaries (trace only)
     ts[0] = clock64();
     for (int i = threadIdx.x; i < SW * 256; i += ST) (&sm.whist[0][0])[i] = 0;
-    if (threadIdx.x == 0) sm.tile_id = atomicAdd(tile_ctr, 1u);
+    if (threadIdx.x == 0) {
+        const uint32_t t = atomicAdd(tile_ctr, 1u);
+        sm.tile_id = t;
+        if (sg.tile0) {  // the segment holding tile t: the last one whose first tile is at or below t
+            int lo = 0, hi = sg.nseg - 1;
+            while (lo < hi) {
+                const int m = (lo + hi + 1) >> 1;
+                if (sg.tile0[m] <= t) lo = m; else hi = m - 1;
+            }
+            const uint64_t b = sg.tstart[lo] + (uint64_t)(t - sg.tile0[lo]) * STILE;
+            sm.seg = (uint32_t)lo;
+            sm.first_tile = sg.tile0[lo];
+            sm.base = b;
+            sm.nvalid = (uint32_t)min((uint64_t)STILE, sg.tstart[lo + 1] - b);
+        } else {
+            sm.seg = 0;
+            sm.first_tile = 0;
+            sm.base = (uint64_t)t * STILE;
+            sm.nvalid = (uint32_t)min((uint64_t)STILE, n - (uint64_t)t * STILE);
+        }
+    }
     __syncthreads();
     ts[1] = clock64();
-    const uint64_t tile = sm.tile_id;
-    const uint64_t base = tile * STILE;
+    const uint64_t tile = sm.tile_id, first_tile = sm.first_tile;
+    const uint64_t base = sm.base, tend = base + sm.nvalid;
     const bool has_hi = in_hi != nullptr;
-    if (pf_tiles) {  // the tile that starts pf_tiles later (about one wave of resident tiles) into L2
+    if (pf_tiles) {  // the tuples pf_tiles tiles later (about one wave of resident tiles) into L2
         const uint64_t pb = base + (uint64_t)pf_tiles * STILE;
         if (pb < n) {
             const uint64_t pn = min((uint64_t)STILE, n - pb);
@@ -138,7 +171,7 @@ __global__ void __launch_bounds__(ST, 3) k_onesweep(const uint64_t *__restrict__
 #pragma unroll
     for (int j = 0; j < SI; j++) {
         const uint64_t idx = base + (uint64_t)warp * (32 * SI) + (uint64_t)j * 32 + lane;
-        const bool v = idx < n;
+        const bool v = idx < tend;
         key[j] = v ? in_lo[idx] : 0ull;
         const uint32_t h = (has_hi && v) ? (uint32_t)in_hi[idx] : 0u;
         hv[j >> 2] |= h << (8 * (j & 3));
@@ -177,7 +210,7 @@ __global__ void __launch_bounds__(ST, 3) k_onesweep(const uint64_t *__restrict__
 #pragma unroll
     for (int j = 0; j < SI; j++) {
         const uint64_t idx = base + (uint64_t)warp * (32 * SI) + (uint64_t)j * 32 + lane;
-        val[j] = idx < n ? in_id[idx] : 0u;
+        val[j] = idx < tend ? in_id[idx] : 0u;
     }
     __syncthreads();
     ts[2] = clock64();
@@ -195,7 +228,7 @@ __global__ void __launch_bounds__(ST, 3) k_onesweep(const uint64_t *__restrict__
             cnt += t;
         }
         const unsigned long long E = (unsigned long long)epoch << 60, PF = 1ull << 59;
-        if (walk) st_relaxed(status + tile * 256 + d, tile == 0 ? (E | PF | cnt) : (E | cnt));
+        if (walk) st_relaxed(status + tile * 256 + d, tile == first_tile ? (E | PF | cnt) : (E | cnt));
         // tile-local exclusive scan of the digit counts (warps 0..7 are all digit owners)
         x = cnt;
 #pragma unroll
@@ -211,7 +244,6 @@ __global__ void __launch_bounds__(ST, 3) k_onesweep(const uint64_t *__restrict__
         for (int w = 0; w < warp; w++) before += sm.wsum[w];
         sm.tstart[d] = before + x - cnt;
     }
-    if (threadIdx.x == 0) sm.nvalid = (uint32_t)min((uint64_t)STILE, n - base);
     __syncthreads();
     ts[3] = clock64();
     // tile order in shared memory first: the look-back below then finds more predecessors done
@@ -230,7 +262,7 @@ __global__ void __launch_bounds__(ST, 3) k_onesweep(const uint64_t *__restrict__
         // decoupled look-back for digit d
         const unsigned long long E = (unsigned long long)epoch << 60, PF = 1ull << 59, CM = PF - 1;
         unsigned long long excl = 0;
-        if (tile > 0) {
+        if (tile > first_tile) {
             // LB predecessors' words are read at once, then summed in order up to the first prefix;
             // a word not yet posted ends the round and the next round starts from it
             int64_t p = (int64_t)tile - 1;
@@ -241,7 +273,8 @@ __global__ void __launch_bounds__(ST, 3) k_onesweep(const uint64_t *__restrict__
 #pragma unroll
                 for (int q = 0; q < LB; q++) {
                     const int64_t pq = p - q;
-                    v[q] = pq >= 0 ? ld_relaxed(status + (uint64_t)pq * 256 + d) : (E | PF);  // before tile 0: prefix 0
+                    // before the segment's first tile: prefix 0
+                    v[q] = pq >= (int64_t)first_tile ? ld_relaxed(status + (uint64_t)pq * 256 + d) : (E | PF);
                 }
                 int adv = 0;
                 bool stall = false;
@@ -260,7 +293,7 @@ __global__ void __launch_bounds__(ST, 3) k_onesweep(const uint64_t *__restrict__
                 lb_steps += (uint32_t)adv;
                 if (stall && !found) {
                     lb_waits++;
-                    if (++spins > SPIN_CAP) {
+                    if (++spins >= spin_cap) {  // spin_cap polls of unposted words at most
                         atomicOr(err, DERR_SPIN);
                         break;
                     }
@@ -268,7 +301,7 @@ __global__ void __launch_bounds__(ST, 3) k_onesweep(const uint64_t *__restrict__
             }
             st_relaxed(status + tile * 256 + d, E | PF | (excl + cnt));
         }
-        sm.gbase[d] = dbase[d] + excl;
+        sm.gbase[d] = dbase[(uint64_t)sm.seg * sg.dstride + d] + excl;
     }
     __syncthreads();
     ts[4] = clock64();
@@ -345,11 +378,11 @@ int radix_sort(SortBufs &b, uint64_t n, bool has_hi, DeviceArena &arena, cudaStr
         if (dgt < 8)
             (mp::count_launch(), k_onesweep<0><<<(unsigned)tiles, ST, sizeof(SortSmem), st>>>(b.lo[src], ih, b.id[src], b.lo[dst], oh,
                                                                          b.id[dst], n, 8 * dgt, 8, dbase + dgt * 256, nullptr, status,
-                                                                         ctr + pi, (uint32_t)(pi + 1), err, pf, nullptr));
+                                                                         ctr + pi, (uint32_t)(pi + 1), err, pf, nullptr, Segs{}, arena.lim.lookback_spins));
         else
             (mp::count_launch(), k_onesweep<1><<<(unsigned)tiles, ST, sizeof(SortSmem), st>>>(b.lo[src], ih, b.id[src], b.lo[dst], oh,
                                                                          b.id[dst], n, 0, 8, dbase + dgt * 256, nullptr, status,
-                                                                         ctr + pi, (uint32_t)(pi + 1), err, pf, nullptr));
+                                                                         ctr + pi, (uint32_t)(pi + 1), err, pf, nullptr, Segs{}, arena.lim.lookback_spins));
         cudaEventRecord(ev[pi + 1], st);
         b.cur = dst;
     }
@@ -519,7 +552,7 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) k_segsort(const uint6
     for (uint32_t u = blockIdx.x; u < nunits; u += gridDim.x) {
         const long long t0 = clock64();
         const uint64_t start = ustart[u];
-        const uint32_t cnt = ucount[u], b0 = ubucket[u];
+        const uint32_t cnt = ucount[u], b0 = ubucket[u] & (NB - 1);  // the first bucket within its segment
         if (u + gridDim.x < nunits) {
             const uint64_t ns = ustart[u + gridDim.x], nc = ucount[u + gridDim.x];
             prefetch_range(lo_in + ns, nc * 8, SS_THREADS);
@@ -621,7 +654,7 @@ __global__ void k_big_scatter(const uint64_t *__restrict__ bstart, const uint32_
 {
     const uint32_t b = blockIdx.x;
     const uint64_t lowmask = (1ull << lowbits) - 1, s = bstart[b], o = boff[b];
-    const uint64_t hibits = (uint64_t)bbucket[b] << lowbits;
+    const uint64_t hibits = (uint64_t)(bbucket[b] & (NB - 1)) << lowbits;  // the bucket within its segment
     for (uint32_t e = threadIdx.x; e < bcount[b]; e += blockDim.x) {
         lo_out[s + e] = hibits | (tk[o + e] & lowmask);
         id_out[s + e] = tid[o + e];
@@ -637,34 +670,46 @@ struct BucketPasses {
     int sh[3], w[3];
 };
 
-// Digit counts of the passes (weighted by the bucket counts) and the populated-bucket flags.
-__global__ void k_bp_count(const uint64_t *__restrict__ hist, uint64_t lo, uint64_t nbk, BucketPasses bp,
-                           unsigned long long *dcnt, uint32_t *pop)
+// Digit counts of the passes (weighted by the bucket counts) and the populated-bucket flags.  A block takes
+// BP_CHUNK consecutive buckets from lo; with segments (lo = 0) the chunk lies in one segment's NB buckets,
+// whose counts go to that segment's rows: dcnt[(seg * 3 + pass) * 256 + digit].
+constexpr uint64_t BP_CHUNK = 4096;
+static_assert(NB % BP_CHUNK == 0, "a chunk of buckets never spans two segments");
+
+__global__ void __launch_bounds__(256) k_bp_count(const uint64_t *__restrict__ hist, uint64_t lo, uint64_t nbk,
+                                                  BucketPasses bp, bool segmented, unsigned long long *dcnt,
+                                                  uint32_t *pop)
 {
     __shared__ unsigned long long h[3 * 256];
     for (int i = threadIdx.x; i < 3 * 256; i += blockDim.x) h[i] = 0;
     __syncthreads();
-    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nbk; i += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t c0 = (uint64_t)blockIdx.x * BP_CHUNK, c1 = min(nbk, c0 + BP_CHUNK);
+    const uint64_t seg = segmented ? ((lo + c0) / NB) : 0;
+    for (uint64_t i = c0 + threadIdx.x; i < c1; i += blockDim.x) {
         const uint64_t b = lo + i, c = hist[b + 1] - hist[b];
         pop[i] = c ? 1u : 0u;
         if (!c) continue;
+        const uint32_t lb = (uint32_t)(b & (NB - 1));  // the bucket within its segment
 #pragma unroll
         for (int p = 0; p < 3; p++)
-            if (p < bp.np) atomicAdd(&h[p * 256 + ((b >> bp.sh[p]) & ((1u << bp.w[p]) - 1))], (unsigned long long)c);
+            if (p < bp.np) atomicAdd(&h[p * 256 + ((lb >> bp.sh[p]) & ((1u << bp.w[p]) - 1))], (unsigned long long)c);
     }
     __syncthreads();
     for (int i = threadIdx.x; i < bp.np * 256; i += blockDim.x)
-        if (h[i]) atomicAdd(&dcnt[i], h[i]);
+        if (h[i]) atomicAdd(&dcnt[seg * 3 * 256 + i], h[i]);
 }
 
-// Per pass (one block of 256): exclusive digit offsets, the mask of digits that occur, the largest
-// digit count (a digit holding every tuple is constant: no pass) and the total.
-__global__ void __launch_bounds__(256) k_bp_digits(const unsigned long long *dcnt, uint64_t *dbase, uint32_t *dnz,
-                                                   unsigned long long *dmax, unsigned long long *dtot)
+// Per (segment, pass), one block of 256: digit offsets (the segment's first tuple plus the exclusive digit
+// prefix), the digits that occur (ORed over the segments), the largest digit count and the total.
+__global__ void __launch_bounds__(256) k_bp_digits(const unsigned long long *dcnt, int np, const uint64_t *tstart,
+                                                   uint64_t *dbase, uint32_t *dnz, unsigned long long *dmax,
+                                                   unsigned long long *dtot)
 {
     __shared__ unsigned long long ws[8];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, p = blockIdx.x;
-    const unsigned long long c = dcnt[p * 256 + threadIdx.x];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int seg = blockIdx.x / np, p = blockIdx.x % np;
+    const uint64_t row = (uint64_t)seg * 3 + p;
+    const unsigned long long c = dcnt[row * 256 + threadIdx.x];
     unsigned long long x = c, m = c;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
@@ -673,20 +718,20 @@ __global__ void __launch_bounds__(256) k_bp_digits(const unsigned long long *dcn
         m = max(m, __shfl_xor_sync(FULLM, m, o));
     }
     const uint32_t nzw = __ballot_sync(FULLM, c != 0);
-    if (lane == 0) dnz[p * 8 + warp] = nzw;
+    if (lane == 0 && nzw) atomicOr(&dnz[p * 8 + warp], nzw);
     if (lane == 31) ws[warp] = x;
     __syncthreads();
     unsigned long long before = 0;
     for (int q = 0; q < warp; q++) before += ws[q];
-    dbase[p * 256 + threadIdx.x] = before + x - c;
-    if (threadIdx.x == 255) dtot[p] = before + x;
+    dbase[row * 256 + threadIdx.x] = (tstart ? tstart[seg] : 0ull) + before + x - c;
+    if (threadIdx.x == 255) dtot[row] = before + x;
     __syncthreads();
     if (lane == 0) ws[warp] = m;
     __syncthreads();
     if (threadIdx.x == 0) {
         unsigned long long mm = 0;
         for (int q = 0; q < 8; q++) mm = max(mm, ws[q]);
-        dmax[p] = mm;
+        dmax[row] = mm;
     }
 }
 
@@ -698,9 +743,9 @@ __global__ void k_bp_compact(const uint32_t *pop, const uint64_t *popoff, uint64
 
 constexpr int BP_BLOCK = 256;  // populated buckets packed greedily by one thread
 
-// Greedy packing of consecutive populated buckets into units (at most cap tuples, SS_MAXB buckets),
-// one thread per block of BP_BLOCK populated buckets; buckets above cap are listed apart.  Units never
-// cross a block, so each block ends with one partial unit.  Block g writes its units from g * BP_BLOCK
+// Greedy packing of consecutive populated buckets into units (at most cap tuples, SS_MAXB buckets, all
+// of one segment), one thread per block of BP_BLOCK populated buckets; buckets above cap are listed
+// apart.  Units never cross a block, so each block ends with one partial unit.  Block g writes its units from g * BP_BLOCK
 // into the staging arrays and their counts to nu_blk[g], nb_blk[g].
 __global__ void k_bp_greedy(const uint32_t *P, uint64_t np, const uint64_t *__restrict__ hist, uint64_t lo,
                             uint64_t *sus, uint32_t *suc, uint32_t *sub, uint64_t *sbs, uint32_t *sbc, uint32_t *sbb,
@@ -723,7 +768,7 @@ __global__ void k_bp_greedy(const uint32_t *P, uint64_t np, const uint64_t *__re
             sbs[i0 + nb] = s; sbc[i0 + nb] = (uint32_t)c; sbb[i0 + nb] = (uint32_t)bk; nb++;
             continue;
         }
-        if (have && (u_cnt + c > (uint64_t)cap || bk - u_b0 >= SS_MAXB)) {
+        if (have && (u_cnt + c > (uint64_t)cap || bk - u_b0 >= SS_MAXB || bk / NB != u_b0 / NB)) {
             sus[i0 + nu] = u_start; suc[i0 + nu] = (uint32_t)u_cnt; sub[i0 + nu] = u_b0; nu++;
             have = false;
         }
@@ -808,22 +853,26 @@ static void sort_kernel_attrs()
 }
 
 int bucket_sort(SortBufs &b, uint64_t n, bool has_hi, int k, const uint64_t *d_hist, uint64_t scan_lo, uint64_t scan_hi,
-                DeviceArena &arena, cudaStream_t st, SortStats *stats, int *out_lo_buf, int *out_hi_buf)
+                DeviceArena &arena, cudaStream_t st, SortStats *stats, int *out_lo_buf, int *out_hi_buf,
+                const SortSegments *segs)
 {
     if (stats) *stats = SortStats{};
     *out_lo_buf = *out_hi_buf = b.cur;
     if (n <= 1) return 0;
     if (scan_hi <= scan_lo) return set_error(MP_EFMT, "the histogram does not match the scan's tuples");
+    const int nseg = segs ? segs->nseg : 1;
+    if (segs && (scan_lo != 0 || scan_hi != (uint64_t)nseg * NB || (int)segs->tstart.size() != nseg + 1))
+        return set_error(MP_EARG, "segmented bucket sort: the buckets must be the segments' NB each");
     const int bsh = 2 * (k - 10), lowbits = 2 * (k - 10) + 8;
     const uint64_t nbk = scan_hi - scan_lo;
     // ---- plan on the device: digit offsets of the passes, populated buckets.  The scan's varying bucket
-    // bits (those of scan_lo ^ (scan_hi - 1)) are split into the fewest passes of at most 8 bits, of
-    // near-equal widths (19 bits: 7 + 6 + 6), so no pass ranks or looks back over digits that cannot occur;
-    // MP_SORT_BUCKET_DIGITS=bytes takes the bucket's bytes instead.
+    // bits (those of scan_lo ^ (scan_hi - 1); every bucket bit with segments) are split into the fewest
+    // passes of at most 8 bits, of near-equal widths (19 bits: 7 + 6 + 6), so no pass ranks or looks back
+    // over digits that cannot occur; MP_SORT_BUCKET_DIGITS=bytes takes the bucket's bytes instead.
     BucketPasses bpl{};
     {
         int vb = 0;
-        for (uint64_t v = scan_lo ^ (scan_hi - 1); v; v >>= 1) vb++;
+        for (uint64_t v = segs ? (uint64_t)(NB - 1) : (scan_lo ^ (scan_hi - 1)); v; v >>= 1) vb++;
         if (byte_bucket_digits()) {
             bpl.np = 3;
             for (int p = 0; p < 3; p++) bpl.sh[p] = 8 * p, bpl.w[p] = 8;
@@ -838,32 +887,62 @@ int bucket_sort(SortBufs &b, uint64_t n, bool has_hi, int k, const uint64_t *d_h
             }
         }
     }
-    unsigned long long *dcnt = arena.alloc<unsigned long long>(3 * 256), *dmax = arena.alloc<unsigned long long>(6);
-    uint64_t *dbase = arena.alloc<uint64_t>(3 * 256), *tot = arena.alloc<uint64_t>(4), *popoff = arena.alloc<uint64_t>(nbk + 2);
+    const uint64_t rows = (uint64_t)nseg * 3;
+    unsigned long long *dcnt = arena.alloc<unsigned long long>(rows * 256), *dmax = arena.alloc<unsigned long long>(2 * rows);
+    uint64_t *dbase = arena.alloc<uint64_t>(rows * 256), *tot = arena.alloc<uint64_t>(4), *popoff = arena.alloc<uint64_t>(nbk + 2);
     uint32_t *dnz = arena.alloc<uint32_t>(3 * 8), *pop = arena.alloc<uint32_t>(nbk + 1);
     const size_t tbp = scan_tmp_bytes(nbk + 1);
     void *tmp = arena.alloc<uint8_t>(tbp);
-    if (!dcnt || !dmax || !dbase || !tot || !popoff || !dnz || !pop || !tmp)
+    uint64_t *d_tstart = segs ? arena.alloc<uint64_t>(nseg + 1) : nullptr;
+    uint32_t *d_tile0 = segs ? arena.alloc<uint32_t>(nseg + 1) : nullptr;
+    if (!dcnt || !dmax || !dbase || !tot || !popoff || !dnz || !pop || !tmp || (segs && (!d_tstart || !d_tile0)))
         return set_error(MP_ENOMEM, "device memory for the bucket sort");
-    MP_CUDA(cudaMemsetAsync(dcnt, 0, 3 * 256 * sizeof(unsigned long long), st));
-    MP_CUDA(cudaMemsetAsync(pop + nbk, 0, sizeof(uint32_t), st));
-    {
-        const unsigned g = (unsigned)std::min<uint64_t>((nbk + 255) / 256, 8ull * (uint64_t)sm_count());
-        (mp::count_launch(), k_bp_count<<<g, 256, 0, st>>>(d_hist, scan_lo, nbk, bpl, dcnt, pop));
+    // tiles: each segment's own, from its first tuple
+    uint64_t tiles = (n + STILE - 1) / STILE;
+    if (segs) {
+        std::vector<uint32_t> t0(nseg + 1, 0);
+        uint64_t acc = 0;
+        for (int q = 0; q < nseg; q++) {
+            t0[q] = (uint32_t)acc;
+            acc += (segs->tstart[q + 1] - segs->tstart[q] + STILE - 1) / STILE;
+        }
+        t0[nseg] = (uint32_t)acc;
+        if (acc >= 0xFFFFFFFFull || segs->tstart[nseg] != n) return set_error(MP_EARG, "segmented bucket sort: bad segments");
+        tiles = acc;
+        MP_CUDA(cudaMemcpyAsync(d_tstart, segs->tstart.data(), (nseg + 1) * 8, cudaMemcpyHostToDevice, st));
+        MP_CUDA(cudaMemcpyAsync(d_tile0, t0.data(), (nseg + 1) * 4, cudaMemcpyHostToDevice, st));
     }
-    (mp::count_launch(), k_bp_digits<<<bpl.np, 256, 0, st>>>(dcnt, dbase, dnz, dmax, dmax + 3));
+    MP_CUDA(cudaMemsetAsync(dcnt, 0, rows * 256 * sizeof(unsigned long long), st));
+    MP_CUDA(cudaMemsetAsync(dnz, 0, 3 * 8 * sizeof(uint32_t), st));
+    MP_CUDA(cudaMemsetAsync(pop + nbk, 0, sizeof(uint32_t), st));
+    (mp::count_launch(), k_bp_count<<<(unsigned)((nbk + BP_CHUNK - 1) / BP_CHUNK), 256, 0, st>>>(d_hist, scan_lo, nbk, bpl,
+                                                                                              segs != nullptr, dcnt, pop));
+    (mp::count_launch(), k_bp_digits<<<(unsigned)(nseg * bpl.np), 256, 0, st>>>(dcnt, bpl.np, d_tstart, dbase, dnz, dmax,
+                                                                             dmax + rows));
     scan_u32_to_u64(pop, popoff, nbk + 1, tot, tmp, tbp, st);
-    uint64_t hd = 0;                   // populated buckets
-    unsigned long long hm[6] = {};     // per pass: largest digit count, then the totals
+    uint64_t hd = 0;  // populated buckets
+    std::vector<unsigned long long> hm(2 * rows);  // per (segment, pass): largest digit count, then the totals
     MP_CUDA(cudaMemcpyAsync(&hd, tot, 8, cudaMemcpyDeviceToHost, st));
-    MP_CUDA(cudaMemcpyAsync(hm, dmax, sizeof hm, cudaMemcpyDeviceToHost, st));
+    MP_CUDA(cudaMemcpyAsync(hm.data(), dmax, hm.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
     MP_CUDA(cudaStreamSynchronize(st));
-    if (hm[3] != n) return set_error(MP_EFMT, "the histogram does not match the scan's tuples");
+    {
+        uint64_t total = 0;
+        for (int q = 0; q < nseg; q++) {
+            const unsigned long long t = hm[rows + (uint64_t)q * 3];
+            if (segs && t != segs->tstart[q + 1] - segs->tstart[q])
+                return set_error(MP_EFMT, "the histogram does not match segment %d's tuples", q);
+            total += t;
+        }
+        if (total != n) return set_error(MP_EFMT, "the histogram does not match the scan's tuples");
+    }
     const uint64_t np = hd;
-    std::vector<int> passes;
-    for (int d = 0; d < bpl.np; d++)
-        if (hm[d] != n) passes.push_back(d);
-    const uint64_t tiles = (n + STILE - 1) / STILE;
+    std::vector<int> passes;  // a pass runs unless its digit is constant within every segment
+    for (int d = 0; d < bpl.np; d++) {
+        bool constant = true;
+        for (int q = 0; q < nseg && constant; q++)
+            constant = hm[(uint64_t)q * 3 + d] == hm[rows + (uint64_t)q * 3 + d];
+        if (!constant) passes.push_back(d);
+    }
     uint32_t *ctr = arena.alloc<uint32_t>(8), *err = arena.alloc<uint32_t>(1);
     unsigned long long *trace = arena.alloc<unsigned long long>(16);  // [0..3] unit sort, [8..12] digit passes
     unsigned long long *status = passes.empty() ? nullptr : arena.alloc<unsigned long long>(tiles * 256);
@@ -874,6 +953,13 @@ int bucket_sort(SortBufs &b, uint64_t n, bool has_hi, int k, const uint64_t *d_h
     if (status) MP_CUDA(cudaMemsetAsync(status, 0, tiles * 256 * sizeof(unsigned long long), st));
     sort_kernel_attrs();
     const uint32_t pf = onesweep_prefetch_tiles();
+    Segs sg;
+    if (segs) {
+        sg.tile0 = d_tile0;
+        sg.tstart = d_tstart;
+        sg.nseg = nseg;
+        sg.dstride = 3 * 256;
+    }
     Events ev(5);
     cudaEventRecord(ev[0], st);
     for (size_t pi = 0; pi < passes.size(); pi++) {
@@ -884,7 +970,7 @@ int bucket_sort(SortBufs &b, uint64_t n, bool has_hi, int k, const uint64_t *d_h
         (mp::count_launch(), kern<<<(unsigned)tiles, ST, sizeof(SortSmem), st>>>(
             b.lo[src], has_hi ? b.hi[src] : nullptr, b.id[src], b.lo[dst], has_hi ? b.hi[dst] : nullptr, b.id[dst], n,
             bsh + bpl.sh[d], bpl.w[d], dbase + d * 256, dnz + d * 8, status, ctr + pi, (uint32_t)(pi + 1), err, pf,
-            trace + 8));
+            trace + 8, sg, arena.lim.lookback_spins));
         b.cur = dst;
     }
     cudaEventRecord(ev[1], st);
@@ -1177,11 +1263,11 @@ int sort_tuples_noalloc(const uint64_t *lo_in, const uint8_t *hi_in, const uint3
         if (dgt < 8)
             (mp::count_launch(), k_onesweep<0><<<(unsigned)tiles, ST, sizeof(SortSmem), st>>>(
                 src_lo, src_hi, src_id, d_lo, d_hi, d_id, n, 8 * dgt, 8, S->dbase + dgt * 256, nullptr, S->status, S->ctr + i,
-                (uint32_t)(i + 1), &S->err, 0u, nullptr));
+                (uint32_t)(i + 1), &S->err, 0u, nullptr, Segs{}, WaitLimits{}.lookback_spins));
         else
             (mp::count_launch(), k_onesweep<1><<<(unsigned)tiles, ST, sizeof(SortSmem), st>>>(
                 src_lo, src_hi, src_id, d_lo, d_hi, d_id, n, 0, 8, S->dbase + dgt * 256, nullptr, S->status, S->ctr + i,
-                (uint32_t)(i + 1), &S->err, 0u, nullptr));
+                (uint32_t)(i + 1), &S->err, 0u, nullptr, Segs{}, WaitLimits{}.lookback_spins));
         src_lo = d_lo;
         src_hi = d_hi;
         src_id = d_id;

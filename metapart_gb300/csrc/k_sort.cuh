@@ -1,4 +1,6 @@
 #pragma once
+#include <vector>
+
 #include "k_reads.cuh"
 
 namespace mp {
@@ -31,10 +33,20 @@ struct SortStats {
 // Stable sort of b[cur][0, n) by (hi, lo); on return b.cur names the sorted buffer.
 int radix_sort(SortBufs &b, uint64_t n, bool has_hi, DeviceArena &arena, cudaStream_t st, SortStats *stats);
 
+// Independent tuple sets (samples) one after another in one tuple array: segment q holds the tuples
+// [tstart[q], tstart[q + 1]) and the m-mer buckets q * NB .. q * NB + NB - 1 of a segmented histogram.
+struct SortSegments {
+    int nseg = 0;
+    std::vector<uint64_t> tstart;  // nseg + 1 tuple offsets (host)
+};
+
 // Stable sort of one scan's tuples by (k-mer, adjacency) using the scan's m-mer bucket counts
 // (d_hist: the 1048577-entry .kmerHist prefix in device memory, buckets [scan_lo, scan_hi)).  On return
-// lo/id are in b.*[*out_lo_buf] and hi in b.hi[*out_hi_buf].
+// lo/id are in b.*[*out_lo_buf] and hi in b.hi[*out_hi_buf].  With segs, each segment is sorted on its own
+// (its tuples stay in its range): d_hist is then the prefix over the segments' buckets one after another
+// (nseg * NB + 1 entries, tuple offsets into the whole array) and [scan_lo, scan_hi) = [0, nseg * NB).
 int bucket_sort(SortBufs &b, uint64_t n, bool has_hi, int k, const uint64_t *d_hist, uint64_t scan_lo, uint64_t scan_hi,
-                DeviceArena &arena, cudaStream_t st, SortStats *stats, int *out_lo_buf, int *out_hi_buf);
+                DeviceArena &arena, cudaStream_t st, SortStats *stats, int *out_lo_buf, int *out_hi_buf,
+                const SortSegments *segs = nullptr);
 
 }  // namespace mp

@@ -13,6 +13,7 @@
 #include "k_output.cuh"
 #include "k_reads.cuh"
 #include "k_sort.cuh"
+#include "mp_internal.cuh"
 
 namespace mp {
 
@@ -55,6 +56,63 @@ int sm_count()
     return n;
 }
 
+__global__ void k_init_parent(uint32_t *parent, uint64_t n)
+{
+    const uint64_t x = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (x < n) parent[x] = (uint32_t)x;
+}
+
+void launch_init_parent(uint32_t *parent, uint64_t n, cudaStream_t st)
+{
+    if (n) (count_launch(), k_init_parent<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(parent, n));
+}
+
+void free_kc_piece(DeviceArena &arena, KcPiece &q)
+{
+    arena.free_persistent(q.off);
+    arena.free_persistent(q.lo);
+    arena.free_persistent(q.hi);
+    q = KcPiece{};
+}
+
+bool make_kc_piece(DeviceArena &arena, cudaStream_t st, const ParsedReads &pr, uint64_t r0, int k, KcPiece *out)
+{
+    const uint64_t N = pr.n_reads;
+    KcPiece q;
+    q.r0 = r0;
+    q.n = N;
+    uint32_t *npos = arena.alloc<uint32_t>(N + 1);
+    uint64_t *tot = arena.alloc<uint64_t>(1);
+    size_t tb = scan_tmp_bytes(N + 1);
+    void *tmp = arena.alloc<uint8_t>(tb);
+    q.off = arena.alloc_persistent<uint64_t>(N + 2);
+    uint64_t P = 0;
+    bool ok = npos && tot && tmp && q.off;
+    if (ok) {
+        launch_kc_positions(pr, k, npos, st);
+        ok = cudaMemsetAsync(npos + N, 0, 4, st) == cudaSuccess;
+    }
+    if (ok) {
+        scan_u32_to_u64(npos, q.off, N + 1, tot, tmp, tb, st);
+        ok = cudaMemcpyAsync(&P, tot, 8, cudaMemcpyDeviceToHost, st) == cudaSuccess &&
+             cudaStreamSynchronize(st) == cudaSuccess;
+    }
+    if (ok) {
+        q.lo = arena.alloc_persistent<uint64_t>(P + 1);
+        q.hi = arena.alloc_persistent<uint8_t>(P + 1);
+        ok = q.lo && q.hi;
+    }
+    arena.free_scratch(npos);
+    arena.free_scratch(tot);
+    arena.free_scratch(tmp);
+    if (!ok) {
+        free_kc_piece(arena, q);
+        return false;
+    }
+    *out = q;
+    return true;
+}
+
 }  // namespace mp
 
 using namespace mp;
@@ -66,13 +124,13 @@ struct mp_ctx {
     std::mutex mu;
 };
 
-// A piece of the k-mer cache: the reads r0 .. r0 + n - 1, their position offsets off (n + 1, from 0)
-// and per position lo = canon << 8 | adj, hi = canon >> 56 (KC_NONE: the window holds an N).
-struct KcPiece {
-    uint64_t r0 = 0, n = 0;
-    uint64_t *off = nullptr, *lo = nullptr;
-    uint8_t *hi = nullptr;
-};
+int mp::ctx_device(const mp_ctx *ctx) { return ctx->device; }
+
+void mp::ctx_budget(mp_ctx *ctx, std::atomic<uint64_t> **used, uint64_t *limit)
+{
+    *used = &ctx->used;
+    *limit = ctx->budget;
+}
 
 struct mp_job {
     mp_ctx *ctx = nullptr;
@@ -119,28 +177,6 @@ struct mp_job {
 // ------------------------------------------------------------------ helpers
 
 namespace {
-
-struct StageTimer {
-    cudaEvent_t a, b;
-    cudaStream_t st;
-    double *acc;
-    StageTimer(cudaStream_t s, double *slot) : st(s), acc(slot)
-    {
-        cudaEventCreate(&a);
-        cudaEventCreate(&b);
-        cudaEventRecord(a, st);
-    }
-    ~StageTimer()
-    {
-        cudaEventRecord(b, st);
-        cudaEventSynchronize(b);
-        float ms = 0;
-        cudaEventElapsedTime(&ms, a, b);
-        *acc += ms;
-        cudaEventDestroy(a);
-        cudaEventDestroy(b);
-    }
-};
 
 int write_file(const std::string &path, const void *buf, size_t n, bool append = false)
 {
@@ -204,11 +240,6 @@ int dump_state(mp_job *j, const char *pname, const char *sname, bool with_parent
     return rc;
 }
 
-__global__ void k_init_parent(uint32_t *parent, uint64_t n)
-{
-    const uint64_t x = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (x < n) parent[x] = (uint32_t)x;
-}
 
 __global__ void k_sizes_raw(const uint32_t *parent, uint64_t n, uint32_t *size)
 {
@@ -284,52 +315,9 @@ int range_bounds(const uint64_t *hist, const uint64_t *ltr, int T, uint64_t scan
 
 void drop_kmer_cache(mp_job *j)
 {
-    for (KcPiece &q : j->kc) {
-        j->arena.free_persistent(q.off);
-        j->arena.free_persistent(q.lo);
-        j->arena.free_persistent(q.hi);
-    }
+    for (KcPiece &q : j->kc) free_kc_piece(j->arena, q);
     j->kc.clear();
     j->kc_k = 0;
-}
-
-// One cache piece for the reads of pr (global reads r0 ..): position offsets by a scan of L - k + 1,
-// and the lo/hi arrays; false (nothing kept) when device memory or the budget does not allow it.
-static bool make_kc_piece(mp_job *j, const ParsedReads &pr, uint64_t r0, int k, KcPiece *out)
-{
-    const uint64_t N = pr.n_reads;
-    KcPiece q;
-    q.r0 = r0;
-    q.n = N;
-    uint32_t *npos = j->arena.alloc<uint32_t>(N + 1);
-    uint64_t *tot = j->arena.alloc<uint64_t>(1);
-    size_t tb = scan_tmp_bytes(N + 1);
-    void *tmp = j->arena.alloc<uint8_t>(tb);
-    q.off = j->arena.alloc_persistent<uint64_t>(N + 2);
-    uint64_t P = 0;
-    bool ok = npos && tot && tmp && q.off;
-    if (ok) {
-        launch_kc_positions(pr, k, npos, j->st);
-        ok = cudaMemsetAsync(npos + N, 0, 4, j->st) == cudaSuccess;
-    }
-    if (ok) {
-        scan_u32_to_u64(npos, q.off, N + 1, tot, tmp, tb, j->st);
-        ok = cudaMemcpyAsync(&P, tot, 8, cudaMemcpyDeviceToHost, j->st) == cudaSuccess &&
-             cudaStreamSynchronize(j->st) == cudaSuccess;
-    }
-    if (ok) {
-        q.lo = j->arena.alloc_persistent<uint64_t>(P + 1);
-        q.hi = j->arena.alloc_persistent<uint8_t>(P + 1);
-        ok = q.lo && q.hi;
-    }
-    if (!ok) {
-        j->arena.free_persistent(q.off);
-        j->arena.free_persistent(q.lo);
-        j->arena.free_persistent(q.hi);
-        return false;
-    }
-    *out = q;
-    return true;
 }
 
 // The cache for the plain variant's count pass, one piece for all reads; false (and no cache) when
@@ -337,7 +325,7 @@ static bool make_kc_piece(mp_job *j, const ParsedReads &pr, uint64_t r0, int k, 
 bool make_kmer_cache(mp_job *j, int k)
 {
     KcPiece q;
-    if (!make_kc_piece(j, j->pr, 0, k, &q)) {
+    if (!make_kc_piece(j->arena, j->st, j->pr, 0, k, &q)) {
         drop_kmer_cache(j);
         return false;
     }
@@ -618,7 +606,7 @@ int load_count_pipelined(mp_job *j, const char *bytes, uint64_t nbytes, const ui
         R[i + 1] = R[i] + prs[i].n_reads;
         StageTimer tm(j->st, &j->stage_ms[1]);
         KcPiece q;
-        if (!make_kc_piece(j, prs[i], R[i], k, &q)) return MP_ENOMEM;
+        if (!make_kc_piece(j->arena, j->st, prs[i], R[i], k, &q)) return MP_ENOMEM;
         j->kc.push_back(q);
         launch_count(j->d_fq + seg[i], prs[i], k, 0, nullptr, 0, nullptr, glob, err, j->st, q.off, q.lo, q.hi);
     }
@@ -990,7 +978,7 @@ int mp_job_partition(mp_job *j, const mp_part_params *p, const uint64_t *chunk_s
     uint32_t *err = j->arena.alloc_persistent<uint32_t>(1);
     if (!j->d_parent || !j->d_size || !j->d_filtered || !err) return set_error(MP_ENOMEM, "device memory for the forest");
     const unsigned gN = (unsigned)((N + 255) / 256);
-    (mp::count_launch(), k_init_parent<<<gN, 256, 0, j->st>>>(j->d_parent, N));
+    launch_init_parent(j->d_parent, N, j->st);
     MP_CUDA(cudaMemsetAsync(j->d_filtered, 0, N + 1, j->st));
     MP_CUDA(cudaMemsetAsync(err, 0, 4, j->st));
     const bool has_hi = 2 * k + 8 > 64;
@@ -1290,6 +1278,16 @@ int mp_job_set_kmer_cache(mp_job *j, int enable)
     if (!j) return set_error(MP_EARG, "null job");
     j->kc_on = enable != 0;
     if (!j->kc_on) drop_kmer_cache(j);
+    return 0;
+}
+
+int mp_job_set_wait_limits(mp_job *j, uint32_t lookback_spins, uint32_t union_retries, uint32_t mate_rounds)
+{
+    if (!j) return set_error(MP_EARG, "null job");
+    const WaitLimits d;
+    j->arena.lim.lookback_spins = lookback_spins ? lookback_spins : d.lookback_spins;
+    j->arena.lim.union_retries = union_retries ? union_retries : d.union_retries;
+    j->arena.lim.mate_rounds = mate_rounds ? mate_rounds : d.mate_rounds;
     return 0;
 }
 

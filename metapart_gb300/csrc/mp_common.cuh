@@ -22,6 +22,15 @@ enum DevErr : uint32_t {
     DERR_TOO_MANY = 1u << 3,   // a read has 256 or more tuples in one scan
 };
 
+// Iteration limits of the device's bounded waits: the sort's look-back polls of one status word, the
+// union-find's hook retries, and the mate union's rounds.  A wait that runs out sets DERR_SPIN (or the
+// round count ends the stage) and the call returns MP_EDEVICE; nothing waits without a limit.
+struct WaitLimits {
+    uint32_t lookback_spins = 1u << 22;
+    uint32_t union_retries = 1u << 20;
+    uint32_t mate_rounds = 4000000u;
+};
+
 struct DevStatus {
     uint32_t err;
     uint32_t pad;

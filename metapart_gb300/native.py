@@ -62,6 +62,8 @@ def lib():
         L.mp_job_set_dump_dir.argtypes = [C.c_void_p, C.c_char_p]
         L.mp_job_set_kmer_cache.argtypes = [C.c_void_p, C.c_int]
         L.mp_job_set_scan_piece_tuples.argtypes = [C.c_void_p, C.c_uint64]
+        L.mp_job_set_wait_limits.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32]
+        L.mp_batch_set_wait_limits.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32]
         L.mp_job_scan_pieces.argtypes = [C.c_void_p]
         L.mp_job_stage_ms.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.c_int]
         L.mp_job_sort_stats.argtypes = [C.c_void_p, u64p, C.POINTER(C.c_int), C.POINTER(C.c_double), u64p]
@@ -69,6 +71,12 @@ def lib():
                                         C.POINTER(C.c_double), u64p, u64p, u64p, u64p]
         L.mp_sort_tuples.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                      C.c_void_p, C.c_uint64, C.c_void_p]
+        L.mp_batch_create.argtypes = [C.c_void_p, C.POINTER(C.c_void_p)]
+        L.mp_batch_destroy.argtypes = [C.c_void_p]
+        L.mp_batch_run.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
+        L.mp_batch_stage_ms.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.c_int]
+        L.mp_batch_groups.argtypes = [C.c_void_p]
+        L.mp_batch_sort_stats.argtypes = [C.c_void_p, u64p, C.POINTER(C.c_int), C.POINTER(C.c_double), u64p]
         _lib = L
     return _lib
 
@@ -214,6 +222,10 @@ class Job:
         bucket-range pieces with the same results."""
         _check(lib().mp_job_set_scan_piece_tuples(self.h, int(max_tuples)), "set_scan_piece_tuples")
 
+    def set_wait_limits(self, lookback_spins: int = 0, union_retries: int = 0, mate_rounds: int = 0):
+        """Iteration limits of the bounded device waits (0: the default)."""
+        _check(lib().mp_job_set_wait_limits(self.h, lookback_spins, union_retries, mate_rounds), "set_wait_limits")
+
     @property
     def scan_pieces(self) -> int:
         """Bucket-range pieces the last partition ran its scans in (numScans when none was split)."""
@@ -344,3 +356,90 @@ def run_pipeline(ctx: Context, fastq: bytes, k: int, num_chunks: int, num_scans:
     cnt = job.count(k, starts, min3)
     bounds = job.partition(k, num_scans, num_threads, starts, cnt.chunk_first_read, cnt.hist, min3)
     return job, bounds, cnt
+
+
+class BatchParams(C.Structure):
+    _fields_ = [("k", C.c_int), ("interleaved", C.c_int)]
+
+
+class BatchSample(C.Structure):
+    _fields_ = [("fastq", C.c_void_p), ("nbytes", C.c_uint64), ("num_chunks", C.c_int), ("num_threads", C.c_int),
+                ("out", C.c_void_p), ("out_cap", C.c_uint64), ("file_sizes", C.POINTER(C.c_uint64)),
+                ("labels", C.POINTER(C.c_uint32)), ("labels_cap", C.c_uint64)]
+
+
+class BatchResult(C.Structure):
+    _fields_ = [("status", C.c_int), ("error", C.c_char * 256), ("n_reads", C.c_uint64), ("out_total", C.c_uint64),
+                ("bounds", C.c_uint64 * 17)]
+
+
+@dataclass
+class SampleIn:
+    """One sample of a batch: its FASTQ at a host address (pinned memory for overlapped uploads), its chunk
+    and thread counts, and where its partition files (and optionally labels) go."""
+    fastq_ptr: int
+    nbytes: int
+    num_chunks: int
+    num_threads: int
+    out_ptr: int = 0
+    out_cap: int = 0
+    file_sizes: np.ndarray | None = None
+    labels: np.ndarray | None = None
+
+
+class Batch:
+    """Many independent samples partitioned together (mp_batch_run): each gets the bounds, labels and
+    partition files it gets alone with one scan."""
+
+    def __init__(self, ctx: Context):
+        self.ctx = ctx
+        self.h = C.c_void_p()
+        _check(lib().mp_batch_create(ctx.h, C.byref(self.h)), "mp_batch_create")
+
+    def close(self):
+        if self.h:
+            lib().mp_batch_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def run(self, k: int, samples: list, interleaved: bool = False) -> list:
+        n = len(samples)
+        arr = (BatchSample * n)()
+        for i, s in enumerate(samples):
+            arr[i].fastq = s.fastq_ptr
+            arr[i].nbytes = s.nbytes
+            arr[i].num_chunks = s.num_chunks
+            arr[i].num_threads = s.num_threads
+            arr[i].out = s.out_ptr or None
+            arr[i].out_cap = s.out_cap
+            if s.file_sizes is not None:
+                arr[i].file_sizes = s.file_sizes.ctypes.data_as(C.POINTER(C.c_uint64))
+            if s.labels is not None:
+                arr[i].labels = s.labels.ctypes.data_as(C.POINTER(C.c_uint32))
+                arr[i].labels_cap = len(s.labels)
+        res = (BatchResult * n)()
+        p = BatchParams(k, int(interleaved))
+        _check(lib().mp_batch_run(self.h, C.byref(p), n, arr, res), "mp_batch_run")
+        return [{"n_reads": r.n_reads, "out_total": r.out_total, "bounds": np.array(list(r.bounds), dtype=np.uint64)}
+                for r in res]
+
+    def stage_ms(self) -> dict:
+        a = (C.c_double * 8)()
+        _check(lib().mp_batch_stage_ms(self.h, a, 8), "mp_batch_stage_ms")
+        names = ["parse", "count", "enumerate", "sort", "filter", "union_find", "mate_union_plan", "output"]
+        return dict(zip(names, list(a)))
+
+    @property
+    def groups(self) -> int:
+        return int(lib().mp_batch_groups(self.h))
+
+    def sort_stats(self) -> dict:
+        t, b = C.c_uint64(), C.c_uint64()
+        p, ms = C.c_int(), C.c_double()
+        _check(lib().mp_batch_sort_stats(self.h, C.byref(t), C.byref(p), C.byref(ms), C.byref(b)), "mp_batch_sort_stats")
+        return {"tuples": t.value, "passes": p.value, "pass_ms": ms.value, "bytes": b.value}

@@ -30,4 +30,9 @@ def test_oracle_equals_reference(tmp_path, built, name, n, seed, p):
     a = pu.outputs(pu.run("ref", tmp_path, [fq], p), p, "in.fastq")
     b = pu.outputs(pu.run("oracle", tmp_path, [fq], p), p, "in.fastq")
     assert sorted(a) == sorted(b)
-    assert pu.diff_keys(a, b) == []
+    # compSizes between scans: the reference's edge replay (unionFind, metapart.c:2736-2800) runs its
+    # unionOp calls on every thread at once without atomics, so with giant components the sizes it
+    # accumulates depend on thread timing; nothing reads them before the reset ahead of the mate union
+    # (metapart.c:4010-4030), whose sizes are compared with everything else.
+    racy = {f"dump/stats{s}_sizes.bin" for s in range(p.scans)}
+    assert pu.diff_keys(a, b, [x for x in sorted(a) if x not in racy]) == []
