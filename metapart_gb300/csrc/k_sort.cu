@@ -100,10 +100,11 @@ __device__ __forceinline__ uint32_t digit_of(uint64_t lo, uint32_t hi, int shift
 
 // W: ballots per tuple in the ranking, at least the digit's width w (digits are masked to w bits, so
 // the planes above w are zero in every lane and filter nothing).
-// Segments (batches of samples): the tuple array holds nseg segments one after another, each sorted on its
-// own -- seg_tstart (nseg + 1 tuple offsets) and seg_tile0 (nseg + 1 tile offsets: a segment's tiles start
-// at its first tuple, so no tile spans two segments); a tile's look-back stops at its segment's first tile
-// and its digit bases are dbase[seg * dstride + digit].  seg_tile0 == nullptr: one segment of n tuples.
+// SEGD: segments (batches of samples) -- the tuple array holds sg.nseg segments one after another, each
+// sorted on its own: sg.tstart (nseg + 1 tuple offsets) and sg.tile0 (nseg + 1 tile offsets: a segment's
+// tiles start at its first tuple, so no tile spans two segments); a tile's look-back stops at its
+// segment's first tile and its digit bases are dbase[seg * sg.dstride + digit].  Without SEGD the array is
+// one segment of n tuples (and the kernel keeps its registers for the ranking).
 struct Segs {
     const uint32_t *tile0 = nullptr;
     const uint64_t *tstart = nullptr;
@@ -111,7 +112,7 @@ struct Segs {
     uint32_t dstride = 0;
 };
 
-template <int SRC, int W = 8>
+template <int SRC, int W = 8, bool SEGD = false>
 __global__ void __launch_bounds__(ST, 3) k_onesweep(const uint64_t *__restrict__ in_lo, const uint8_t *__restrict__ in_hi,
                                                     const uint32_t *__restrict__ in_id, uint64_t *__restrict__ out_lo,
                                                     uint8_t *__restrict__ out_hi, uint32_t *__restrict__ out_id, uint64_t n,
@@ -124,13 +125,14 @@ __global__ void __launch_bounds__(ST, 3) k_onesweep(const uint64_t *__restrict__
     SortSmem &sm = *reinterpret_cast<SortSmem *>(smraw);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t dmask = (1u << w) - 1;
-    long long ts[5];  // thread 0's clock at the phase boundaries (trace only)
-    ts[0] = clock64();
+    long long ts[5];  // thread 0's clock at the phase boundaries (trace only; not with segments)
+    if constexpr (!SEGD) ts[0] = clock64();
     for (int i = threadIdx.x; i < SW * 256; i += ST) (&sm.whist[0][0])[i] = 0;
-    if (threadIdx.x == 0) {
-        const uint32_t t = atomicAdd(tile_ctr, 1u);
-        sm.tile_id = t;
-        if (sg.tile0) {  // the segment holding tile t: the last one whose first tile is at or below t
+    if (threadIdx.x == 0) sm.tile_id = atomicAdd(tile_ctr, 1u);
+    __syncthreads();
+    if constexpr (SEGD) {  // the segment holding the tile: the last one whose first tile is at or below it
+        if (threadIdx.x == 0) {
+            const uint32_t t = sm.tile_id;
             int lo = 0, hi = sg.nseg - 1;
             while (lo < hi) {
                 const int m = (lo + hi + 1) >> 1;
@@ -141,19 +143,15 @@ __global__ void __launch_bounds__(ST, 3) k_onesweep(const uint64_t *__restrict__
             sm.first_tile = sg.tile0[lo];
             sm.base = b;
             sm.nvalid = (uint32_t)min((uint64_t)STILE, sg.tstart[lo + 1] - b);
-        } else {
-            sm.seg = 0;
-            sm.first_tile = 0;
-            sm.base = (uint64_t)t * STILE;
-            sm.nvalid = (uint32_t)min((uint64_t)STILE, n - (uint64_t)t * STILE);
         }
+        __syncthreads();
     }
-    __syncthreads();
-    ts[1] = clock64();
-    const uint64_t tile = sm.tile_id, first_tile = sm.first_tile;
-    const uint64_t base = sm.base, tend = base + sm.nvalid;
+    if constexpr (!SEGD) ts[1] = clock64();
+    const uint64_t tile = sm.tile_id;
+    const uint64_t base = SEGD ? sm.base : tile * STILE;
+    const uint64_t tend = SEGD ? base + sm.nvalid : n;  // the tile's tuples end below tend
     const bool has_hi = in_hi != nullptr;
-    if (pf_tiles) {  // the tuples pf_tiles tiles later (about one wave of resident tiles) into L2
+    if (pf_tiles) {  // the tile that starts pf_tiles later (about one wave of resident tiles) into L2
         const uint64_t pb = base + (uint64_t)pf_tiles * STILE;
         if (pb < n) {
             const uint64_t pn = min((uint64_t)STILE, n - pb);
@@ -209,11 +207,13 @@ __global__ void __launch_bounds__(ST, 3) k_onesweep(const uint64_t *__restrict__
     // the ids are needed only for the tile order below: loaded now, they arrive during the digit scan
 #pragma unroll
     for (int j = 0; j < SI; j++) {
-        const uint64_t idx = base + (uint64_t)warp * (32 * SI) + (uint64_t)j * 32 + lane;
-        val[j] = idx < tend ? in_id[idx] : 0u;
+        // (with segments the tile's bounds are read again: no registers held through the ranking)
+        const uint64_t b2 = SEGD ? sm.base : base, e2 = SEGD ? sm.base + sm.nvalid : n;
+        const uint64_t idx = b2 + (uint64_t)warp * (32 * SI) + (uint64_t)j * 32 + lane;
+        val[j] = idx < e2 ? in_id[idx] : 0u;
     }
     __syncthreads();
-    ts[2] = clock64();
+    if constexpr (!SEGD) ts[2] = clock64();
     // threads 0..255 own one digit each: warp prefixes, the tile count, its look-back (skipped, with the
     // status word, for a digit that no tuple of the input has: bit clear in nzmask)
     const uint32_t d = threadIdx.x;
@@ -228,7 +228,8 @@ __global__ void __launch_bounds__(ST, 3) k_onesweep(const uint64_t *__restrict__
             cnt += t;
         }
         const unsigned long long E = (unsigned long long)epoch << 60, PF = 1ull << 59;
-        if (walk) st_relaxed(status + tile * 256 + d, tile == first_tile ? (E | PF | cnt) : (E | cnt));
+        const uint64_t first = SEGD ? (uint64_t)sm.first_tile : 0ull;  // the segment's first tile posts a prefix
+        if (walk) st_relaxed(status + tile * 256 + d, tile == first ? (E | PF | cnt) : (E | cnt));
         // tile-local exclusive scan of the digit counts (warps 0..7 are all digit owners)
         x = cnt;
 #pragma unroll
@@ -244,8 +245,9 @@ __global__ void __launch_bounds__(ST, 3) k_onesweep(const uint64_t *__restrict__
         for (int w = 0; w < warp; w++) before += sm.wsum[w];
         sm.tstart[d] = before + x - cnt;
     }
+    if (!SEGD && threadIdx.x == 0) sm.nvalid = (uint32_t)min((uint64_t)STILE, n - base);
     __syncthreads();
-    ts[3] = clock64();
+    if constexpr (!SEGD) ts[3] = clock64();
     // tile order in shared memory first: the look-back below then finds more predecessors done
 #pragma unroll
     for (int j = 0; j < SI; j++) {
@@ -262,7 +264,8 @@ __global__ void __launch_bounds__(ST, 3) k_onesweep(const uint64_t *__restrict__
         // decoupled look-back for digit d
         const unsigned long long E = (unsigned long long)epoch << 60, PF = 1ull << 59, CM = PF - 1;
         unsigned long long excl = 0;
-        if (tile > first_tile) {
+        const int64_t first = SEGD ? (int64_t)sm.first_tile : 0;  // before it: prefix 0
+        if ((int64_t)tile > first) {
             // LB predecessors' words are read at once, then summed in order up to the first prefix;
             // a word not yet posted ends the round and the next round starts from it
             int64_t p = (int64_t)tile - 1;
@@ -273,8 +276,7 @@ __global__ void __launch_bounds__(ST, 3) k_onesweep(const uint64_t *__restrict__
 #pragma unroll
                 for (int q = 0; q < LB; q++) {
                     const int64_t pq = p - q;
-                    // before the segment's first tile: prefix 0
-                    v[q] = pq >= (int64_t)first_tile ? ld_relaxed(status + (uint64_t)pq * 256 + d) : (E | PF);
+                    v[q] = pq >= first ? ld_relaxed(status + (uint64_t)pq * 256 + d) : (E | PF);
                 }
                 int adv = 0;
                 bool stall = false;
@@ -301,10 +303,10 @@ __global__ void __launch_bounds__(ST, 3) k_onesweep(const uint64_t *__restrict__
             }
             st_relaxed(status + tile * 256 + d, E | PF | (excl + cnt));
         }
-        sm.gbase[d] = dbase[(uint64_t)sm.seg * sg.dstride + d] + excl;
+        sm.gbase[d] = (SEGD ? dbase[(uint64_t)sm.seg * sg.dstride + d] : dbase[d]) + excl;
     }
     __syncthreads();
-    ts[4] = clock64();
+    if constexpr (!SEGD) ts[4] = clock64();
     const uint32_t nv = sm.nvalid;
     for (uint32_t s = threadIdx.x; s < nv; s += ST) {
         const uint64_t kk = sm.keys[s];
@@ -317,7 +319,7 @@ __global__ void __launch_bounds__(ST, 3) k_onesweep(const uint64_t *__restrict__
     }
     // [0] tile id, [1] loads and ranks, [2] digit scan, [3] tile order and look-back, [4] stores (cycles);
     // [5] [6] look-back status words read and polls of unposted words (digit 0)
-    if (trace && threadIdx.x == 0) {
+    if (!SEGD && trace && threadIdx.x == 0) {
         const long long te = clock64();
         for (int q = 0; q < 4; q++) atomicAdd(&trace[q], (unsigned long long)(ts[q + 1] - ts[q]));
         atomicAdd(&trace[4], (unsigned long long)(te - ts[4]));
@@ -847,6 +849,10 @@ static void sort_kernel_attrs()
         cudaFuncSetAttribute(k_onesweep<2, 7>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SortSmem));
         cudaFuncSetAttribute(k_onesweep<2, 6>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SortSmem));
         cudaFuncSetAttribute(k_onesweep<2, 5>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SortSmem));
+        cudaFuncSetAttribute(k_onesweep<2, 8, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SortSmem));
+        cudaFuncSetAttribute(k_onesweep<2, 7, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SortSmem));
+        cudaFuncSetAttribute(k_onesweep<2, 6, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SortSmem));
+        cudaFuncSetAttribute(k_onesweep<2, 5, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SortSmem));
         cudaFuncSetAttribute(k_segsort<1024, SS_CAP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SegSmemL));
         cudaFuncSetAttribute(k_segsort<512, SS_SMALL_CAP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SegSmemS));
     });
@@ -966,7 +972,9 @@ int bucket_sort(SortBufs &b, uint64_t n, bool has_hi, int k, const uint64_t *d_h
         const int d = passes[pi];
         const int src = b.cur, dst = b.cur ^ 1;
         const int w = bpl.w[d];
-        auto kern = w >= 8 ? k_onesweep<2, 8> : w == 7 ? k_onesweep<2, 7> : w == 6 ? k_onesweep<2, 6> : k_onesweep<2, 5>;
+        auto kern = segs ? (w >= 8 ? k_onesweep<2, 8, true> : w == 7 ? k_onesweep<2, 7, true> : w == 6 ? k_onesweep<2, 6, true>
+                                                                                               : k_onesweep<2, 5, true>)
+                         : (w >= 8 ? k_onesweep<2, 8> : w == 7 ? k_onesweep<2, 7> : w == 6 ? k_onesweep<2, 6> : k_onesweep<2, 5>);
         (mp::count_launch(), kern<<<(unsigned)tiles, ST, sizeof(SortSmem), st>>>(
             b.lo[src], has_hi ? b.hi[src] : nullptr, b.id[src], b.lo[dst], has_hi ? b.hi[dst] : nullptr, b.id[dst], n,
             bsh + bpl.sh[d], bpl.w[d], dbase + d * 256, dnz + d * 8, status, ctr + pi, (uint32_t)(pi + 1), err, pf,

@@ -37,6 +37,7 @@ constexpr uint64_t UMAX32B = 4294967295ull;
 // after the previous threshold.  rb: every sample's T_q + 1 global tuple bounds at rb0[q]; status[q]:
 // 0, 1 no k-mers, 2 ranges not covering the scan, 3 ranges not monotone over populated buckets.
 constexpr int PLAN_MAX_T = 256;
+constexpr int UPLOAD_SEGMENTS = 8;  // upload segments of a group (each parsed and counted as it arrives)
 
 __device__ __forceinline__ uint64_t lower_bound_dev(const uint64_t *h, uint64_t n, uint64_t x)
 {
@@ -172,56 +173,102 @@ static int run_group(mp_batch *b, const mp_batch_params *p, const mp_batch_sampl
             cudaStreamSynchronize(b->st);
         }
     } release{b};
-    // ---- upload: the samples one after another, each its own copy (the copy stream runs ahead)
+    // ---- upload: the samples one after another, each its own copy (the copy stream runs ahead), in
+    // segments of consecutive samples of about an eighth of the group's bytes each
     uint64_t total_bytes = 0;
     for (Sample &s : g) {
         s.byte0 = total_bytes;
         total_bytes += smp[s.idx].nbytes;
     }
+    std::vector<int> useg{0};  // first sample of every upload segment, then nseg
+    {
+        uint64_t acc = 0;
+        for (int q = 0; q < nseg; q++) {
+            acc += smp[g[q].idx].nbytes;
+            if (q + 1 < nseg && acc * UPLOAD_SEGMENTS >= total_bytes * useg.size()) useg.push_back(q + 1);
+        }
+        useg.push_back(nseg);
+    }
+    const int nu = (int)useg.size() - 1;
     uint8_t *d_fq = A.alloc_persistent<uint8_t>(total_bytes + 64);
     if (!d_fq) return set_error(MP_ENOMEM, "device memory for a group's %llu FASTQ bytes", (unsigned long long)total_bytes);
-    Events ev(nseg + 1, cudaEventDisableTiming);
-    cudaEventRecord(ev[nseg], st);
-    MP_CUDA(cudaStreamWaitEvent(b->copy_st, ev[nseg], 0));
-    for (int q = 0; q < nseg; q++) {
-        const mp_batch_sample &s = smp[g[q].idx];
-        MP_CUDA(cudaMemcpyAsync(d_fq + g[q].byte0, s.fastq, s.nbytes, cudaMemcpyHostToDevice, b->copy_st));
-        cudaEventRecord(ev[q], b->copy_st);
+    Events ev(nu + 1, cudaEventDisableTiming);
+    cudaEventRecord(ev[nu], st);
+    MP_CUDA(cudaStreamWaitEvent(b->copy_st, ev[nu], 0));
+    for (int u = 0; u < nu; u++) {
+        for (int q = useg[u]; q < useg[u + 1]; q++) {
+            const mp_batch_sample &s = smp[g[q].idx];
+            MP_CUDA(cudaMemcpyAsync(d_fq + g[q].byte0, s.fastq, s.nbytes, cudaMemcpyHostToDevice, b->copy_st));
+        }
+        cudaEventRecord(ev[u], b->copy_st);
     }
     MP_CUDA(cudaMemsetAsync(d_fq + total_bytes, 0, 64, st));
-    // ---- per sample: parse, check the chunk starts, k-mer cache and bucket counts
+    // ---- per upload segment, as its bytes arrive: parse, the samples' and their chunks' first records,
+    // k-mer cache and per-sample bucket counts
     uint32_t *cc = A.alloc_persistent<uint32_t>((size_t)nseg * NB);
     uint32_t *err = A.alloc_persistent<uint32_t>(1);
-    if (!cc || !err) return set_error(MP_ENOMEM, "device memory for a group's bucket counts");
+    uint64_t *d_srec = A.alloc_persistent<uint64_t>(nseg + nu);  // each segment's sample read offsets (local)
+    if (!cc || !err || !d_srec) return set_error(MP_ENOMEM, "device memory for a group's bucket counts");
     MP_CUDA(cudaMemsetAsync(cc, 0, (size_t)nseg * NB * sizeof(uint32_t), st));
     MP_CUDA(cudaMemsetAsync(err, 0, 4, st));
-    std::vector<ParsedReads> prs(nseg);
-    std::vector<KcPiece> kc(nseg);
-    std::vector<uint64_t> R(nseg + 1, 0);
-    for (int q = 0; q < nseg; q++) {
-        const mp_batch_sample &s = smp[g[q].idx];
-        MP_CUDA(cudaStreamWaitEvent(st, ev[q], 0));
+    std::vector<ParsedReads> prs(nu);
+    std::vector<KcPiece> kc(nu);
+    std::vector<uint64_t> R(nseg + 1, 0), RU(nu + 1, 0);
+    for (int u = 0; u < nu; u++) {
+        const int qa = useg[u], qb = useg[u + 1];
+        const uint64_t b0 = g[qa].byte0, b1 = g[qb - 1].byte0 + smp[g[qb - 1].idx].nbytes;
+        MP_CUDA(cudaStreamWaitEvent(st, ev[u], 0));
         {
             StageTimer tm(st, &b->stage_ms[0]);
-            if ((rc = parse_fastq_range(d_fq, g[q].byte0, g[q].byte0 + s.nbytes, &prs[q], A, st)))
-                return sample_error(rc, g[q].idx, mp_last_error());
+            rc = parse_fastq_range(d_fq, b0, b1, &prs[u], A, st);
         }
-        const uint64_t n = prs[q].n_reads;
-        if (il && (n & 1)) return sample_error(MP_EFMT, g[q].idx, "interleaved input with an odd record count");
-        if (n & 1) return sample_error(MP_EUNSUP, g[q].idx, "the mate union needs an even read count");
-        g[q].chunk_rec.assign(g[q].starts.size(), 0);
-        if ((rc = records_at_offsets(&prs[q], g[q].starts.data(), (int)g[q].starts.size(), g[q].chunk_rec.data(), A, st)))
-            return sample_error(rc, g[q].idx, mp_last_error());
-        if (il)
-            for (size_t c = 0; c + 1 < g[q].chunk_rec.size(); c++)
-                if ((g[q].chunk_rec[c + 1] - g[q].chunk_rec[c]) & 1)
-                    return sample_error(MP_EFMT, g[q].idx, "an interleaved chunk has an odd record count");
-        R[q + 1] = R[q] + n;
+        if (rc) {  // name the sample: parse the segment's samples one by one until one fails
+            const std::string msg = mp_last_error();
+            for (int q = qa; q < qb; q++) {
+                ParsedReads one;
+                const int r1 = parse_fastq_range(d_fq, g[q].byte0, g[q].byte0 + smp[g[q].idx].nbytes, &one, A, st);
+                A.free_persistent(one.rec_start);
+                A.free_persistent(one.seq_off);
+                A.free_persistent(one.seq_len);
+                if (r1) return sample_error(r1, g[q].idx, mp_last_error());
+            }
+            return set_error(rc, "samples %d..%d: %s", g[qa].idx, g[qb - 1].idx, msg.c_str());
+        }
+        // every sample's chunk starts (its first is its own start, its last its end), relative to the segment
+        std::vector<uint64_t> qs, qr;
+        for (int q = qa; q < qb; q++)
+            for (uint64_t x : g[q].starts) qs.push_back(g[q].byte0 - b0 + x);
+        qr.assign(qs.size(), 0);
+        rc = records_at_offsets(&prs[u], qs.data(), (int)qs.size(), qr.data(), A, st);
+        for (int q = qa, at = 0; q < qb; q++) {
+            const int nq = (int)g[q].starts.size();
+            for (int c = 0; c < nq; c++)
+                if (qr[at + c] == ~0ull)
+                    return sample_error(MP_EFMT, g[q].idx, c == nq - 1 ? "the FASTQ does not end on a record end"
+                                                                     : "a chunk does not start on a record");
+            g[q].chunk_rec.assign(nq, 0);
+            for (int c = 0; c < nq; c++) g[q].chunk_rec[c] = qr[at + c] - qr[at];
+            const uint64_t n = g[q].chunk_rec[nq - 1];
+            if (il && (n & 1)) return sample_error(MP_EFMT, g[q].idx, "interleaved input with an odd record count");
+            if (n & 1) return sample_error(MP_EUNSUP, g[q].idx, "the mate union needs an even read count");
+            if (il)
+                for (int c = 0; c + 1 < nq; c++)
+                    if ((g[q].chunk_rec[c + 1] - g[q].chunk_rec[c]) & 1)
+                        return sample_error(MP_EFMT, g[q].idx, "an interleaved chunk has an odd record count");
+            R[q + 1] = R[q] + n;
+            at += nq;
+        }
+        if (rc) return rc;
+        RU[u + 1] = R[qb];
         StageTimer tm(st, &b->stage_ms[1]);
-        if (!make_kc_piece(A, st, prs[q], R[q], k, &kc[q]))
-            return sample_error(MP_ENOMEM, g[q].idx, "device memory for the k-mer cache");
-        launch_count(d_fq + g[q].byte0, prs[q], k, 0, (const uint64_t *)d_fq, 1, cc + (size_t)q * NB, nullptr, err, st,
-                     kc[q].off, kc[q].lo, kc[q].hi);
+        if (!make_kc_piece(A, st, prs[u], RU[u], k, &kc[u]))
+            return set_error(MP_ENOMEM, "device memory for the k-mer cache of samples %d..%d", g[qa].idx, g[qb - 1].idx);
+        std::vector<uint64_t> loc(qb - qa + 1);
+        for (int q = qa; q <= qb; q++) loc[q - qa] = R[q] - RU[u];
+        uint64_t *dl = d_srec + qa + u;
+        MP_CUDA(cudaMemcpyAsync(dl, loc.data(), loc.size() * 8, cudaMemcpyHostToDevice, st));
+        launch_count(d_fq + b0, prs[u], k, 0, dl, qb - qa, cc + (size_t)qa * NB, nullptr, err, st, kc[u].off, kc[u].lo,
+                     kc[u].hi);
     }
     const uint64_t N = R[nseg];
     if (N >= UMAX32B) return set_error(MP_EUNSUP, "a group of more than 2^32 - 2 reads");
@@ -234,7 +281,7 @@ static int run_group(mp_batch *b, const mp_batch_params *p, const mp_batch_sampl
         pr.seq_off = A.alloc_persistent<uint64_t>(N + 1);
         pr.seq_len = A.alloc_persistent<uint32_t>(N + 1);
         if (!pr.rec_start || !pr.seq_off || !pr.seq_len) return set_error(MP_ENOMEM, "device memory for the read table");
-        for (int q = 0; q < nseg; q++) concat_records(prs[q], g[q].byte0, pr, R[q], st);
+        for (int u = 0; u < nu; u++) concat_records(prs[u], g[useg[u]].byte0, pr, RU[u], st);
     }
     for (auto &x : prs) {
         A.free_persistent(x.rec_start);
@@ -295,8 +342,8 @@ static int run_group(mp_batch *b, const mp_batch_params *p, const mp_batch_sampl
         if (!cnt || !d_b || !off || !ntot || !tmp) return set_error(MP_ENOMEM, "device memory for enumeration offsets");
         const uint32_t hb[2] = {0, NB};
         MP_CUDA(cudaMemcpyAsync(d_b, hb, 8, cudaMemcpyHostToDevice, st));
-        for (int q = 0; q < nseg; q++)
-            if (kc[q].n && launch_kc_count_scans(kc[q].off, kc[q].lo, kc[q].hi, kc[q].n, k, d_b, 1, cnt + kc[q].r0, N + 1, err, st))
+        for (const KcPiece &q : kc)
+            if (q.n && launch_kc_count_scans(q.off, q.lo, q.hi, q.n, k, d_b, 1, cnt + q.r0, N + 1, err, st))
                 return set_error(MP_EARG, "enumeration count");
         MP_CUDA(cudaMemsetAsync(cnt + N, 0, 4, st));
         scan_u32_to_u64(cnt, off, N + 1, ntot, tmp, tb, st);
@@ -318,9 +365,8 @@ static int run_group(mp_batch *b, const mp_batch_params *p, const mp_batch_sampl
             if (!sb.lo[x] || !sb.id[x] || (has_hi && !sb.hi[x]))
                 return set_error(MP_ENOMEM, "device memory for %llu tuples", (unsigned long long)n);
         }
-        for (int q = 0; q < nseg; q++)
-            launch_kc_write(kc[q].off, kc[q].lo, kc[q].hi, kc[q].r0, kc[q].n, k, 0, NB, nullptr, off, sb.lo[0], sb.hi[0],
-                            sb.id[0], st);
+        for (const KcPiece &q : kc)
+            launch_kc_write(q.off, q.lo, q.hi, q.r0, q.n, k, 0, NB, nullptr, off, sb.lo[0], sb.hi[0], sb.id[0], st);
         for (auto &x : kc) free_kc_piece(A, x);
         A.release_scratch();
     }
@@ -516,6 +562,7 @@ int mp_batch_run(mp_batch *b, const mp_batch_params *p, int nsamples, const mp_b
         int rc = mp_fastq_index(s.num_chunks, 0, p->interleaved ? 0 : 1, p->interleaved ? 1 : 0, 1, files, sizes, fno.data(),
                                 ofs.data(), &cnt);
         if (rc) return sample_error(rc, q, mp_last_error());
+        if (cnt < 2 || ofs[0] != 0) return sample_error(MP_EFMT, q, "too short for a chunk index");
         if ((cnt - 1) % s.num_threads) return sample_error(MP_EARG, q, "numThreads must divide the number of chunks");
         all[q].idx = q;
         all[q].starts.assign(ofs.begin(), ofs.begin() + cnt);
