@@ -113,6 +113,9 @@ __device__ __forceinline__ void mark_tuple(uint32_t J, uint64_t q, uint32_t adj,
 // before/after adjacency-code counts by popcount.  A run still open at the end of a window is
 // carried: while it is uniform its counts follow from its length and byte; when it spans windows
 // its marks are applied by one more pass over it after it is judged.
+// MULTI: the thread ranges of several scans one after another (a batch of samples), whose boundaries may
+// cut a run of equal k-mers; within one scan ranges cut runs only between buckets.
+template <bool MULTI>
 __global__ void __launch_bounds__(256) k_filter_warp(const uint64_t *lo, const uint8_t *hi, const uint32_t *id,
                                                      uint64_t n, const uint64_t *range_ends, int T, uint32_t *parent,
                                                      uint8_t *filtered, uint32_t *z)
@@ -153,12 +156,16 @@ __global__ void __launch_bounds__(256) k_filter_warp(const uint64_t *lo, const u
         }
         ne = lo_i;
     }
+    uint64_t nxt_end = ne < T ? ends[ne] : ~0ull;  // the next range end at or after the window
     for (uint64_t p = c0;; p += 32) {
         const bool owned = p < c1;
         if (!owned && !open) break;
         uint64_t emask = 0;
-        while (ne < T && ends[ne] < p + 32) emask |= 1ull << (ends[ne++] - p);
-        if (ne < T && ends[ne] == p + 32) emask |= 1ull << 32;
+        while (nxt_end < p + 32) {
+            emask |= 1ull << (nxt_end - p);
+            nxt_end = ++ne < T ? ends[ne] : ~0ull;
+        }
+        if (nxt_end == p + 32) emask |= 1ull << 32;
         const uint64_t i = p + lane;
         const bool valid = i < n;
         const uint64_t lv = nlv;
@@ -175,7 +182,7 @@ __global__ void __launch_bounds__(256) k_filter_warp(const uint64_t *lo, const u
             pa = prev_adj;
         }
         // a thread range starts a run whatever the k-mer before it (each range is its own sweep)
-        const bool head = valid && (i == 0 || km != pk || ((emask >> lane) & 1u));
+        const bool head = valid && (i == 0 || km != pk || (MULTI && ((emask >> lane) & 1u)));
         const uint32_t H = __ballot_sync(FULLW, head), V = __ballot_sync(FULLW, valid);
         const uint32_t D = __ballot_sync(FULLW, valid && !head && adj != pa);
         const uint32_t run_adj = prev_adj;  // byte of a uniform carried run
@@ -367,6 +374,10 @@ struct EdgeCtx {
 // anchor is the scan's first read (the sweep's initial state, :2539-2548).  One warp per
 // SEG tuples, windows of 32 as in the filter; the anchor of a run still open at the end of a
 // window is carried.
+// MULTI: many thread ranges of several scans (a batch of samples): a range start is a run head whatever the
+// k-mer before it, and every range has its own initial state (c.r_*), found by cursors over the ranges.
+// Without it (one scan), ranges cut runs only between buckets and the initial state is the scan's own.
+template <bool MULTI>
 __global__ void __launch_bounds__(256) k_edges_warp(EdgeCtx c)
 {
     const int lane = threadIdx.x & 31;
@@ -378,8 +389,9 @@ __global__ void __launch_bounds__(256) k_edges_warp(EdgeCtx c)
     uint32_t anchor = 0;
     // cursors over the thread ranges: their starts (run heads) and their first valid tuples (the positions
     // where a range's sweep may take the scan's initial state); both ascend with the range index
-    int nb, nf;
-    {
+    int nb = 0, nf = 0;
+    uint64_t nxt_b = ~0ull, nxt_f = ~0ull;  // the next range start, the next range's first valid tuple
+    if constexpr (MULTI) {
         int a = 1, b = c.T;  // first t in [1, T] with range_bounds[t] >= c0 (T when none)
         while (a < b) {
             const int m = (a + b) >> 1;
@@ -392,6 +404,9 @@ __global__ void __launch_bounds__(256) k_edges_warp(EdgeCtx c)
             if (c.range_bounds[m] <= c0) a = m; else b = m - 1;
         }
         nf = a;
+        nxt_b = nb < c.T ? c.range_bounds[nb] : ~0ull;
+        nxt_f = c.first_valid[nf];
+        while (nxt_f == ~0ull && ++nf < c.T) nxt_f = c.first_valid[nf];
     }
     uint64_t prev_km = c0 ? kmer_of(c.lo, c.hi, c0 - 1) : 0;
     // the next window's k-mer, read id and zero-mark word (windows start at multiples of 32), loaded one
@@ -414,22 +429,22 @@ __global__ void __launch_bounds__(256) k_edges_warp(EdgeCtx c)
         }
         uint32_t smask = 0, fmask = 0;  // lanes at a range start, lanes at a range's first valid tuple
         int my_t = 0;                   // the range whose first valid tuple this lane holds
-        while (nb < c.T && c.range_bounds[nb] < p + 32) {
-            if (c.range_bounds[nb] >= p) smask |= 1u << (c.range_bounds[nb] - p);
-            nb++;
+        while (MULTI && nxt_b < p + 32) {
+            if (nxt_b >= p) smask |= 1u << (nxt_b - p);
+            nxt_b = ++nb < c.T ? c.range_bounds[nb] : ~0ull;
         }
-        while (nf < c.T) {
-            const uint64_t f = c.first_valid[nf];
-            if (f != ~0ull && f >= p + 32) break;
-            if (f != ~0ull && f >= p) {
-                fmask |= 1u << (f - p);
-                if ((uint64_t)lane == f - p) my_t = nf;
+        while (MULTI && nxt_f < p + 32) {  // ranges without a valid tuple (~0) never enter
+            if (nxt_f >= p) {
+                fmask |= 1u << (nxt_f - p);
+                if ((uint64_t)lane == nxt_f - p) my_t = nf;
             }
-            nf++;
+            do {
+                nxt_f = ++nf < c.T ? c.first_valid[nf] : ~0ull;
+            } while (nf < c.T && nxt_f == ~0ull);
         }
         uint64_t pk = __shfl_up_sync(FULLW, km, 1);
         if (lane == 0) pk = prev_km;
-        const bool head = valid && (i == 0 || km != pk || ((smask >> lane) & 1u));
+        const bool head = valid && (i == 0 || km != pk || ((smask >> lane) & 1u));  // smask: MULTI only
         const uint32_t H = __ballot_sync(FULLW, head);
         prev_km = __shfl_sync(FULLW, km, 31);
         const bool nz = valid && km != 0 && !((zw >> lane) & 1u);
@@ -450,10 +465,22 @@ __global__ void __launch_bounds__(256) k_edges_warp(EdgeCtx c)
         // quirk check by the lane holding a run's first good tuple when the run has no anchor yet
         uint32_t aval = r;
         bool quirk = false;
-        if (good && lane == fg && !(carried && has_anchor) && ((fmask >> lane) & 1u)) {
-            const uint64_t ik = c.r_kmer ? c.r_kmer[my_t] : c.init_kmer;
-            const bool ok = c.r_ok ? c.r_ok[my_t] != 0 : c.init_min_ok != 0;
-            if (km == ik && ok) { quirk = true; aval = c.r_min ? c.r_min[my_t] : c.init_min; }
+        if constexpr (MULTI) {
+            if (good && lane == fg && !(carried && has_anchor) && ((fmask >> lane) & 1u) && km == c.r_kmer[my_t] &&
+                c.r_ok[my_t]) {
+                quirk = true;
+                aval = c.r_min[my_t];
+            }
+        } else if (good && lane == fg && !(carried && has_anchor) && km == c.init_kmer && c.init_min_ok) {
+            int lo = 0, hi = c.T - 1;  // the range holding i: the quirk is its first valid tuple's alone
+            while (lo < hi) {
+                const int m = (lo + hi + 1) >> 1;
+                if (c.range_bounds[m] <= i) lo = m; else hi = m - 1;
+            }
+            if (c.first_valid[lo] == i) {
+                quirk = true;
+                aval = c.init_min;
+            }
         }
         const uint32_t av = __shfl_sync(FULLW, aval, fg < 0 ? 0 : fg);
         const bool qk = __shfl_sync(FULLW, quirk, fg < 0 ? 0 : fg);
@@ -680,7 +707,7 @@ __global__ void k_pe_bigsmall(uint32_t *parent, uint32_t *size, const uint32_t *
 static unsigned blocks_for(uint64_t n, int t) { return (unsigned)((n + t - 1) / t); }
 
 int filter_scan(Tuples &tp, const std::vector<uint64_t> &range_bounds, uint32_t *parent, uint8_t *filtered,
-                DeviceArena &arena, cudaStream_t st, bool apply_zero)
+                DeviceArena &arena, cudaStream_t st, bool apply_zero, bool multi)
 {
     const uint64_t n = tp.n;
     const int T = (int)range_bounds.size() - 1;
@@ -691,8 +718,12 @@ int filter_scan(Tuples &tp, const std::vector<uint64_t> &range_bounds, uint32_t 
     if (n == 0) return 0;
     MP_CUDA(cudaMemcpyAsync(ends, range_bounds.data() + 1, T * sizeof(uint64_t), cudaMemcpyHostToDevice, st));
     const uint64_t warps = (n + SEG - 1) / SEG;
-    (mp::count_launch(), k_filter_warp<<<blocks_for(warps * 32, 256), 256, 0, st>>>(tp.lo, tp.hi, tp.id, n, ends, T, parent,
-                                                                                   filtered, tp.z));
+    if (multi)
+        (mp::count_launch(), k_filter_warp<true><<<blocks_for(warps * 32, 256), 256, 0, st>>>(tp.lo, tp.hi, tp.id, n, ends, T,
+                                                                                         parent, filtered, tp.z));
+    else
+        (mp::count_launch(), k_filter_warp<false><<<blocks_for(warps * 32, 256), 256, 0, st>>>(tp.lo, tp.hi, tp.id, n, ends, T,
+                                                                                          parent, filtered, tp.z));
     if (apply_zero) (mp::count_launch(), k_apply_zero<<<blocks_for(n, 256), 256, 0, st>>>(tp.lo, tp.hi, n, tp.z));
     MP_CUDA(cudaGetLastError());
     return 0;
@@ -735,7 +766,7 @@ int union_scan(Tuples &tp, const std::vector<uint64_t> &range_bounds, uint32_t *
         (mp::count_launch(), k_range_first_valid<<<blocks_for(T, 64), 64, 0, st>>>(tp.lo, tp.hi, tp.id, tp.z, bounds, T, parent,
                                                                                   first));
         const uint64_t warps = (n + SEG - 1) / SEG;
-        (mp::count_launch(), k_edges_warp<<<blocks_for(warps * 32, 256), 256, 0, st>>>(c));
+        (mp::count_launch(), k_edges_warp<false><<<blocks_for(warps * 32, 256), 256, 0, st>>>(c));
     }
     (mp::count_launch(), k_compress<<<blocks_for(n_reads, 256), 256, 0, st>>>(parent, n_reads));
     uint32_t herr = 0;
@@ -781,7 +812,7 @@ int union_piece(Tuples &tp, const std::vector<uint64_t> &bounds, const std::vect
     c.r_ok = nullptr;
     c.uf_cap = arena.lim.union_retries;
     const uint64_t warps = (n + SEG - 1) / SEG;
-    (mp::count_launch(), k_edges_warp<<<blocks_for(warps * 32, 256), 256, 0, st>>>(c));
+    (mp::count_launch(), k_edges_warp<false><<<blocks_for(warps * 32, 256), 256, 0, st>>>(c));
     uint32_t herr = 0;
     MP_CUDA(cudaMemcpyAsync(&herr, err, sizeof herr, cudaMemcpyDeviceToHost, st));
     MP_CUDA(cudaStreamSynchronize(st));
@@ -961,7 +992,7 @@ int union_segments(Tuples &tp, const std::vector<uint64_t> &range_bounds, const 
         c.r_ok = ro;
         c.uf_cap = arena.lim.union_retries;
         const uint64_t warps = (n + SEG - 1) / SEG;
-        (mp::count_launch(), k_edges_warp<<<blocks_for(warps * 32, 256), 256, 0, st>>>(c));
+        (mp::count_launch(), k_edges_warp<true><<<blocks_for(warps * 32, 256), 256, 0, st>>>(c));
     }
     (mp::count_launch(), k_compress<<<blocks_for(n_reads, 256), 256, 0, st>>>(parent, n_reads));
     uint32_t herr = 0;

@@ -15,8 +15,9 @@ struct Tuples {
 };
 
 // K4: markMischiefKmers over the scan; range_bounds = T + 1 tuple bounds of the thread ranges.
+// multi: the ranges of several scans one after another (a batch of samples), whose boundaries may cut a run.
 int filter_scan(Tuples &tp, const std::vector<uint64_t> &range_bounds, uint32_t *parent, uint8_t *filtered,
-                DeviceArena &arena, cudaStream_t st, bool apply_zero);
+                DeviceArena &arena, cudaStream_t st, bool apply_zero, bool multi = false);
 // K5: unionFindPar2 + unionFind + printStats compression for the scan.
 int union_scan(Tuples &tp, const std::vector<uint64_t> &range_bounds, uint32_t *parent, const uint8_t *filtered,
                uint64_t n_reads, DeviceArena &arena, cudaStream_t st);

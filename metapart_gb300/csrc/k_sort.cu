@@ -10,6 +10,8 @@
 // pass: a CTA ranks its 4096-tuple tile with warp-level multi-split, publishes its digit
 // counts, looks back over earlier tiles for its global offsets, reorders the tile in
 // shared memory and writes each digit's run contiguously.
+#include <dlfcn.h>
+
 #include <algorithm>
 #include <cstddef>
 #include <cstdlib>
@@ -808,27 +810,97 @@ __global__ void k_bp_gather(uint64_t nblk, const uint32_t *nu_blk, const uint64_
     }
 }
 
-// Widest digit of the unit sort (MP_UNIT_SORT_MAX_BITS, 5..10; default 10).  The tests also run
-// narrower digits, which change every unit's pass plan.
-static int unit_sort_max_bits()
+// ---- the bucket sort's plan knobs, by k and scan size
+//
+// Three knobs shape the bucket sort: the bucket digits (the scan's varying bits in passes of near-equal
+// width, or the bucket's bytes: MP_SORT_BUCKET_DIGITS=bytes), the unit sort's widest digit (5..9 bits:
+// MP_UNIT_SORT_MAX_BITS) and how far ahead a digit-pass tile prefetches its successor (SM waves:
+// MP_ONESWEEP_PF_WAVES, 0 = none).  Their values come from the environment when set, else from the table
+// the autotuner (metapart_gb300/autotune.py) measured -- rows "k min_tuples digits unit_bits pf_waves",
+// the row of the nearest k and the largest min_tuples not above the scan's tuples -- read once per process
+// from MP_SORT_TUNING or sort_tuning.tsv one directory above the library, else the defaults below (one
+// wave ahead measured best at 20M reads: 57.8 ms for the digit passes at one wave, 58.4 at two, 60.6 at
+// three, 64.6 without).
+struct SortTuning {
+    bool byte_digits = false;
+    int unit_bits = SS_MAXBITS;
+    int pf_waves = 1;
+};
+
+struct TuneRow {
+    int k;
+    uint64_t min_tuples;
+    SortTuning t;
+};
+
+static std::vector<TuneRow> g_tune;
+static std::once_flag g_tune_once;
+
+static void load_tuning()
 {
-    const char *e = getenv("MP_UNIT_SORT_MAX_BITS");
-    const int v = e && *e ? atoi(e) : SS_MAXBITS;
-    return v < 5 ? 5 : (v > SS_MAXBITS ? SS_MAXBITS : v);
+    std::string path;
+    const char *e = getenv("MP_SORT_TUNING");
+    if (e && *e) {
+        path = e;
+    } else {
+        Dl_info info;
+        if (dladdr((void *)&load_tuning, &info) && info.dli_fname) {
+            path = info.dli_fname;
+            const size_t cut = path.find_last_of('/');
+            path = (cut == std::string::npos ? std::string(".") : path.substr(0, cut)) + "/../sort_tuning.tsv";
+        }
+    }
+    FILE *f = path.empty() ? nullptr : fopen(path.c_str(), "r");
+    if (!f) return;
+    char line[256];
+    while (fgets(line, sizeof line, f)) {
+        if (line[0] == '#') continue;
+        int k = 0, bits = 0, pf = 0;
+        unsigned long long mt = 0;
+        char dig[32] = {0};
+        if (sscanf(line, "%d %llu %31s %d %d", &k, &mt, dig, &bits, &pf) != 5) continue;
+        TuneRow r;
+        r.k = k;
+        r.min_tuples = mt;
+        r.t.byte_digits = std::string(dig) == "bytes";
+        r.t.unit_bits = bits < 5 ? 5 : (bits > SS_MAXBITS ? SS_MAXBITS : bits);
+        r.t.pf_waves = pf < 0 ? 0 : (pf > 16 ? 16 : pf);
+        g_tune.push_back(r);
+    }
+    fclose(f);
 }
 
-// MP_SORT_BUCKET_DIGITS=bytes: the bucket sort's digit passes take the bucket's bytes (three passes
-// over a 20-bit bucket) instead of the scan's varying bits in passes of near-equal width.
-static bool byte_bucket_digits()
+static SortTuning sort_tuning(int k, uint64_t n)
 {
+    std::call_once(g_tune_once, load_tuning);
+    SortTuning t;
+    int bk = -1;
+    uint64_t bmt = 0;
+    for (const TuneRow &r : g_tune) {  // nearest k, then the largest min_tuples <= n
+        const int dk = std::abs(r.k - k), dbk = bk < 0 ? 1 << 30 : std::abs(bk - k);
+        if (r.min_tuples > n || dk > dbk) continue;
+        if (dk < dbk || r.min_tuples >= bmt) {
+            t = r.t;
+            bk = r.k;
+            bmt = r.min_tuples;
+        }
+    }
     const char *e = getenv("MP_SORT_BUCKET_DIGITS");
-    return e && std::string(e) == "bytes";
+    if (e && *e) t.byte_digits = std::string(e) == "bytes";
+    e = getenv("MP_UNIT_SORT_MAX_BITS");
+    if (e && *e) {
+        const int v = atoi(e);
+        t.unit_bits = v < 5 ? 5 : (v > SS_MAXBITS ? SS_MAXBITS : v);
+    }
+    e = getenv("MP_ONESWEEP_PF_WAVES");
+    if (e && *e) {
+        const int w = atoi(e);
+        t.pf_waves = w < 0 ? 0 : (w > 16 ? 16 : w);
+    }
+    return t;
 }
 
-// How far ahead (in tiles) a digit-pass tile prefetches its successor into L2: a number of SM
-// waves (MP_ONESWEEP_PF_WAVES, 0 = no prefetch) times the SM count.  Three tiles are resident per
-// SM; one wave ahead measured best (the bucket-digit passes at 20M reads: 57.8 ms at one wave,
-// 58.4 at two, 60.6 at three, 64.6 without).
+// Prefetch distance of the device-wide sort (no k or scan plan): MP_ONESWEEP_PF_WAVES or one wave.
 static uint32_t onesweep_prefetch_tiles()
 {
     const char *e = getenv("MP_ONESWEEP_PF_WAVES");
@@ -871,6 +943,7 @@ int bucket_sort(SortBufs &b, uint64_t n, bool has_hi, int k, const uint64_t *d_h
         return set_error(MP_EARG, "segmented bucket sort: the buckets must be the segments' NB each");
     const int bsh = 2 * (k - 10), lowbits = 2 * (k - 10) + 8;
     const uint64_t nbk = scan_hi - scan_lo;
+    const SortTuning tune = sort_tuning(k, n);
     // ---- plan on the device: digit offsets of the passes, populated buckets.  The scan's varying bucket
     // bits (those of scan_lo ^ (scan_hi - 1); every bucket bit with segments) are split into the fewest
     // passes of at most 8 bits, of near-equal widths (19 bits: 7 + 6 + 6), so no pass ranks or looks back
@@ -879,7 +952,7 @@ int bucket_sort(SortBufs &b, uint64_t n, bool has_hi, int k, const uint64_t *d_h
     {
         int vb = 0;
         for (uint64_t v = segs ? (uint64_t)(NB - 1) : (scan_lo ^ (scan_hi - 1)); v; v >>= 1) vb++;
-        if (byte_bucket_digits()) {
+        if (tune.byte_digits) {
             bpl.np = 3;
             for (int p = 0; p < 3; p++) bpl.sh[p] = 8 * p, bpl.w[p] = 8;
         } else {
@@ -958,7 +1031,7 @@ int bucket_sort(SortBufs &b, uint64_t n, bool has_hi, int k, const uint64_t *d_h
     MP_CUDA(cudaMemsetAsync(err, 0, sizeof(uint32_t), st));
     if (status) MP_CUDA(cudaMemsetAsync(status, 0, tiles * 256 * sizeof(unsigned long long), st));
     sort_kernel_attrs();
-    const uint32_t pf = onesweep_prefetch_tiles();
+    const uint32_t pf = (uint32_t)tune.pf_waves * (uint32_t)sm_count();
     Segs sg;
     if (segs) {
         sg.tile0 = d_tile0;
@@ -1021,7 +1094,7 @@ int bucket_sort(SortBufs &b, uint64_t n, bool has_hi, int k, const uint64_t *d_h
         (mp::count_launch(), k_segsort<512, SS_SMALL_CAP><<<(unsigned)std::min<uint64_t>(nu, 2ull * (uint64_t)sm_count()), 512,
                                                             sizeof(SegSmemS), st>>>(
             d_us, d_uc, d_ub, (uint32_t)nu, b.lo[in], has_hi ? b.hi[in] : nullptr, b.id[in], b.lo[out], b.id[out], bsh,
-            lowbits, unit_sort_max_bits(), trace));
+            lowbits, tune.unit_bits, trace));
     // buckets above a small unit: up to SS_CAP tuples each is a unit of its own for the 1024-thread blocks,
     // the rest take the device-wide sort
     std::vector<uint32_t> bc;
@@ -1057,7 +1130,7 @@ int bucket_sort(SortBufs &b, uint64_t n, bool has_hi, int k, const uint64_t *d_h
             (mp::count_launch(), k_segsort<1024, SS_CAP><<<(unsigned)std::min<uint64_t>(nm, (uint64_t)sm_count()), 1024,
                                                           sizeof(SegSmemL), st>>>(
                 d_ms, d_mc, d_mk, (uint32_t)nm, b.lo[in], has_hi ? b.hi[in] : nullptr, b.id[in], b.lo[out], b.id[out], bsh,
-                lowbits, unit_sort_max_bits(), trace));
+                lowbits, tune.unit_bits, trace));
         }
         if (nb) {  // the oversized buckets, in order, at the front of the lists
             MP_CUDA(cudaMemcpyAsync(d_bs, gs.data(), nb * 8, cudaMemcpyHostToDevice, st));

@@ -114,8 +114,9 @@ using namespace mp;
 struct mp_batch {
     mp_ctx *ctx = nullptr;
     int device = 0;
-    cudaStream_t st = nullptr, copy_st = nullptr;
-    DeviceArena arena;
+    cudaStream_t st = nullptr, copy_st = nullptr, dl_st = nullptr;  // kernels, uploads, downloads
+    DeviceArena arena;  // a group's stage state, released once the group's kernels are queued
+    DeviceArena io;     // the groups' FASTQ and partition-file bytes: freed once their copies are done
     double stage_ms[8] = {0};
     int groups = 0;
     double sort_pass_ms = 0;
@@ -155,22 +156,41 @@ uint64_t estimate_sample(const char *fq, uint64_t nbytes, int k)
 
 }  // namespace
 
-// One group of samples through every stage.
+// A group's FASTQ and partition-file buffers whose copies to the host are still queued (done: recorded
+// after them on the download stream).
+struct PendingIO {
+    uint8_t *fq = nullptr, *out = nullptr;
+    cudaEvent_t done = nullptr;
+};
+
+static void retire(mp_batch *b, PendingIO &x)
+{
+    if (x.done) {
+        cudaEventSynchronize(x.done);
+        cudaEventDestroy(x.done);
+    }
+    b->io.free_persistent(x.fq);
+    b->io.free_persistent(x.out);
+    x = PendingIO{};
+}
+
+// One group of samples through every stage.  Its partition files' copies to the host are queued at the end
+// on their own stream and keep running during the next group's kernels (pending); the previous group's
+// buffers (older) go back once this group's upload and count are done.
 static int run_group(mp_batch *b, const mp_batch_params *p, const mp_batch_sample *smp, std::vector<Sample> &g,
-                     mp_batch_result *res)
+                     PendingIO &older, PendingIO &pending, mp_batch_result *res)
 {
     cudaStream_t st = b->st;
     DeviceArena &A = b->arena;
     const int k = p->k, il = p->interleaved ? 1 : 0, nseg = (int)g.size();
     const bool has_hi = 2 * k + 8 > 64;
     int rc = 0;
-    struct Release {  // every device allocation of the group goes back on every return path
+    struct Release {  // the group's stage state goes back on every return path (stream-ordered frees)
         mp_batch *b;
         ~Release()
         {
             cudaStreamSynchronize(b->copy_st);
             b->arena.release_all();
-            cudaStreamSynchronize(b->st);
         }
     } release{b};
     // ---- upload: the samples one after another, each its own copy (the copy stream runs ahead), in
@@ -190,7 +210,8 @@ static int run_group(mp_batch *b, const mp_batch_params *p, const mp_batch_sampl
         useg.push_back(nseg);
     }
     const int nu = (int)useg.size() - 1;
-    uint8_t *d_fq = A.alloc_persistent<uint8_t>(total_bytes + 64);
+    uint8_t *d_fq = b->io.alloc_persistent<uint8_t>(total_bytes + 64);
+    pending.fq = d_fq;  // from here on the caller frees it
     if (!d_fq) return set_error(MP_ENOMEM, "device memory for a group's %llu FASTQ bytes", (unsigned long long)total_bytes);
     Events ev(nu + 1, cudaEventDisableTiming);
     cudaEventRecord(ev[nu], st);
@@ -270,6 +291,9 @@ static int run_group(mp_batch *b, const mp_batch_params *p, const mp_batch_sampl
         launch_count(d_fq + b0, prs[u], k, 0, dl, qb - qa, cc + (size_t)qa * NB, nullptr, err, st, kc[u].off, kc[u].lo,
                      kc[u].hi);
     }
+    // the previous group's files have gone down during this group's upload and count: its buffers go back
+    // before this group's tuples are allocated
+    retire(b, older);
     const uint64_t N = R[nseg];
     if (N >= UMAX32B) return set_error(MP_EUNSUP, "a group of more than 2^32 - 2 reads");
     // ---- one read table for the group, global read ids
@@ -400,7 +424,7 @@ static int run_group(mp_batch *b, const mp_batch_params *p, const mp_batch_sampl
     MP_CUDA(cudaMemsetAsync(filtered, 0, N + 1, st));
     {
         StageTimer tm(st, &b->stage_ms[4]);
-        if ((rc = filter_scan(tp, rb, parent, filtered, A, st, false))) return rc;
+        if ((rc = filter_scan(tp, rb, parent, filtered, A, st, false, true))) return rc;
     }
     {
         std::vector<uint32_t> rseg(Rn);
@@ -452,8 +476,24 @@ static int run_group(mp_batch *b, const mp_batch_params *p, const mp_batch_sampl
         memcpy(r.bounds, &bounds[(size_t)q * 17], sizeof r.bounds);
         if (s.file_sizes) memcpy(s.file_sizes, &fsz[file0[q]], 16ull * Ts[q] * sizeof(uint64_t));
     }
-    uint8_t *d_out = A.alloc_persistent<uint8_t>(plan.total + 16);
+    // labels first (the forest goes back with the group's stage state)
+    for (int q = 0; q < nseg; q++) {
+        const mp_batch_sample &s = smp[g[q].idx];
+        const uint64_t n = R[q + 1] - R[q];
+        if (!s.labels) continue;
+        if (s.labels_cap < n) return sample_error(MP_EARG, g[q].idx, "labels buffer too small");
+        MP_CUDA(cudaMemcpyAsync(s.labels, parent + R[q], n * 4, cudaMemcpyDeviceToHost, st));
+    }
+    MP_CUDA(cudaStreamSynchronize(st));
+    for (int q = 0; q < nseg; q++) {  // labels in each sample's own read ids
+        const mp_batch_sample &s = smp[g[q].idx];
+        if (!s.labels) continue;
+        const uint64_t n = R[q + 1] - R[q];
+        for (uint64_t x = 0; x < n; x++) s.labels[x] -= (uint32_t)R[q];
+    }
+    uint8_t *d_out = b->io.alloc_persistent<uint8_t>(plan.total + 16);
     if (!d_out) return set_error(MP_ENOMEM, "device memory for the output bytes");
+    pending.out = d_out;
     {
         constexpr int KB = 8;
         StageTimer tm(st, &b->stage_ms[7]);
@@ -469,31 +509,19 @@ static int run_group(mp_batch *b, const mp_batch_params *p, const mp_batch_sampl
         for (int x = 0; x < KB; x++) {
             if ((rc = copy_output_range(plan, e[x], e[x + 1], d_fq, d_out, st))) return rc;
             cudaEventRecord(bev[x], st);
-            MP_CUDA(cudaStreamWaitEvent(b->copy_st, bev[x], 0));
+            MP_CUDA(cudaStreamWaitEvent(b->dl_st, bev[x], 0));
             for (int q = 0; q < nseg; q++) {  // the part of each sample's bytes this batch built
                 const mp_batch_sample &s = smp[g[q].idx];
                 const uint64_t s0 = fb[file0[q]], s1 = fb[file0[q + 1]];
                 const uint64_t a = std::max(s0, o[x]), z = std::min(s1, o[x + 1]);
                 if (s.out && a < z)
-                    MP_CUDA(cudaMemcpyAsync(s.out + (a - s0), d_out + a, z - a, cudaMemcpyDeviceToHost, b->copy_st));
+                    MP_CUDA(cudaMemcpyAsync(s.out + (a - s0), d_out + a, z - a, cudaMemcpyDeviceToHost, b->dl_st));
             }
         }
-        for (int q = 0; q < nseg; q++) {
-            const mp_batch_sample &s = smp[g[q].idx];
-            const uint64_t n = R[q + 1] - R[q];
-            if (!s.labels) continue;
-            if (s.labels_cap < n) return sample_error(MP_EARG, g[q].idx, "labels buffer too small");
-            MP_CUDA(cudaMemcpyAsync(s.labels, parent + R[q], n * 4, cudaMemcpyDeviceToHost, b->copy_st));
-        }
-        MP_CUDA(cudaStreamSynchronize(b->copy_st));
-        MP_CUDA(cudaStreamSynchronize(st));
+        // the copies to the host run on during the next group's kernels; the buffers wait for them
+        MP_CUDA(cudaEventCreateWithFlags(&pending.done, cudaEventDisableTiming));
+        MP_CUDA(cudaEventRecord(pending.done, b->dl_st));
         MP_CUDA(cudaGetLastError());
-    }
-    for (int q = 0; q < nseg; q++) {  // labels in each sample's own read ids
-        const mp_batch_sample &s = smp[g[q].idx];
-        if (!s.labels) continue;
-        const uint64_t n = R[q + 1] - R[q];
-        for (uint64_t x = 0; x < n; x++) s.labels[x] -= (uint32_t)R[q];
     }
     b->groups++;
     return 0;
@@ -510,13 +538,17 @@ int mp_batch_create(mp_ctx *ctx, mp_batch **out)
     b->ctx = ctx;
     b->device = dev;
     if (cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaStreamCreateWithFlags(&b->copy_st, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaStreamCreateWithFlags(&b->copy_st, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&b->dl_st, cudaStreamNonBlocking) != cudaSuccess) {
         if (b->st) cudaStreamDestroy(b->st);
+        if (b->copy_st) cudaStreamDestroy(b->copy_st);
         delete b;
         return set_error(MP_ECUDA, "cannot create a stream");
     }
     b->arena.st = b->st;
+    b->io.st = b->st;
     ctx_budget(ctx, &b->arena.budget_used, &b->arena.budget_limit);
+    ctx_budget(ctx, &b->io.budget_used, &b->io.budget_limit);
     *out = b;
     return 0;
 }
@@ -525,10 +557,14 @@ void mp_batch_destroy(mp_batch *b)
 {
     if (!b) return;
     cudaSetDevice(b->device);
+    cudaStreamSynchronize(b->copy_st);
+    cudaStreamSynchronize(b->dl_st);
     b->arena.release_all();
+    b->io.release_all();
     cudaStreamSynchronize(b->st);
     cudaStreamDestroy(b->st);
     cudaStreamDestroy(b->copy_st);
+    cudaStreamDestroy(b->dl_st);
     delete b;
 }
 
@@ -587,7 +623,7 @@ int mp_batch_run(mp_batch *b, const mp_batch_params *p, int nsamples, const mp_b
         }
         const char *e = getenv("MP_BATCH_GROUP_BYTES");  // a smaller group size (tests)
         if (e && *e) avail = std::min<uint64_t>(avail, strtoull(e, nullptr, 10));
-        avail = avail / 10 * 9;
+        avail = avail / 20 * 17;  // room for the previous group's files, still going down as a group starts
     }
     std::vector<std::vector<Sample>> groups;
     uint64_t acc = 0;
@@ -600,17 +636,30 @@ int mp_batch_run(mp_batch *b, const mp_batch_params *p, int nsamples, const mp_b
         groups.back().push_back(all[q]);
         acc += need;
     }
-    for (auto &g : groups) {
-        int rc = run_group(b, p, samples, g, results);
-        if (rc) {
-            for (const Sample &s : g) {
+    // groups one after another on the device; group g - 1's files go down during group g's kernels
+    PendingIO prev, cur;
+    int rc = 0;
+    for (size_t gi = 0; gi < groups.size() && !rc; gi++) {
+        rc = run_group(b, p, samples, groups[gi], prev, cur, results);
+        retire(b, prev);  // (already done inside, unless the group failed early)
+        prev = cur;
+        cur = PendingIO{};
+        if (rc)
+            for (const Sample &s : groups[gi]) {
                 results[s.idx].status = rc;
                 snprintf(results[s.idx].error, sizeof results[s.idx].error, "%s", mp_last_error());
             }
-            return rc;
-        }
     }
-    return 0;
+    // every copy to the host is done before the call returns; a failure leaves nothing behind
+    const std::string msg = rc ? std::string(mp_last_error()) : std::string();
+    retire(b, prev);
+    cudaStreamSynchronize(b->copy_st);
+    cudaStreamSynchronize(b->dl_st);
+    b->io.release_all();
+    const cudaError_t e = cudaStreamSynchronize(b->st);
+    if (!rc && e != cudaSuccess) rc = set_cuda_error(e, "mp_batch_run", __FILE__, __LINE__);
+    if (rc && !msg.empty()) set_error(rc, "%s", msg.c_str());
+    return rc;
 }
 
 int mp_batch_stage_ms(const mp_batch *b, double *ms, int n)
