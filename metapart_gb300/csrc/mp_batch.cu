@@ -175,8 +175,8 @@ static void retire(mp_batch *b, PendingIO &x)
 }
 
 // One group of samples through every stage.  Its partition files' copies to the host are queued at the end
-// on their own stream and keep running during the next group's kernels (pending); the previous group's
-// buffers (older) go back once this group's upload and count are done.
+// on their own stream and left running (pending); the next group waits for them (as older) once its own
+// upload is queued, so the two directions of the host link overlap.
 static int run_group(mp_batch *b, const mp_batch_params *p, const mp_batch_sample *smp, std::vector<Sample> &g,
                      PendingIO &older, PendingIO &pending, mp_batch_result *res)
 {
@@ -224,6 +224,9 @@ static int run_group(mp_batch *b, const mp_batch_params *p, const mp_batch_sampl
         cudaEventRecord(ev[u], b->copy_st);
     }
     MP_CUDA(cudaMemsetAsync(d_fq + total_bytes, 0, 64, st));
+    // the previous group's files go down while this group's bytes go up (the link carries both ways at
+    // once); the parse waits for them, since its small read-backs would queue behind the big copies
+    retire(b, older);
     // ---- per upload segment, as its bytes arrive: parse, the samples' and their chunks' first records,
     // k-mer cache and per-sample bucket counts
     uint32_t *cc = A.alloc_persistent<uint32_t>((size_t)nseg * NB);
@@ -291,9 +294,6 @@ static int run_group(mp_batch *b, const mp_batch_params *p, const mp_batch_sampl
         launch_count(d_fq + b0, prs[u], k, 0, dl, qb - qa, cc + (size_t)qa * NB, nullptr, err, st, kc[u].off, kc[u].lo,
                      kc[u].hi);
     }
-    // the previous group's files have gone down during this group's upload and count: its buffers go back
-    // before this group's tuples are allocated
-    retire(b, older);
     const uint64_t N = R[nseg];
     if (N >= UMAX32B) return set_error(MP_EUNSUP, "a group of more than 2^32 - 2 reads");
     // ---- one read table for the group, global read ids
@@ -623,7 +623,7 @@ int mp_batch_run(mp_batch *b, const mp_batch_params *p, int nsamples, const mp_b
         }
         const char *e = getenv("MP_BATCH_GROUP_BYTES");  // a smaller group size (tests)
         if (e && *e) avail = std::min<uint64_t>(avail, strtoull(e, nullptr, 10));
-        avail = avail / 20 * 17;  // room for the previous group's files, still going down as a group starts
+        avail = avail / 10 * 9;
     }
     std::vector<std::vector<Sample>> groups;
     uint64_t acc = 0;
@@ -636,7 +636,7 @@ int mp_batch_run(mp_batch *b, const mp_batch_params *p, int nsamples, const mp_b
         groups.back().push_back(all[q]);
         acc += need;
     }
-    // groups one after another on the device; group g - 1's files go down during group g's kernels
+    // groups one after another on the device; group g - 1's files go down while group g's bytes go up
     PendingIO prev, cur;
     int rc = 0;
     for (size_t gi = 0; gi < groups.size() && !rc; gi++) {

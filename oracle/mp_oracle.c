@@ -364,6 +364,14 @@ static inline int tpush(tvec *v, uint64_t kmer, uint32_t id, uint8_t adj)
 static int enum_plain(const unsigned char *s, int L, int k, uint64_t lo, uint64_t hi, uint32_t id, tvec *out)
 {
     if (L <= k) return 0;
+    if (out->cap - out->n < (uint64_t)(L - k + 1)) {  /* room for every position, so tpush never grows */
+        uint64_t nc = out->cap ? out->cap : 4096;
+        while (nc - out->n < (uint64_t)(L - k + 1)) nc *= 2;
+        tup *nt = (tup *)realloc(out->t, nc * sizeof(tup));
+        if (!nt) return -1;
+        out->t = nt;
+        out->cap = nc;
+    }
     int last = L - k, lastN = -1, sh = 2 * (k - 10);
     uint64_t mask = (1ull << (2 * k)) - 1, fwd = 0, rc = 0;
     unsigned char prev = 'N', next = s[k];
@@ -384,13 +392,17 @@ static int enum_plain(const unsigned char *s, int L, int k, uint64_t lo, uint64_
         } else if (lastN != -1) {
             continue;
         }
-        if (fwd < rc) {
-            uint64_t b = fwd >> sh;
-            if (b >= lo && b < hi && tpush(out, fwd, id, adj_fwd(prev, next))) return -1;
-        } else {
-            uint64_t b = rc >> sh;
-            if (b >= lo && b < hi && tpush(out, rc, id, adj_rc(cmpl(prev), cmpl(next)))) return -1;
-        }
+        /* written in place and kept when in range, without branches on the (unpredictable) orientation and
+           range tests: the room is reserved above */
+        const int f = fwd < rc;
+        const uint64_t canon = f ? fwd : rc, b = canon >> sh;
+        const uint8_t a_f = adj_fwd(prev, next), a_r = adj_rc(cmpl(prev), cmpl(next));
+        tup *x = &out->t[out->n];
+        x->kmer = canon;
+        x->id = id;
+        x->adj = f ? a_f : a_r;
+        x->pad[0] = x->pad[1] = x->pad[2] = 0;
+        out->n += (b >= lo) & (b < hi);
     }
     return 0;
 }
@@ -681,30 +693,33 @@ static int plan_ranges(const uint64_t *hist, int scans, int T, uint64_t *scanR, 
 }
 
 /* range partition bin of a bucket (metapart.c:2019-2022) */
-static int bin_of(uint64_t b, const uint64_t *ltr, int T)
-{
-    int cb = 0;
-    while (cb <= T && b >= ltr[cb]) cb++;
-    return cb - 1;
-}
-
-/* radixPass (metapart.c:1494-1598) over passOrder 5..13 (:2169-2195): adj byte, then k-mer bytes 0..7 */
+/* radixPass (metapart.c:1494-1598) over passOrder 5..13 (:2169-2195): adj byte, then k-mer bytes 0..7.
+   A digit that is the same in every tuple of the bin moves nothing in a stable pass, so it is skipped;
+   the passes alternate between the two buffers and the result is copied back once. */
 static void sort_bin(tup *a, tup *tmp, uint64_t n)
 {
-    uint64_t cnt[257];
-    for (int pass = 0; pass < 9; pass++) {
-        memset(cnt, 0, sizeof cnt);
-        for (uint64_t i = 0; i < n; i++) {
-            unsigned d = pass == 0 ? a[i].adj : (unsigned)((a[i].kmer >> (8 * (pass - 1))) & 0xFF);
-            cnt[d + 1]++;
-        }
-        for (int d = 1; d <= 256; d++) cnt[d] += cnt[d - 1];
-        for (uint64_t i = 0; i < n; i++) {
-            unsigned d = pass == 0 ? a[i].adj : (unsigned)((a[i].kmer >> (8 * (pass - 1))) & 0xFF);
-            tmp[cnt[d]++] = a[i];
-        }
-        memcpy(a, tmp, n * sizeof(tup));
+    uint64_t cnt[9][257];
+    memset(cnt, 0, sizeof cnt);
+    for (uint64_t i = 0; i < n; i++) {
+        cnt[0][a[i].adj + 1]++;
+        const uint64_t km = a[i].kmer;
+        for (int b = 0; b < 8; b++) cnt[b + 1][((km >> (8 * b)) & 0xFF) + 1]++;
     }
+    tup *src = a, *dst = tmp;
+    for (int pass = 0; pass < 9; pass++) {
+        int constant = 0;
+        for (int d = 1; d <= 256; d++)
+            if (cnt[pass][d] == n) constant = 1;
+        if (constant) continue;
+        uint64_t *c = cnt[pass];
+        for (int d = 1; d <= 256; d++) c[d] += c[d - 1];
+        for (uint64_t i = 0; i < n; i++) {
+            unsigned d = pass == 0 ? src[i].adj : (unsigned)((src[i].kmer >> (8 * (pass - 1))) & 0xFF);
+            dst[c[d]++] = src[i];
+        }
+        tup *x = src; src = dst; dst = x;
+    }
+    if (src != a) memcpy(a, src, n * sizeof(tup));
 }
 
 /* markMischiefKmers body for one thread range (metapart.c:2276-2468) */
@@ -807,13 +822,32 @@ int mpo_metapart(const char *out_prefix, uint64_t fastq_buffer_size, int k, int 
     tvec *per = (tvec *)calloc((size_t)T, sizeof(tvec));
     chunk_view *cvs = (chunk_view *)calloc(nchunks, sizeof(chunk_view));
     tup *arr = NULL, *tmp = NULL;
+    uint64_t arr_cap = 0;
     g_parent = NULL; g_sizes = NULL; g_filtered = NULL;
     if ((rc = plan_ranges(hist, S, T, scanR, thrR))) goto out;
     if ((rc = load_files(nfiles, files, f))) goto out;
-    for (uint64_t c = 0; c < nchunks; c++) {
-        if ((rc = chunk_bytes(f, &hd[c], &hd[c + 1], &cvs[c]))) goto out;
-        if (cvs[c].n >= fastq_buffer_size) { rc = fail(MPO_EARG, "fastqBufferSize is smaller than a chunk"); goto out; }
-        if ((rc = parse_chunk(&cvs[c]))) goto out;
+    {   /* the chunks in parallel; the first failing chunk (in chunk order) is redone alone for its message */
+        int *crc = (int *)calloc(nchunks, sizeof(int));
+        if (!crc) { rc = fail(MPO_ENOMEM, "out of memory"); goto out; }
+#pragma omp parallel for schedule(dynamic, 1)
+        for (uint64_t c = 0; c < nchunks; c++) {
+            chunk_view cv = {0};
+            int r = chunk_bytes(f, &hd[c], &hd[c + 1], &cv);
+            if (!r && cv.n >= fastq_buffer_size) r = MPO_EARG;
+            if (!r) r = parse_chunk(&cv);
+            crc[c] = r;
+            cvs[c] = cv;
+        }
+        for (uint64_t c = 0; c < nchunks && !rc; c++) {
+            if (!crc[c]) continue;
+            chunk_free(&cvs[c]);
+            if ((rc = chunk_bytes(f, &hd[c], &hd[c + 1], &cvs[c]))) break;
+            if (cvs[c].n >= fastq_buffer_size) { rc = fail(MPO_EARG, "fastqBufferSize is smaller than a chunk"); break; }
+            rc = parse_chunk(&cvs[c]);
+            if (!rc) rc = fail(crc[c], "chunk %llu failed", (unsigned long long)c);
+        }
+        free(crc);
+        if (rc) goto out;
     }
     {
         uint64_t nread_seen = 0;
@@ -849,13 +883,19 @@ int mpo_metapart(const char *out_prefix, uint64_t fastq_buffer_size, int k, int 
         if (err) { rc = fail(MPO_ENOMEM, "out of memory enumerating"); goto out; }
         uint64_t n = 0;
         for (int t = 0; t < T; t++) n += per[t].n;
-        free(arr); free(tmp);
-        arr = (tup *)malloc((n + 1) * sizeof(tup));
-        tmp = (tup *)malloc((n + 1) * sizeof(tup));
-        if (!arr || !tmp) { rc = fail(MPO_ENOMEM, "out of memory"); goto out; }
+        if (n + 1 > arr_cap) {  /* the scan arrays, kept from scan to scan */
+            free(arr); free(tmp);
+            arr_cap = n + 1;
+            arr = (tup *)malloc(arr_cap * sizeof(tup));
+            tmp = (tup *)malloc(arr_cap * sizeof(tup));
+            if (!arr || !tmp) { rc = fail(MPO_ENOMEM, "out of memory"); goto out; }
+        }
         {
-            uint64_t p = 0;
-            for (int t = 0; t < T; t++) { memcpy(arr + p, per[t].t, per[t].n * sizeof(tup)); p += per[t].n; }
+            uint64_t at[257];
+            at[0] = 0;
+            for (int t = 0; t < T; t++) at[t + 1] = at[t] + per[t].n;
+#pragma omp parallel for schedule(dynamic, 1)
+            for (int t = 0; t < T; t++) memcpy(arr + at[t], per[t].t, per[t].n * sizeof(tup));
         }
         char name[64];
         snprintf(name, sizeof name, "scan%d_enum.bin", s);
@@ -870,27 +910,59 @@ int mpo_metapart(const char *out_prefix, uint64_t fastq_buffer_size, int k, int 
         /* sortKmerList: stable range partition into thread bins, then LSD per bin */
         const uint64_t *ltr = thrR + (size_t)s * T;
         uint64_t bcount[257] = {0}, refcount[257] = {0};
+        /* the range partition's bin of a tuple (metapart.c:2019-2022): walking the range starts from the
+           first, the bin before the first start above the bucket; that start is the first running maximum
+           of the starts above the bucket, so a binary search over the running maxima finds it */
+        uint64_t M[258];
+        M[0] = ltr[0];
+        for (int t = 1; t <= T; t++) M[t] = M[t - 1] > ltr[t] ? M[t - 1] : ltr[t];
+        uint16_t *bin = (uint16_t *)malloc((n + 1) * sizeof(uint16_t));
+        if (!bin) { rc = fail(MPO_ENOMEM, "out of memory"); goto out; }
+        int bad_bin = 0;
+#pragma omp parallel for schedule(static)
         for (uint64_t i = 0; i < n; i++) {
-            int b = bin_of(arr[i].kmer >> sh, ltr, T);
-            if (b < 0 || b >= T) { rc = fail(MPO_EUNSUP, "thread k-mer ranges do not cover a bucket"); goto out; }
-            bcount[b + 1]++;
+            const uint64_t b = arr[i].kmer >> sh;
+            int l = 0, h = T + 1;  /* first t in [0, T] with M[t] > b (T + 1: none) */
+            while (l < h) { int m = (l + h) >> 1; if (M[m] > b) h = m; else l = m + 1; }
+            const int cb = l - 1;
+            if (cb < 0 || cb >= T) bad_bin = 1;
+            bin[i] = (uint16_t)(cb < 0 ? 0 : cb);
         }
+        if (bad_bin) { free(bin); rc = fail(MPO_EUNSUP, "thread k-mer ranges do not cover a bucket"); goto out; }
+        for (uint64_t i = 0; i < n; i++) bcount[bin[i] + 1]++;
         /* the reference sizes bins from bucket counts over [ltr[t], ltr[t+1]) (:1810-1850) */
         for (int t = 0; t < T; t++) {
             uint64_t a = ltr[t], b = ltr[t + 1];
             refcount[t + 1] = (b > a) ? hist[b] - hist[a] : 0;
             if (refcount[t + 1] != bcount[t + 1]) {
+                free(bin);
                 rc = fail(MPO_EUNSUP, "thread k-mer ranges are not monotone over populated buckets");
                 goto out;
             }
         }
         for (int t = 0; t < T; t++) bcount[t + 1] += bcount[t];
-        {
-            uint64_t pos[257];
-            memcpy(pos, bcount, sizeof pos);
-            for (uint64_t i = 0; i < n; i++) tmp[pos[bin_of(arr[i].kmer >> sh, ltr, T)]++] = arr[i];
+        {  /* stable scatter into the bins: the input in NP parts, each part's tuples of a bin after the earlier
+              parts' (counts per part and bin, then every part scatters on its own) */
+            enum { NP = 64 };
+            static uint64_t pc[NP][257];
+            memset(pc, 0, sizeof pc);
+#pragma omp parallel for schedule(static)
+            for (int q = 0; q < NP; q++)
+                for (uint64_t i = n * q / NP; i < n * (q + 1) / NP; i++) pc[q][bin[i]]++;
+            for (int t = 0; t < T; t++) {
+                uint64_t at = bcount[t];
+                for (int q = 0; q < NP; q++) {
+                    const uint64_t c = pc[q][t];
+                    pc[q][t] = at;
+                    at += c;
+                }
+            }
+#pragma omp parallel for schedule(static)
+            for (int q = 0; q < NP; q++)
+                for (uint64_t i = n * q / NP; i < n * (q + 1) / NP; i++) tmp[pc[q][bin[i]]++] = arr[i];
             memcpy(arr, tmp, n * sizeof(tup));
         }
+        free(bin);
 #pragma omp parallel for schedule(dynamic, 1)
         for (int t = 0; t < T; t++) sort_bin(arr + bcount[t], tmp + bcount[t], bcount[t + 1] - bcount[t]);
         snprintf(name, sizeof name, "scan%d_sorted.bin", s);
@@ -961,6 +1033,8 @@ int mpo_metapart(const char *out_prefix, uint64_t fastq_buffer_size, int k, int 
                 goto out;
             }
         }
+        /* every thread writes only its own files (FromTid<t>_*), as the reference's threads do */
+#pragma omp parallel for schedule(dynamic, 1)
         for (int t = 0; t < T; t++) {
             for (uint64_t c = (uint64_t)t * per_thread; c < (uint64_t)(t + 1) * per_thread; c++) {
                 uint64_t rid = (uint64_t)hd[c].extra * UMAX32 + hd[c].read_id;
