@@ -68,6 +68,8 @@ def parse_args():
     ap.add_argument("--serve-seconds", type=float, default=15.0,
                     help="plain mode: seconds of Poisson arrivals for the line's p50/p99 (0: none)")
     ap.add_argument("--no-batch", action="store_true", help="plain mode: leave out the batched-vs-plain run")
+    ap.add_argument("--store", default="kmer_cache", choices=["kmer_cache", "packed", "fastq"],
+                    help="plain mode: what the count pass keeps of the reads for the partition")
     return ap.parse_args()
 
 
@@ -210,6 +212,7 @@ def main():
     del fq
     ctx = native.Context(dev)
     job = native.Job(ctx)
+    job.set_read_store(args.store)
     stream = torch.cuda.ExternalStream(job.stream, device=dev)
     min3 = args.workload == "min3"
 
@@ -302,6 +305,27 @@ def main():
     e2e_pieces = job.scan_pieces
     e2e_ms = dist.max(e0.elapsed_time(e1) / args.steps)
     e2e_value = dist.world * bases / (e2e_ms / 1e3)
+    # the other stores of the reads (what the count pass keeps for the enumeration), device-resident, a few
+    # steps each: their times and device bytes
+    stores = {}
+    reads_pos = args.reads * max(0, spec.lengths[0] - args.k + 1)
+    rounds = args.reads * ((spec.lengths[0] + 31) // 32)
+    store_bytes = {"kmer_cache": 9 * reads_pos + 8 * args.reads, "packed": 12 * rounds + 8 * args.reads, "fastq": 0}
+    for other in [x for x in ("kmer_cache", "packed", "fastq") if x != args.store] if not min3 else []:
+        job.set_read_store(other)
+        device_step()
+        e_a = torch.cuda.Event(enable_timing=True)
+        e_b = torch.cuda.Event(enable_timing=True)
+        e_a.record(stream)
+        for _ in range(3):
+            device_step()
+        e_b.record(stream)
+        e_b.synchronize()
+        stores[other] = {"ms_per_step": round(e_a.elapsed_time(e_b) / 3, 3),
+                         "enumerate_ms": round(job.stage_ms()["enumerate"], 3), "device_bytes": store_bytes[other]}
+        job.set_read_store(args.store)
+    stores[args.store] = {"ms_per_step": round(ms, 3), "enumerate_ms": round(stage.get("enumerate", 0) / args.steps, 3),
+                          "device_bytes": store_bytes[args.store]}
     link = link_bandwidth(host_in, dev_in[:nbytes], out_host)
 
     peak, peak_kind = measured_peak()
@@ -340,6 +364,7 @@ def main():
                      "bytes_per_launch": int(per_launch_bytes),
                      "launch_ms": round(sort_ms / max(sort_passes, 1), 4),
                      "traffic": (round(traffic) if traffic else None)},
+        "read_stores": stores,
         "gpu_launches": int(launches),
         "stage_ms": {kk: round(v / args.steps, 3) for kk, v in stage.items()},
         "sort_split": {kk: ({k2: int(v2 / args.steps) for k2, v2 in v.items()} if isinstance(v, dict) else

@@ -224,6 +224,9 @@ typedef struct {
     int k, min3, num_scans, num_threads;  /* as mp_part_params */
     int num_chunks;                       /* genFastqIdx chunks; a multiple of num_threads */
     int interleaved;                      /* 1: interleaved pairs, 0: single end */
+    int read_store;                       /* MP_STORE_*: what the request's count pass keeps for its partition
+                                             (MP_STORE_PACKED admits the most requests at once: 0.375 bytes per
+                                             base against the k-mer cache's 9 per position) */
 } mp_request_params;
 
 typedef struct {
@@ -243,7 +246,8 @@ typedef struct {
 } mp_server_stats_t;
 
 /* Estimated device bytes of one request (FASTQ, read table, forest, the largest scan's tuple
- * buffers, output), from the request size and its first records. */
+ * buffers, output, the store of the reads its count pass keeps), from the request size and its first
+ * records. */
 uint64_t mp_request_footprint(const char *fastq, uint64_t nbytes, const mp_request_params *p);
 
 /* slots: worker threads (jobs in flight at most); hbm_budget: bytes the admitted footprints may add
@@ -272,6 +276,23 @@ void mp_server_destroy(mp_server *s);
  * count-only job (the drop-in genHistograms).  No counterpart in the reference, whose stages are
  * separate processes. */
 int mp_job_set_kmer_cache(mp_job *job, int enable);
+
+/* What the count pass of the plain variant keeps of the reads for the next mp_job_partition of the same k
+ * (mp_job_count, mp_job_load_count):
+ *   MP_STORE_KMER_CACHE (default): every position's canonical k-mer and adjacency byte, 9 bytes per
+ *     position (21.6 GB for 20M reads of 150 bp); the partition's enumeration only filters it;
+ *   MP_STORE_PACKED: the reads 2 bits per base with an N mask, 0.375 bytes per base (1.1 GB for the same
+ *     reads); the enumeration recomputes the k-mers from them, so it takes longer;
+ *   MP_STORE_FASTQ: nothing; the enumeration recomputes the k-mers from the FASTQ bytes.
+ * An input with any sequence byte other than A, C, G, T, N keeps no packed copy (the FASTQ path runs); a
+ * store that does not fit the budget or the device is skipped.  mp_job_set_kmer_cache(job, 1 / 0) is
+ * MP_STORE_KMER_CACHE / MP_STORE_FASTQ.  mp_job_read_store tells which store the job holds now.  No
+ * counterpart in the reference, whose stages are separate processes that re-read the FASTQ files. */
+#define MP_STORE_FASTQ 0
+#define MP_STORE_KMER_CACHE 1
+#define MP_STORE_PACKED 2
+int mp_job_set_read_store(mp_job *job, int store);
+int mp_job_read_store(const mp_job *job);
 
 /* Most tuples one scan of mp_job_partition holds in HBM at once (0, the default: what the context's
  * budget, or the device, has left at about 32 bytes per tuple; the environment variable

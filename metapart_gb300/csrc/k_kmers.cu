@@ -35,6 +35,20 @@ __device__ __forceinline__ void load_round(const uint8_t *s, uint32_t L, int t, 
     r.c = c;
 }
 
+// The same round from the 2-bit packed reads: one 64-bit code word and one 32-bit N mask per 32 bases,
+// as load_round builds them (positions past the read are code 0 and not N); the lane's character is
+// restored from its code (ACGT) or the mask (N), which is exact for reads of those five letters only
+// (the count pass stores no packed copy of an input with any other byte).
+__device__ __forceinline__ void load_round_packed(const uint64_t *w, const uint32_t *nm, uint32_t nrounds, int t, int lane,
+                                                  Round &r)
+{
+    const bool in = (uint32_t)t < nrounds;
+    r.W = in ? w[t] : 0ull;
+    r.N = in ? nm[t] : 0u;
+    const uint32_t code = (uint32_t)(r.W >> (62 - 2 * lane)) & 3u;
+    r.c = ((r.N >> lane) & 1u) ? 0x4Eu : ((0x54474341u >> (8 * code)) & 0xFFu);  // N, or A C G T
+}
+
 // Forward code, validity (no N in the window) of the k-mer at lane's position of round t.
 __device__ __forceinline__ bool kmer_at(int lane, int k, const Round &c, const Round &n, uint64_t &fwd)
 {
@@ -62,10 +76,14 @@ __device__ __forceinline__ uint32_t chunk_of(const uint64_t *chunk_rec, int nchu
 constexpr uint8_t KC_NONE = 0xFF;
 constexpr int KC_PER_LANE = 10;  // cached positions per lane of a read: L - k + 1 <= 300
 
+// PK: the read's rounds also go to the packed copy at pk_off[r] (ceil(L / 32) rounds of a code word and an
+// N mask); a byte other than A, C, G, T, N sets DERR_NONACGT (no packed copy is usable).
+template <bool PK>
 __global__ void __launch_bounds__(256) k_count_plain(const uint8_t *fq, const uint64_t *seq_off, const uint32_t *seq_len,
                                                      uint64_t r0, uint64_t r1, int k, const uint64_t *chunk_rec,
                                                      int nchunks, uint32_t *cc, unsigned long long *glob, uint32_t *err,
-                                                     const uint64_t *kc_off, uint64_t *kc_lo, uint8_t *kc_hi)
+                                                     const uint64_t *kc_off, uint64_t *kc_lo, uint8_t *kc_hi,
+                                                     const uint64_t *pk_off, uint64_t *pk_w, uint32_t *pk_n)
 {
     const int lane = threadIdx.x & 31;
     const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
@@ -85,7 +103,10 @@ __global__ void __launch_bounds__(256) k_count_plain(const uint8_t *fq, const ui
         load_round(s, L, 0, lane, cur);
         load_round(s, L, 1, lane, nxt);
         prv = cur;
-        for (int t = 0; 32 * t <= last; t++) {
+        const uint64_t pbase = PK ? pk_off[r] : 0;
+        const uint32_t nrounds = (L + 31) / 32;
+        int t = 0;
+        for (; 32 * t <= last; t++) {
             const int i = 32 * t + lane;
             uint64_t fwd;
             bool v = kmer_at(lane, k, cur, nxt, fwd) && i <= last;
@@ -93,6 +114,15 @@ __global__ void __launch_bounds__(256) k_count_plain(const uint8_t *fq, const ui
             const bool f = fwd < rc;
             const uint64_t canon = f ? fwd : rc;
             const uint32_t b = (uint32_t)(canon >> sh);
+            if constexpr (PK) {  // the packed copy of round t
+                const uint32_t c = cur.c;
+                const bool odd = (uint32_t)(32 * t + lane) < L && c != 'A' && c != 'C' && c != 'G' && c != 'T' && c != 'N';
+                if (__any_sync(FULL, odd) && lane == 0) atomicOr(err, DERR_NONACGT);
+                if (lane == 0 && (uint32_t)t < nrounds) {
+                    pk_w[pbase + t] = cur.W;
+                    pk_n[pbase + t] = cur.N;
+                }
+            }
             if (kc_lo) {
                 const uint32_t x = __shfl_sync(FULL, cur.c, (lane + 31) & 31), y = __shfl_sync(FULL, prv.c, 31);
                 const int q = lane + k;
@@ -115,7 +145,27 @@ __global__ void __launch_bounds__(256) k_count_plain(const uint8_t *fq, const ui
             cur = nxt;
             load_round(s, L, t + 2, lane, nxt);
         }
+        if constexpr (PK) {  // the rounds after the last k-mer's (at most one: L < 32 t + 32 once 32 t > L - k, k < 32)
+            for (; (uint32_t)t < nrounds; t++) {
+                const uint32_t c = cur.c;
+                const bool odd = (uint32_t)(32 * t + lane) < L && c != 'A' && c != 'C' && c != 'G' && c != 'T' && c != 'N';
+                if (__any_sync(FULL, odd) && lane == 0) atomicOr(err, DERR_NONACGT);
+                if (lane == 0) {
+                    pk_w[pbase + t] = cur.W;
+                    pk_n[pbase + t] = cur.N;
+                }
+                cur = nxt;
+                load_round(s, L, t + 2, lane, nxt);
+            }
+        }
     }
+}
+
+// Rounds of 32 bases per read for the packed copy (ceil(L / 32) when the read has a k-mer, else 0).
+__global__ void k_pk_rounds(const uint32_t *seq_len, uint64_t n, int k, uint32_t *nr)
+{
+    const uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r < n) nr[r] = seq_len[r] > (uint32_t)k ? (seq_len[r] + 31) / 32 : 0u;
 }
 
 // Positions per read (L - k + 1, or 0), for the k-mer cache offsets.
@@ -214,16 +264,28 @@ __global__ void k_sum_chunks(const uint32_t *cc, int nchunks, unsigned long long
 
 // ------------------------------------------------------------ K2 plain
 
-template <bool WRITE>
+// The 2-bit packed copy of a piece of the reads (reads r0 .. r0 + n - 1): round offsets off (n + 1, from 0),
+// code words w and N masks nm.
+struct PackedPiece {
+    const uint64_t *off = nullptr, *w = nullptr;
+    const uint32_t *nm = nullptr;
+    uint64_t r0 = 0;
+};
+
+// PK: the bases come from a packed piece (read r of the loop is read pk.r0 + r; seq_len, label, out_off and
+// cnt are indexed by that global id), else from the FASTQ bytes.
+template <bool WRITE, bool PK = false>
 __global__ void __launch_bounds__(256) k_enum_plain(const uint8_t *fq, const uint64_t *seq_off, const uint32_t *seq_len,
                                                     uint64_t n_reads, int k, uint32_t lo, uint32_t hi,
                                                     const uint32_t *label, const uint64_t *out_off, uint32_t *cnt,
-                                                    uint64_t *o_lo, uint8_t *o_hi, uint32_t *o_id, uint32_t *err)
+                                                    uint64_t *o_lo, uint8_t *o_hi, uint32_t *o_id, uint32_t *err,
+                                                    PackedPiece pk = PackedPiece{})
 {
     const int lane = threadIdx.x & 31;
     const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
     const int sh = 2 * (k - 10);
-    for (uint64_t r = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < n_reads; r += nw) {
+    for (uint64_t lr = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; lr < n_reads; lr += nw) {
+        const uint64_t r = PK ? pk.r0 + lr : lr;
         const uint32_t L = seq_len[r];
         if (L <= (uint32_t)k) {
             if (!WRITE && lane == 0) cnt[r] = 0;
@@ -233,7 +295,14 @@ __global__ void __launch_bounds__(256) k_enum_plain(const uint8_t *fq, const uin
             if (lane == 0) { atomicOr(err, DERR_LONG_READ); if (!WRITE) cnt[r] = 0; }
             continue;
         }
-        const uint8_t *s = fq + seq_off[r];
+        const uint8_t *s = PK ? nullptr : fq + seq_off[r];
+        const uint64_t *pw = PK ? pk.w + pk.off[lr] : nullptr;
+        const uint32_t *pn = PK ? pk.nm + pk.off[lr] : nullptr;
+        const uint32_t nrounds = PK ? (uint32_t)(pk.off[lr + 1] - pk.off[lr]) : 0u;
+        auto load = [&](int t, Round &x) {
+            if constexpr (PK) load_round_packed(pw, pn, nrounds, t, lane, x);
+            else load_round(s, L, t, lane, x);
+        };
         const int last = (int)L - k;
         uint64_t base = WRITE ? out_off[r] : 0;
         uint32_t id = (uint32_t)r;
@@ -242,8 +311,8 @@ __global__ void __launch_bounds__(256) k_enum_plain(const uint8_t *fq, const uin
             id = (p == BAD) ? (uint32_t)r : p;  // findRoot after full compression (metapart.c:543-568)
         }
         Round prv, cur, nxt;
-        load_round(s, L, 0, lane, cur);
-        load_round(s, L, 1, lane, nxt);
+        load(0, cur);
+        load(1, nxt);
         prv = cur;
         uint32_t total = 0;
         for (int t = 0; 32 * t <= last; t++) {
@@ -277,7 +346,7 @@ __global__ void __launch_bounds__(256) k_enum_plain(const uint8_t *fq, const uin
             total += __popc(bal);
             prv = cur;
             cur = nxt;
-            load_round(s, L, t + 2, lane, nxt);
+            load(t + 2, nxt);
         }
         if (!WRITE && lane == 0) {
             cnt[r] = total;
@@ -290,10 +359,11 @@ __global__ void __launch_bounds__(256) k_enum_plain(const uint8_t *fq, const uin
 // cnt[s * stride + r]; S <= MAX_SCAN_COUNT.
 constexpr int MAX_SCAN_COUNT = 8;
 
+template <bool PK = false>
 __global__ void __launch_bounds__(256) k_enum_count_scans(const uint8_t *fq, const uint64_t *seq_off,
                                                           const uint32_t *seq_len, uint64_t n_reads, int k,
                                                           const uint32_t *bounds, int S, uint32_t *cnt, uint64_t stride,
-                                                          uint32_t *err)
+                                                          uint32_t *err, PackedPiece pk = PackedPiece{})
 {
     __shared__ uint32_t sb[MAX_SCAN_COUNT + 1];
     if (threadIdx.x <= (unsigned)S) sb[threadIdx.x] = bounds[threadIdx.x];
@@ -302,7 +372,8 @@ __global__ void __launch_bounds__(256) k_enum_count_scans(const uint8_t *fq, con
     const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
     const int sh = 2 * (k - 10);
     const uint32_t b_lo = sb[0], b_hi = sb[S];
-    for (uint64_t r = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < n_reads; r += nw) {
+    for (uint64_t lr = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; lr < n_reads; lr += nw) {
+        const uint64_t r = PK ? pk.r0 + lr : lr;
         const uint32_t L = seq_len[r];
         uint32_t c[MAX_SCAN_COUNT];
 #pragma unroll
@@ -310,11 +381,18 @@ __global__ void __launch_bounds__(256) k_enum_count_scans(const uint8_t *fq, con
         if (L > (uint32_t)k && (L > 32u * MAX_ROUNDS_ENUM || L - (uint32_t)k >= 300u)) {
             if (lane == 0) atomicOr(err, DERR_LONG_READ);
         } else if (L > (uint32_t)k) {
-            const uint8_t *s = fq + seq_off[r];
+            const uint8_t *s = PK ? nullptr : fq + seq_off[r];
+            const uint64_t *pw = PK ? pk.w + pk.off[lr] : nullptr;
+            const uint32_t *pn = PK ? pk.nm + pk.off[lr] : nullptr;
+            const uint32_t nrounds = PK ? (uint32_t)(pk.off[lr + 1] - pk.off[lr]) : 0u;
+            auto load = [&](int t, Round &x) {
+                if constexpr (PK) load_round_packed(pw, pn, nrounds, t, lane, x);
+                else load_round(s, L, t, lane, x);
+            };
             const int last = (int)L - k;
             Round cur, nxt;
-            load_round(s, L, 0, lane, cur);
-            load_round(s, L, 1, lane, nxt);
+            load(0, cur);
+            load(1, nxt);
             for (int t = 0; 32 * t <= last; t++) {
                 const int i = 32 * t + lane;
                 uint64_t fwd;
@@ -329,7 +407,7 @@ __global__ void __launch_bounds__(256) k_enum_count_scans(const uint8_t *fq, con
                     for (int q = 0; q < MAX_SCAN_COUNT; q++) c[q] += (sc == q) ? 1u : 0u;
                 }
                 cur = nxt;
-                load_round(s, L, t + 2, lane, nxt);
+                load(t + 2, nxt);
             }
         }
         for (int q = 0; q < S; q++) {
@@ -518,14 +596,15 @@ static unsigned grid_for(uint64_t work, int per_block, int waves = 16)
 
 void launch_count(const uint8_t *fq, const ParsedReads &pr, int k, int min3, const uint64_t *chunk_rec, int nchunks,
                   uint32_t *cc, unsigned long long *glob, uint32_t *err, cudaStream_t st, const uint64_t *kc_off,
-                  uint64_t *kc_lo, uint8_t *kc_hi)
+                  uint64_t *kc_lo, uint8_t *kc_hi, const uint64_t *pk_off, uint64_t *pk_w, uint32_t *pk_n)
 {
     if (min3)
         (mp::count_launch(), k_count_min3<<<grid_for(pr.n_reads, 128, 32), 128, 0, st>>>(fq, pr.seq_off, pr.seq_len, 0, pr.n_reads, k,
                                                                           chunk_rec, nchunks, cc, glob, err));
     else
-        (mp::count_launch(), k_count_plain<<<grid_for(pr.n_reads, 8), 256, 0, st>>>(fq, pr.seq_off, pr.seq_len, 0, pr.n_reads, k, chunk_rec,
-                                                               nchunks, cc, glob, err, kc_off, kc_lo, kc_hi));
+        (mp::count_launch(), (pk_w ? k_count_plain<true> : k_count_plain<false>)<<<grid_for(pr.n_reads, 8), 256, 0, st>>>(
+            fq, pr.seq_off, pr.seq_len, 0, pr.n_reads, k, chunk_rec, nchunks, cc, glob, err, kc_off, kc_lo, kc_hi, pk_off,
+            pk_w, pk_n));
     if (cc && glob) (mp::count_launch(), k_sum_chunks<<<NB / 256, 256, 0, st>>>(cc, nchunks, glob));
 }
 
@@ -547,6 +626,51 @@ int launch_enum_count_scans(const uint8_t *fq, const ParsedReads &pr, int k, con
     (mp::count_launch(), k_enum_count_scans<<<grid_for(pr.n_reads, 8), 256, 0, st>>>(
         fq, pr.seq_off, pr.seq_len, pr.n_reads, k, bounds, S, cnt, stride, err));
     return 0;
+}
+
+void launch_pk_rounds(const ParsedReads &pr, int k, uint32_t *nr, cudaStream_t st)
+{
+    (mp::count_launch(), k_pk_rounds<<<(unsigned)((pr.n_reads + 255) / 256), 256, 0, st>>>(pr.seq_len, pr.n_reads, k, nr));
+}
+
+static PackedPiece packed_piece(const uint64_t *off, const uint64_t *w, const uint32_t *nm, uint64_t r0)
+{
+    PackedPiece p;
+    p.off = off;
+    p.w = w;
+    p.nm = nm;
+    p.r0 = r0;
+    return p;
+}
+
+int launch_pk_count_scans(const uint64_t *pk_off, const uint64_t *pk_w, const uint32_t *pk_n, uint64_t r0, uint64_t n_reads,
+                          const uint32_t *seq_len, int k, const uint32_t *bounds, int S, uint32_t *cnt, uint64_t stride,
+                          uint32_t *err, cudaStream_t st)
+{
+    if (S < 1 || S > MAX_SCAN_COUNT) return -1;
+    if (n_reads == 0) return 0;
+    (mp::count_launch(), k_enum_count_scans<true><<<grid_for(n_reads, 8), 256, 0, st>>>(
+        nullptr, nullptr, seq_len, n_reads, k, bounds, S, cnt, stride, err, packed_piece(pk_off, pk_w, pk_n, r0)));
+    return 0;
+}
+
+void launch_pk_count(const uint64_t *pk_off, const uint64_t *pk_w, const uint32_t *pk_n, uint64_t r0, uint64_t n_reads,
+                     const uint32_t *seq_len, int k, uint32_t lo, uint32_t hi, uint32_t *cnt, uint32_t *err, cudaStream_t st)
+{
+    if (n_reads == 0) return;
+    (mp::count_launch(), k_enum_plain<false, true><<<grid_for(n_reads, 8), 256, 0, st>>>(
+        nullptr, nullptr, seq_len, n_reads, k, lo, hi, nullptr, nullptr, cnt, nullptr, nullptr, nullptr, err,
+        packed_piece(pk_off, pk_w, pk_n, r0)));
+}
+
+void launch_pk_write(const uint64_t *pk_off, const uint64_t *pk_w, const uint32_t *pk_n, uint64_t r0, uint64_t n_reads,
+                     const uint32_t *seq_len, int k, uint32_t lo, uint32_t hi, const uint32_t *label, const uint64_t *off,
+                     uint64_t *o_lo, uint8_t *o_hi, uint32_t *o_id, uint32_t *err, cudaStream_t st)
+{
+    if (n_reads == 0) return;
+    (mp::count_launch(), k_enum_plain<true, true><<<grid_for(n_reads, 8), 256, 0, st>>>(
+        nullptr, nullptr, seq_len, n_reads, k, lo, hi, label, off, nullptr, o_lo, o_hi, o_id, err,
+        packed_piece(pk_off, pk_w, pk_n, r0)));
 }
 
 void launch_kc_positions(const ParsedReads &pr, int k, uint32_t *npos, cudaStream_t st)

@@ -72,7 +72,65 @@ void free_kc_piece(DeviceArena &arena, KcPiece &q)
     arena.free_persistent(q.off);
     arena.free_persistent(q.lo);
     arena.free_persistent(q.hi);
+    arena.free_persistent(q.poff);
+    arena.free_persistent(q.pw);
+    arena.free_persistent(q.pn);
     q = KcPiece{};
+}
+
+bool make_pk_piece(DeviceArena &arena, cudaStream_t st, const ParsedReads &pr, uint64_t r0, int k, KcPiece *out)
+{
+    const uint64_t N = pr.n_reads;
+    KcPiece q;
+    q.r0 = r0;
+    q.n = N;
+    uint32_t *nr = arena.alloc<uint32_t>(N + 1);
+    uint64_t *tot = arena.alloc<uint64_t>(1);
+    size_t tb = scan_tmp_bytes(N + 1);
+    void *tmp = arena.alloc<uint8_t>(tb);
+    q.poff = arena.alloc_persistent<uint64_t>(N + 2);
+    uint64_t P = 0;
+    bool ok = nr && tot && tmp && q.poff;
+    if (ok) {
+        launch_pk_rounds(pr, k, nr, st);
+        ok = cudaMemsetAsync(nr + N, 0, 4, st) == cudaSuccess;
+    }
+    if (ok) {
+        scan_u32_to_u64(nr, q.poff, N + 1, tot, tmp, tb, st);
+        ok = cudaMemcpyAsync(&P, tot, 8, cudaMemcpyDeviceToHost, st) == cudaSuccess &&
+             cudaStreamSynchronize(st) == cudaSuccess;
+    }
+    if (ok) {
+        q.pw = arena.alloc_persistent<uint64_t>(P + 1);
+        q.pn = arena.alloc_persistent<uint32_t>(P + 1);
+        ok = q.pw && q.pn;
+    }
+    arena.free_scratch(nr);
+    arena.free_scratch(tot);
+    arena.free_scratch(tmp);
+    if (!ok) {
+        free_kc_piece(arena, q);
+        return false;
+    }
+    *out = q;
+    return true;
+}
+
+// The enumeration over one piece of the count pass's copy of the reads (either form): every scan's
+// per-read tuple counts (cnt indexed by global read id), and one bucket range's tuples at off.
+int store_count_scans(const KcPiece &q, const uint32_t *seq_len, int k, const uint32_t *bounds, int S, uint32_t *cnt,
+                      uint64_t stride, uint32_t *err, cudaStream_t st)
+{
+    if (!q.n) return 0;
+    if (q.pw) return launch_pk_count_scans(q.poff, q.pw, q.pn, q.r0, q.n, seq_len, k, bounds, S, cnt, stride, err, st);
+    return launch_kc_count_scans(q.off, q.lo, q.hi, q.n, k, bounds, S, cnt + q.r0, stride, err, st);
+}
+
+void store_write(const KcPiece &q, const uint32_t *seq_len, int k, uint32_t lo, uint32_t hi, const uint32_t *label,
+                 const uint64_t *off, uint64_t *o_lo, uint8_t *o_hi, uint32_t *o_id, uint32_t *err, cudaStream_t st)
+{
+    if (q.pw) launch_pk_write(q.poff, q.pw, q.pn, q.r0, q.n, seq_len, k, lo, hi, label, off, o_lo, o_hi, o_id, err, st);
+    else launch_kc_write(q.off, q.lo, q.hi, q.r0, q.n, k, lo, hi, label, off, o_lo, o_hi, o_id, st);
 }
 
 bool make_kc_piece(DeviceArena &arena, cudaStream_t st, const ParsedReads &pr, uint64_t r0, int k, KcPiece *out)
@@ -146,7 +204,7 @@ struct mp_job {
     uint8_t *d_filtered = nullptr;
     // k-mer cache written by the count pass (plain variant), in pieces of consecutive reads (one piece,
     // or one per input segment of mp_job_load_count)
-    bool kc_on = true;
+    int store = STORE_KMER_CACHE;  // what the count pass keeps of the reads for the partition (mp_job_set_read_store)
     int kc_k = 0;
     std::vector<KcPiece> kc;
     cudaStream_t copy_st = nullptr;  // uploads of mp_job_load_count
@@ -172,6 +230,7 @@ struct mp_job {
     int pe_rounds = 0;
     uint64_t piece_tuples = 0;  // most tuples a scan holds in HBM at once (0: from the free device memory)
     int pieces_total = 0;       // bucket-range pieces of the last partition, over all scans
+    uint32_t hooked_bad = ~0u;  // a flagged read the last scan's unions hooked below a component (next scan: BAD)
 };
 
 // ------------------------------------------------------------------ helpers
@@ -320,12 +379,15 @@ void drop_kmer_cache(mp_job *j)
     j->kc_k = 0;
 }
 
-// The cache for the plain variant's count pass, one piece for all reads; false (and no cache) when
-// device memory or the budget does not allow it -- the partition then computes its k-mers from the reads.
+// The store of the reads for the plain variant's count pass (the job's choice: the k-mer cache or the packed
+// reads), one piece for all reads; false (and no store) when the job keeps none or device memory or the
+// budget does not allow it -- the partition then computes its k-mers from the FASTQ bytes.
 bool make_kmer_cache(mp_job *j, int k)
 {
     KcPiece q;
-    if (!make_kc_piece(j->arena, j->st, j->pr, 0, k, &q)) {
+    const bool made = j->store == STORE_PACKED ? make_pk_piece(j->arena, j->st, j->pr, 0, k, &q)
+                                               : make_kc_piece(j->arena, j->st, j->pr, 0, k, &q);
+    if (!made) {
         drop_kmer_cache(j);
         return false;
     }
@@ -519,9 +581,9 @@ int mp_job_count(mp_job *j, int k, int min3, const uint64_t *chunk_starts, int n
     drop_kmer_cache(j);
     {
         StageTimer tm(j->st, &j->stage_ms[1]);
-        const bool kc = j->kc_on && !min3 && make_kmer_cache(j, k);
-        launch_count(j->d_fq, j->pr, k, min3, d_rec, nchunks, cc, glob, err, j->st, kc ? j->kc[0].off : nullptr,
-                     kc ? j->kc[0].lo : nullptr, kc ? j->kc[0].hi : nullptr);
+        const bool kc = j->store != STORE_FASTQ && !min3 && make_kmer_cache(j, k);
+        const KcPiece q = kc ? j->kc[0] : KcPiece{};
+        launch_count(j->d_fq, j->pr, k, min3, d_rec, nchunks, cc, glob, err, j->st, q.off, q.lo, q.hi, q.poff, q.pw, q.pn);
     }
     std::vector<unsigned long long> g(NB);
     uint32_t herr = 0;
@@ -535,6 +597,7 @@ int mp_job_count(mp_job *j, int k, int min3, const uint64_t *chunk_starts, int n
         drop_kmer_cache(j);
         return set_error(MP_EUNSUP, "a read is longer than %d bases", MAX_READ_COUNT);
     }
+    if (herr & DERR_NONACGT) drop_kmer_cache(j);  // a byte the packed reads cannot hold: the FASTQ path
     hist_out[0] = 0;
     for (uint32_t b = 1; b <= NB; b++) hist_out[b] = hist_out[b - 1] + g[b - 1];
     if (chunk_reads_out)
@@ -606,9 +669,12 @@ int load_count_pipelined(mp_job *j, const char *bytes, uint64_t nbytes, const ui
         R[i + 1] = R[i] + prs[i].n_reads;
         StageTimer tm(j->st, &j->stage_ms[1]);
         KcPiece q;
-        if (!make_kc_piece(j->arena, j->st, prs[i], R[i], k, &q)) return MP_ENOMEM;
+        const bool made = j->store == STORE_PACKED ? make_pk_piece(j->arena, j->st, prs[i], R[i], k, &q)
+                                                   : make_kc_piece(j->arena, j->st, prs[i], R[i], k, &q);
+        if (!made) return MP_ENOMEM;
         j->kc.push_back(q);
-        launch_count(j->d_fq + seg[i], prs[i], k, 0, nullptr, 0, nullptr, glob, err, j->st, q.off, q.lo, q.hi);
+        launch_count(j->d_fq + seg[i], prs[i], k, 0, nullptr, 0, nullptr, glob, err, j->st, q.off, q.lo, q.hi, q.poff, q.pw,
+                     q.pn);
     }
     j->kc_k = k;
     const uint64_t N = R[S];
@@ -646,7 +712,8 @@ int load_count_pipelined(mp_job *j, const char *bytes, uint64_t nbytes, const ui
     j->arena.free_persistent(glob);
     j->arena.free_persistent(err);
     j->arena.release_scratch();
-    if (herr) return MP_EUNSUP;
+    if (herr & DERR_NONACGT) drop_kmer_cache(j);  // a byte the packed reads cannot hold: the FASTQ path
+    if (herr & ~DERR_NONACGT) return MP_EUNSUP;
     hist_out[0] = 0;
     for (uint32_t b = 1; b <= NB; b++) hist_out[b] = hist_out[b - 1] + g[b - 1];
     if (chunk_reads_out)
@@ -673,7 +740,8 @@ int mp_job_load_count(mp_job *j, const char *bytes, uint64_t nbytes, const uint6
     cudaPointerAttributes pa{};
     const bool pinned = cudaPointerGetAttributes(&pa, bytes) == cudaSuccess && pa.type == cudaMemoryTypeHost;
     cudaGetLastError();
-    bool ok = pinned && !min3 && j->kc_on && nchunks >= 2 && chunk_starts[0] == 0 && chunk_starts[nchunks] == nbytes;
+    bool ok = pinned && !min3 && j->store != STORE_FASTQ && nchunks >= 2 && chunk_starts[0] == 0 &&
+              chunk_starts[nchunks] == nbytes;
     for (int c = 0; ok && c < nchunks; c++) ok = chunk_starts[c] <= chunk_starts[c + 1];
     if (!ok) return one_by_one();
     std::vector<uint64_t> seg = {0};
@@ -800,8 +868,7 @@ static int scan_in_pieces(mp_job *j, int s, int k, bool has_hi, uint64_t lo, uin
             StageTimer tm(j->st, &j->stage_ms[2]);
             int lrc = 0;
             if (use_kc)
-                for (const KcPiece &q : j->kc)
-                    lrc |= q.n ? launch_kc_count_scans(q.off, q.lo, q.hi, q.n, k, d_b + 2 * i, 1, cnt + q.r0, N + 1, err, j->st) : 0;
+                for (const KcPiece &q : j->kc) lrc |= store_count_scans(q, j->pr.seq_len, k, d_b + 2 * i, 1, cnt, N + 1, err, j->st);
             else
                 launch_enum_count(j->d_fq, j->pr, k, 0, (uint32_t)b0, (uint32_t)b1, cnt, err, j->st);
             if (lrc) return set_error(MP_EARG, "enumeration count of a scan piece");
@@ -814,8 +881,8 @@ static int scan_in_pieces(mp_job *j, int s, int k, bool has_hi, uint64_t lo, uin
                                  (unsigned long long)n, (unsigned long long)expect);
             if (use_kc)
                 for (const KcPiece &q : j->kc)
-                    launch_kc_write(q.off, q.lo, q.hi, q.r0, q.n, k, (uint32_t)b0, (uint32_t)b1, roots, off, sb.lo[0],
-                                    sb.hi[0], sb.id[0], j->st);
+                    store_write(q, j->pr.seq_len, k, (uint32_t)b0, (uint32_t)b1, roots, off, sb.lo[0], sb.hi[0], sb.id[0], err,
+                                j->st);
             else
                 launch_enum_write(j->d_fq, j->pr, k, 0, (uint32_t)b0, (uint32_t)b1, roots, off, sb.lo[0], sb.hi[0],
                                   sb.id[0], err, j->st);
@@ -885,6 +952,11 @@ static int scan_in_pieces(mp_job *j, int s, int k, bool has_hi, uint64_t lo, uin
         if (rc) return rc;
     }
     // ---- sweep 2: the unions, piece by piece, from the scan's initial state
+    rebad_read(j->d_parent, j->hooked_bad, j->st);
+    j->hooked_bad = ~0u;
+    uint32_t *anchor = j->arena.alloc<uint32_t>(2);  // the anchor run's read, the hooked read
+    if (!anchor) return set_error(MP_ENOMEM, "device memory");
+    MP_CUDA(cudaMemsetAsync(anchor, 0xFF, 8, j->st));
     uint32_t first_parent = 0;
     MP_CUDA(cudaMemcpyAsync(&first_parent, j->d_parent + first_id, 4, cudaMemcpyDeviceToHost, j->st));
     MP_CUDA(cudaStreamSynchronize(j->st));
@@ -909,14 +981,16 @@ static int scan_in_pieces(mp_job *j, int s, int k, bool has_hi, uint64_t lo, uin
         {
             StageTimer tm(j->st, &j->stage_ms[5]);
             if ((rc = union_piece(tp, bounds, part_seen, last_kmer, first_id, first_parent != BAD, j->d_parent,
-                                  j->d_filtered, j->arena, j->st, has_valid)))
+                                  j->d_filtered, j->arena, j->st, has_valid, anchor)))
                 return rc;
         }
         for (size_t q = 0; q < which.size(); q++) seen[which[q]] |= has_valid[q];
     }
     {
         StageTimer tm(j->st, &j->stage_ms[5]);
+        if (have_first && first_parent == BAD) hook_bad_anchor(j->d_parent, first_id, anchor, anchor + 1, j->st);
         compress_parents(j->d_parent, N, j->st);
+        MP_CUDA(cudaMemcpyAsync(&j->hooked_bad, anchor + 1, 4, cudaMemcpyDeviceToHost, j->st));
         MP_CUDA(cudaStreamSynchronize(j->st));
         MP_CUDA(cudaGetLastError());
     }
@@ -1003,8 +1077,7 @@ int mp_job_partition(mp_job *j, const mp_part_params *p, const uint64_t *chunk_s
             MP_CUDA(cudaMemcpyAsync(d_b, hb.data(), (S + 1) * 4, cudaMemcpyHostToDevice, j->st));
             int lrc = 0;
             if (use_kc)
-                for (const KcPiece &q : j->kc)
-                    lrc |= q.n ? launch_kc_count_scans(q.off, q.lo, q.hi, q.n, k, d_b, S, cnt_all + q.r0, N + 1, err, j->st) : 0;
+                for (const KcPiece &q : j->kc) lrc |= store_count_scans(q, j->pr.seq_len, k, d_b, S, cnt_all, N + 1, err, j->st);
             else
                 lrc = launch_enum_count_scans(j->d_fq, j->pr, k, d_b, S, cnt_all, N + 1, err, j->st);
             if (lrc) return set_error(MP_EARG, "enumeration count over %d scans", S);
@@ -1012,6 +1085,7 @@ int mp_job_partition(mp_job *j, const mp_part_params *p, const uint64_t *chunk_s
         }
     }
     j->pieces_total = 0;
+    j->hooked_bad = ~0u;
     const uint64_t piece_cap = p->min3 ? ~0ull : scan_piece_cap(j);  // the 3-minimizer choice depends on the range
     for (int s = 0; s < S; s++) {
         const uint64_t lo = scanR[s], hi = scanR[s + 1];
@@ -1077,8 +1151,8 @@ int mp_job_partition(mp_job *j, const mp_part_params *p, const uint64_t *chunk_s
             }
             if (use_kc && cnt_all)
                 for (const KcPiece &q : j->kc)
-                    launch_kc_write(q.off, q.lo, q.hi, q.r0, q.n, k, (uint32_t)lo, (uint32_t)hi, s ? j->d_parent : nullptr,
-                                    off, sb.lo[0], sb.hi[0], sb.id[0], j->st);
+                    store_write(q, j->pr.seq_len, k, (uint32_t)lo, (uint32_t)hi, s ? j->d_parent : nullptr, off, sb.lo[0],
+                                sb.hi[0], sb.id[0], err, j->st);
             else
                 launch_enum_write(j->d_fq, j->pr, k, p->min3, (uint32_t)lo, (uint32_t)hi, s ? j->d_parent : nullptr, off,
                                   sb.lo[0], sb.hi[0], sb.id[0], err, j->st);
@@ -1124,7 +1198,8 @@ int mp_job_partition(mp_job *j, const mp_part_params *p, const uint64_t *chunk_s
         }
         {
             StageTimer tm(j->st, &j->stage_ms[5]);
-            if ((rc = union_scan(tp, rb, j->d_parent, j->d_filtered, N, j->arena, j->st))) return rc;
+            if ((rc = union_scan(tp, rb, j->d_parent, j->d_filtered, N, j->arena, j->st, j->hooked_bad, &j->hooked_bad)))
+                return rc;
         }
         j->arena.release_scratch();
         snprintf(name, sizeof name, "stats%d_parent.bin", s);
@@ -1276,9 +1351,26 @@ int mp_job_kmer_cache_pieces(const mp_job *j) { return j ? (int)j->kc.size() : 0
 int mp_job_set_kmer_cache(mp_job *j, int enable)
 {
     if (!j) return set_error(MP_EARG, "null job");
-    j->kc_on = enable != 0;
-    if (!j->kc_on) drop_kmer_cache(j);
+    j->store = enable ? STORE_KMER_CACHE : STORE_FASTQ;
+    if (!enable) drop_kmer_cache(j);
     return 0;
+}
+
+int mp_job_set_read_store(mp_job *j, int store)
+{
+    if (!j) return set_error(MP_EARG, "null job");
+    if (store != MP_STORE_FASTQ && store != MP_STORE_KMER_CACHE && store != MP_STORE_PACKED)
+        return set_error(MP_EARG, "unknown read store %d", store);
+    if (store != j->store) drop_kmer_cache(j);
+    j->store = store;
+    return 0;
+}
+
+int mp_job_read_store(const mp_job *j)
+{
+    if (!j) return set_error(MP_EARG, "null job");
+    if (j->kc.empty()) return MP_STORE_FASTQ;
+    return j->kc[0].pw ? MP_STORE_PACKED : MP_STORE_KMER_CACHE;
 }
 
 int mp_job_set_wait_limits(mp_job *j, uint32_t lookback_spins, uint32_t union_retries, uint32_t mate_rounds)

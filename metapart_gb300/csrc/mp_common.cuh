@@ -20,6 +20,7 @@ enum DevErr : uint32_t {
     DERR_LONG_READ = 1u << 1,  // read longer than the kernel supports
     DERR_OVERFLOW = 1u << 2,   // more output than the count pass reserved
     DERR_TOO_MANY = 1u << 3,   // a read has 256 or more tuples in one scan
+    DERR_NONACGT = 1u << 4,    // a sequence byte other than A, C, G, T, N (no packed copy of the reads)
 };
 
 // Iteration limits of the device's bounded waits: the sort's look-back polls of one status word, the

@@ -102,6 +102,7 @@ void run_request(mp_server *s, mp_job *job, Request &rq, mp_result &res)
     int rc = mp_fastq_index(C, 0, p.interleaved ? 0 : 1, p.interleaved ? 1 : 0, 1, files, &rq.nbytes, fno.data(),
                             ofs.data(), &nrec);
     if (!rc && nrec != C + 1) rc = MP_EFMT;
+    if (!rc) rc = mp_job_set_read_store(job, p.read_store);
     if (!rc) {
         starts.assign(ofs.begin(), ofs.begin() + nrec);
         starts[nrec - 1] = rq.nbytes;
@@ -208,7 +209,8 @@ uint64_t mp_request_footprint(const char *fastq, uint64_t nbytes, const mp_reque
     f += tuples * 27.0;                                 // two tuple buffers of 13 B + look-back status
     f += (double)nbytes * (p->interleaved ? 2 : 1);     // partition FASTQ
     f += reads * 40.0;                                  // output entries and their sort
-    f += bases * 9.0;                                   // k-mer cache of the count pass
+    if (p->read_store == MP_STORE_KMER_CACHE) f += bases * 9.0;            // k-mer cache of the count pass
+    else if (p->read_store == MP_STORE_PACKED) f += bases * 0.375 + reads * 8;  // packed reads and their offsets
     f += 64.0 * (1 << 20);                              // histograms, scan scratch
     return (uint64_t)(f * 1.10);
 }

@@ -62,6 +62,8 @@ def lib():
         L.mp_job_set_dump_dir.argtypes = [C.c_void_p, C.c_char_p]
         L.mp_job_set_kmer_cache.argtypes = [C.c_void_p, C.c_int]
         L.mp_job_set_scan_piece_tuples.argtypes = [C.c_void_p, C.c_uint64]
+        L.mp_job_set_read_store.argtypes = [C.c_void_p, C.c_int]
+        L.mp_job_read_store.argtypes = [C.c_void_p]
         L.mp_job_set_wait_limits.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32]
         L.mp_batch_set_wait_limits.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32]
         L.mp_job_scan_pieces.argtypes = [C.c_void_p]
@@ -217,6 +219,17 @@ class Job:
         """Keep the count pass's k-mers for the next partition of the same k (default on)."""
         _check(lib().mp_job_set_kmer_cache(self.h, int(enable)), "set_kmer_cache")
 
+    STORES = {"fastq": 0, "kmer_cache": 1, "packed": 2}
+
+    def set_read_store(self, store: str):
+        """What the count pass keeps of the reads for the partition: "kmer_cache" (default), "packed" or "fastq"."""
+        _check(lib().mp_job_set_read_store(self.h, self.STORES[store]), "set_read_store")
+
+    @property
+    def read_store(self) -> str:
+        v = lib().mp_job_read_store(self.h)
+        return {b: a for a, b in self.STORES.items()}[v]
+
     def set_scan_piece_tuples(self, max_tuples: int):
         """Most tuples a scan holds in HBM at once (0: from the free device memory); a larger scan runs in
         bucket-range pieces with the same results."""
@@ -344,12 +357,14 @@ def chunk_starts_of(fno: np.ndarray, ofs: np.ndarray, file_sizes) -> np.ndarray:
 
 
 def run_pipeline(ctx: Context, fastq: bytes, k: int, num_chunks: int, num_scans: int, num_threads: int,
-                 min3: bool = False, interleaved: bool = False, dump_dir=None, kmer_cache: bool = True):
-    """genFastqIdx -> genHistograms -> metapart on one in-memory FASTQ; returns (job, bounds, count)."""
+                 min3: bool = False, interleaved: bool = False, dump_dir=None, kmer_cache: bool = True,
+                 store: str | None = None):
+    """genFastqIdx -> genHistograms -> metapart on one in-memory FASTQ; returns (job, bounds, count).  store
+    ("kmer_cache", "packed", "fastq") overrides kmer_cache."""
     fno, ofs = fastq_index(num_chunks, [fastq], interleaved)
     starts = chunk_starts_of(fno, ofs, [len(fastq)])
     job = Job(ctx)
-    job.set_kmer_cache(kmer_cache)
+    job.set_read_store(store or ("kmer_cache" if kmer_cache else "fastq"))
     if dump_dir:
         job.set_dump_dir(dump_dir)
     job.load(fastq, interleaved=interleaved)

@@ -17,8 +17,13 @@ from . import native
 
 
 class RequestParams(C.Structure):
+    """k, min3, num_scans, num_threads, num_chunks, interleaved, read_store (default: the packed reads, the
+    smallest admission footprint)."""
     _fields_ = [("k", C.c_int), ("min3", C.c_int), ("num_scans", C.c_int), ("num_threads", C.c_int),
-                ("num_chunks", C.c_int), ("interleaved", C.c_int)]
+                ("num_chunks", C.c_int), ("interleaved", C.c_int), ("read_store", C.c_int)]
+
+    def __init__(self, k=31, min3=0, num_scans=1, num_threads=16, num_chunks=64, interleaved=0, read_store=2):
+        super().__init__(k, min3, num_scans, num_threads, num_chunks, interleaved, read_store)
 
 
 class _Result(C.Structure):

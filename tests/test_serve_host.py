@@ -20,3 +20,9 @@ def test_footprint_covers_input_output_and_tuples(built_gpu):
     assert _fp(large, scans=2) < fl            # a second scan halves the largest tuple buffers
     assert _fp(large, il=1) > fl               # interleaved output may hold each pair twice
     assert fl < 64 * len(large) + (256 << 20)  # and the estimate stays proportionate
+    # the count pass's store of the reads: 9 bytes per position for the k-mer cache, 0.375 per base packed
+    buf = C.create_string_buffer(large, len(large))
+    fp = {st: serve.footprint(C.addressof(buf), len(large), serve.RequestParams(31, 0, 1, 2, 4, 0, st))
+          for st in (0, 1, 2)}
+    assert fp[0] < fp[2] < fp[1]
+    assert fp[1] - fp[0] >= 9 * bases and fp[2] - fp[0] < bases
