@@ -346,6 +346,69 @@ __global__ void k_range_first_valid(const uint64_t *lo, const uint8_t *hi, const
     first[t] = f;
 }
 
+// A BAD read as a sweep's initial anchor.  A thread range's sweep starts from the scan's last k-mer and
+// the scan's first read (metapart.c:2539-2545), so the run of the range's first valid tuple is united with
+// that read when it carries the last k-mer, BAD or not.  findRoot returns a read whose parent is BAD as
+// its own root (unionfind.h:25) and each union hooks the smaller root below the larger (:2680-2700).  So
+// with a BAD first read B the run's components are hooked below B while their roots are smaller than B,
+// until one is larger: B then goes below it and is a member like any other (parent no longer BAD).  If
+// none is, B keeps its BAD parent and the edge replay's assertion stops the reference (:2772).  The run is
+// the scan's last and the range is the last with tuples, so nothing else joins the component after it:
+// the outcome is B below the component's final root when B is smaller than that root, else nothing.
+// Here the run is united like any other (its first valid tuple as anchor) and B is hooked afterwards.
+// At most one range of a scan has its first valid tuple in the last run (ranges end between buckets).
+
+// The read of the range's first valid tuple when that tuple carries the scan's last k-mer (~0u stays).
+__global__ void k_bad_anchor_find(const uint64_t *lo, const uint8_t *hi, const uint32_t *id, const uint64_t *first, int T,
+                                  uint64_t init_kmer, uint32_t *anchor_v)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= T) return;
+    const uint64_t f = first[t];
+    if (f != ~0ull && kmer_of(lo, hi, f) == init_kmer) *anchor_v = id[f];
+}
+
+__device__ __forceinline__ uint32_t root_of(const uint32_t *parent, uint32_t x)
+{
+    for (uint32_t it = 0; it < UF_CAP; it++) {
+        const uint32_t p = parent[x];
+        if (p == x || p == BAD) break;
+        x = p;
+    }
+    return x;
+}
+
+// After the scan's unions: hooks the BAD first read below the root of the run's component when it is the
+// smaller id (records it in *hooked, which the next scan marks BAD again like every flagged read).
+__global__ void k_bad_anchor_hook(uint32_t *parent, uint32_t b, const uint32_t *anchor_v, uint32_t *hooked)
+{
+    const uint32_t v = *anchor_v;
+    if (v == ~0u || parent[b] != BAD) return;
+    const uint32_t r = root_of(parent, v);
+    if (b < r) {
+        parent[b] = r;
+        *hooked = b;
+    }
+}
+
+// The same for every range of a batch (each sample its own scan, its own first read and last k-mer).
+__global__ void k_seg_bad_anchor(const uint64_t *lo, const uint8_t *hi, const uint32_t *id, const uint64_t *first, int R,
+                                 const uint64_t *r_kmer, const uint32_t *r_min, const uint32_t *r_ok, uint32_t *parent)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= R) return;
+    const uint64_t f = first[t];
+    if (r_ok[t] || f == ~0ull || kmer_of(lo, hi, f) != r_kmer[t]) return;
+    const uint32_t b = r_min[t];
+    if (parent[b] != BAD) return;
+    const uint32_t r = root_of(parent, id[f]);
+    if (b < r) parent[b] = r;
+}
+
+// markMischiefKmers' closing sweep (metapart.c:2503-2516) at a later scan: a flagged read whose parent is
+// not BAD gets BAD again.  Only a hooked first read (above) can be one.
+__global__ void k_rebad(uint32_t *parent, uint32_t r) { parent[r] = BAD; }
+
 struct EdgeCtx {
     const uint64_t *lo;
     const uint8_t *hi;
@@ -730,13 +793,16 @@ int filter_scan(Tuples &tp, const std::vector<uint64_t> &range_bounds, uint32_t 
 }
 
 int union_scan(Tuples &tp, const std::vector<uint64_t> &range_bounds, uint32_t *parent, const uint8_t *filtered,
-               uint64_t n_reads, DeviceArena &arena, cudaStream_t st)
+               uint64_t n_reads, DeviceArena &arena, cudaStream_t st, uint32_t rebad, uint32_t *hooked)
 {
     const uint64_t n = tp.n;
     const int T = (int)range_bounds.size() - 1;
-    uint32_t *err = arena.alloc<uint32_t>(1);
+    *hooked = ~0u;
+    uint32_t *err = arena.alloc<uint32_t>(3);  // error flags, the anchor run's read, the hooked read
     if (!err) return set_error(MP_ENOMEM, "device memory");
-    MP_CUDA(cudaMemsetAsync(err, 0, sizeof *err, st));
+    MP_CUDA(cudaMemsetAsync(err, 0, 4, st));
+    MP_CUDA(cudaMemsetAsync(err + 1, 0xFF, 8, st));
+    if (rebad != ~0u) (mp::count_launch(), k_rebad<<<1, 1, 0, st>>>(parent, rebad));
     if (n) {
         uint64_t *bounds = arena.alloc<uint64_t>(T + 1), *first = arena.alloc<uint64_t>(T);
         if (!bounds || !first) return set_error(MP_ENOMEM, "device memory for union-find");
@@ -765,21 +831,26 @@ int union_scan(Tuples &tp, const std::vector<uint64_t> &range_bounds, uint32_t *
         c.uf_cap = arena.lim.union_retries;
         (mp::count_launch(), k_range_first_valid<<<blocks_for(T, 64), 64, 0, st>>>(tp.lo, tp.hi, tp.id, tp.z, bounds, T, parent,
                                                                                   first));
+        if (!c.init_min_ok)
+            (mp::count_launch(), k_bad_anchor_find<<<blocks_for(T, 64), 64, 0, st>>>(tp.lo, tp.hi, tp.id, first, T, c.init_kmer,
+                                                                                    err + 1));
         const uint64_t warps = (n + SEG - 1) / SEG;
         (mp::count_launch(), k_edges_warp<false><<<blocks_for(warps * 32, 256), 256, 0, st>>>(c));
+        if (!c.init_min_ok) (mp::count_launch(), k_bad_anchor_hook<<<1, 1, 0, st>>>(parent, c.init_min, err + 1, err + 2));
     }
     (mp::count_launch(), k_compress<<<blocks_for(n_reads, 256), 256, 0, st>>>(parent, n_reads));
-    uint32_t herr = 0;
-    MP_CUDA(cudaMemcpyAsync(&herr, err, sizeof herr, cudaMemcpyDeviceToHost, st));
+    uint32_t h[3] = {0, 0, 0};
+    MP_CUDA(cudaMemcpyAsync(h, err, sizeof h, cudaMemcpyDeviceToHost, st));
     MP_CUDA(cudaStreamSynchronize(st));
     MP_CUDA(cudaGetLastError());
-    if (herr) return set_error(MP_EDEVICE, "union-find retry limit reached (flags 0x%x)", herr);
+    if (h[0]) return set_error(MP_EDEVICE, "union-find retry limit reached (flags 0x%x)", h[0]);
+    *hooked = h[2];
     return 0;
 }
 
 int union_piece(Tuples &tp, const std::vector<uint64_t> &bounds, const std::vector<uint8_t> &seen, uint64_t init_kmer,
                 uint32_t init_min, bool init_min_ok, uint32_t *parent, const uint8_t *filtered, DeviceArena &arena,
-                cudaStream_t st, std::vector<uint8_t> &has_valid)
+                cudaStream_t st, std::vector<uint8_t> &has_valid, uint32_t *anchor_v)
 {
     const uint64_t n = tp.n;
     const int T = (int)bounds.size() - 1;
@@ -801,6 +872,9 @@ int union_piece(Tuples &tp, const std::vector<uint64_t> &bounds, const std::vect
         if (seen[t]) hf[t] = ~0ull;
     }
     MP_CUDA(cudaMemcpyAsync(first, hf.data(), T * sizeof(uint64_t), cudaMemcpyHostToDevice, st));
+    if (!init_min_ok)
+        (mp::count_launch(), k_bad_anchor_find<<<blocks_for(T, 64), 64, 0, st>>>(tp.lo, tp.hi, tp.id, first, T, init_kmer,
+                                                                                anchor_v));
     EdgeCtx c;
     c.lo = tp.lo; c.hi = tp.hi; c.id = tp.id; c.z = tp.z; c.n = n;
     c.first_valid = first; c.range_bounds = d_bounds; c.T = T; c.parent = parent; c.filtered = filtered; c.err = err;
@@ -819,6 +893,16 @@ int union_piece(Tuples &tp, const std::vector<uint64_t> &bounds, const std::vect
     MP_CUDA(cudaGetLastError());
     if (herr) return set_error(MP_EDEVICE, "union-find retry limit reached (flags 0x%x)", herr);
     return 0;
+}
+
+void rebad_read(uint32_t *parent, uint32_t r, cudaStream_t st)
+{
+    if (r != ~0u) (mp::count_launch(), k_rebad<<<1, 1, 0, st>>>(parent, r));
+}
+
+void hook_bad_anchor(uint32_t *parent, uint32_t b, const uint32_t *anchor_v, uint32_t *hooked, cudaStream_t st)
+{
+    (mp::count_launch(), k_bad_anchor_hook<<<1, 1, 0, st>>>(parent, b, anchor_v, hooked));
 }
 
 void compress_parents(uint32_t *parent, uint64_t n_reads, cudaStream_t st)
@@ -993,6 +1077,7 @@ int union_segments(Tuples &tp, const std::vector<uint64_t> &range_bounds, const 
         c.uf_cap = arena.lim.union_retries;
         const uint64_t warps = (n + SEG - 1) / SEG;
         (mp::count_launch(), k_edges_warp<true><<<blocks_for(warps * 32, 256), 256, 0, st>>>(c));
+        (mp::count_launch(), k_seg_bad_anchor<<<blocks_for(R, 64), 64, 0, st>>>(tp.lo, tp.hi, tp.id, first, R, rk, rm, ro, parent));
     }
     (mp::count_launch(), k_compress<<<blocks_for(n_reads, 256), 256, 0, st>>>(parent, n_reads));
     uint32_t herr = 0;

@@ -18,18 +18,25 @@ struct Tuples {
 // multi: the ranges of several scans one after another (a batch of samples), whose boundaries may cut a run.
 int filter_scan(Tuples &tp, const std::vector<uint64_t> &range_bounds, uint32_t *parent, uint8_t *filtered,
                 DeviceArena &arena, cudaStream_t st, bool apply_zero, bool multi = false);
-// K5: unionFindPar2 + unionFind + printStats compression for the scan.
+// K5: unionFindPar2 + unionFind + printStats compression for the scan.  rebad: a read flagged in an
+// earlier scan whose parent is not BAD (the first read an earlier scan hooked below a component), marked
+// BAD again first; ~0u for none.  *hooked: the scan's BAD first read when it was hooked below the
+// component of the scan's last run (~0u otherwise), for the next scan's rebad.
 int union_scan(Tuples &tp, const std::vector<uint64_t> &range_bounds, uint32_t *parent, const uint8_t *filtered,
-               uint64_t n_reads, DeviceArena &arena, cudaStream_t st);
+               uint64_t n_reads, DeviceArena &arena, cudaStream_t st, uint32_t rebad, uint32_t *hooked);
 // K5 for one piece of a scan split by bucket ranges (the scan's tuples do not fit at once): the sweep of
 // unionFindPar2 over the piece's part of the thread ranges.  bounds: T' + 1 tuple bounds of those parts;
 // seen[t] = 1 when part t's thread range had a valid tuple in an earlier piece; init_*: the scan's initial
 // sweep state (its last tuple's k-mer after the filter, its first tuple's read, whether that read was BAD
 // when the scan's unions began).  On return has_valid[t] = 1 when part t holds a valid tuple.  No
-// compression (compress_parents, once the scan's last piece is done).
+// compression (compress_parents, once the scan's last piece is done).  With a BAD first read, *anchor_v
+// (device) receives the read of the range's first valid tuple when that tuple carries init_kmer; after
+// the last piece, hook_bad_anchor does what union_scan does with it.
 int union_piece(Tuples &tp, const std::vector<uint64_t> &bounds, const std::vector<uint8_t> &seen, uint64_t init_kmer,
                 uint32_t init_min, bool init_min_ok, uint32_t *parent, const uint8_t *filtered, DeviceArena &arena,
-                cudaStream_t st, std::vector<uint8_t> &has_valid);
+                cudaStream_t st, std::vector<uint8_t> &has_valid, uint32_t *anchor_v);
+void rebad_read(uint32_t *parent, uint32_t r, cudaStream_t st);
+void hook_bad_anchor(uint32_t *parent, uint32_t b, const uint32_t *anchor_v, uint32_t *hooked, cudaStream_t st);
 void compress_parents(uint32_t *parent, uint64_t n_reads, cudaStream_t st);
 // K6: sizes, unionFindPeReads(1000), final compression and the 17 partition bounds (host).
 int mate_union_and_plan(uint32_t *parent, uint64_t n_reads, uint32_t *size, uint64_t *bounds_out, DeviceArena &arena,

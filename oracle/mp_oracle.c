@@ -765,21 +765,26 @@ static void mischief(tup *t, uint64_t n)
     }
 }
 
-/* unionFindPar2 body for one thread range (metapart.c:2537-2727), applied sequentially */
-static void range_unions(const tup *t, uint64_t n, uint64_t init_kmer, uint64_t init_min)
+/* unionFindPar2 body for one thread range (metapart.c:2537-2727), applied sequentially.  The initial
+   anchor (the scan's first read) may be BAD: findRoot returns it as its own root and the hooks go on as
+   for any read.  Returns 1 when it united that BAD read (the caller checks the replay's assertion). */
+static int range_unions(const tup *t, uint64_t n, uint64_t init_kmer, uint64_t init_min)
 {
     uint64_t cur = init_kmer, mn = init_min;
+    int bad_anchor = 0;
     for (uint64_t i = 0; i < n; i++) {
         uint64_t id = t[i].id;
         if (g_parent[id] == BADV) continue;
         if (t[i].kmer == 0) continue;
         if (t[i].kmer != cur) { cur = t[i].kmer; mn = id; continue; }
+        if (mn == init_min && g_parent[mn] == BADV) bad_anchor = 1;
         uint64_t pu = mn, pv = id;
         if (pu != pv) { pu = find_root(pu); pv = find_root(pv); }
         if (pu != pv) {
             if (pu > pv) g_parent[pv] = pu; else g_parent[pu] = pv;
         }
     }
+    return bad_anchor;
 }
 
 typedef struct { FILE **fp; int T; } outset;
@@ -979,7 +984,16 @@ int mpo_metapart(const char *out_prefix, uint64_t fastq_buffer_size, int k, int 
         /* unionFindPar2 + unionFind (:2520-2800) */
         if (n) {
             uint64_t init_kmer = arr[n - 1].kmer, init_min = arr[0].id;
-            for (int t = 0; t < T; t++) range_unions(arr + bcount[t], bcount[t + 1] - bcount[t], init_kmer, init_min);
+            int bad_anchor = 0;
+            for (int t = 0; t < T; t++)
+                bad_anchor |= range_unions(arr + bcount[t], bcount[t + 1] - bcount[t], init_kmer, init_min);
+            /* the replay (unionFind, metapart.c:2772) asserts that no edge's read has a BAD parent: a BAD first
+               read that no union hooked below a larger root stops the reference here */
+            if (bad_anchor && g_parent[init_min] == BADV) {
+                rc = fail(MPO_EUNSUP, "scan %d: the first read (%llu) is BAD and its run's roots are all smaller; the "
+                          "reference's edge replay asserts (metapart.c:2772)", s, (unsigned long long)init_min);
+                goto out;
+            }
         }
         print_stats();
         snprintf(name, sizeof name, "stats%d_parent.bin", s);

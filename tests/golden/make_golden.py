@@ -6,7 +6,9 @@ and the SHA-256 of every output (index files with padding masked, histogram, sta
 is recorded together with the SHA-256 of the input.  The bundled reference fixture (data/reads.fastq) is
 used when the reference tree is present; its bytes are not stored, only the digests of the outputs.
 
-    python tests/golden/make_golden.py [REFERENCE_ROOT]
+    python tests/golden/make_golden.py [REFERENCE_ROOT] [--only CASE ...]
+
+With --only, the named cases are regenerated and the others kept as they are in golden.json.
 """
 from __future__ import annotations
 
@@ -37,6 +39,11 @@ CASES = {
     "edge_k31": dict(gen=("edge", 2000, 9), p=dict(k=31, chunks=4, scans=1, threads=2)),
     "edge_k15_s2": dict(gen=("edge", 2000, 10), p=dict(k=15, chunks=4, scans=2, threads=2)),
     "edge_min3_k21": dict(gen=("edge", 2000, 11), p=dict(k=21, chunks=4, scans=1, threads=2, min3=True)),
+    # the scan's first read is BAD and its last run is a thread range's first valid run (BAD_ANCHOR below)
+    "bad_anchor_k27": dict(gen=("bad_anchor", 0, 0), p=dict(k=27, chunks=4, scans=1, threads=1)),
+    "bad_anchor_k27_t2": dict(gen=("bad_anchor", 0, 0), p=dict(k=27, chunks=4, scans=1, threads=2)),
+    "bad_anchor_k27_s2": dict(gen=("bad_anchor", 1, 0), p=dict(k=27, chunks=4, scans=2, threads=1)),
+    "bad_anchor_k27_s2_t2": dict(gen=("bad_anchor", 1, 0), p=dict(k=27, chunks=4, scans=2, threads=2)),
     "bundled_k27": dict(gen=("bundled", 0, 0), p=dict(k=27, chunks=4, scans=1, threads=2, interleaved=True)),
     "bundled_min3_k27": dict(gen=("bundled", 0, 0), p=dict(k=27, chunks=4, scans=1, threads=2, interleaved=True,
                                                           min3=True)),
@@ -95,6 +102,26 @@ def edge_fastq(n: int, seed: int, k: int, min3: bool) -> bytes:
     return "".join(recs).encode()
 
 
+BAD_ANCHOR = ("first", "two_scans", "last")
+
+
+def bad_anchor_fastq(variant: int) -> bytes:
+    """A BAD read as the scan's first tuple's read while a thread range's first valid run is the scan's
+    last run, so that the sweep's initial state unites that run with a BAD read.  Four poly-A reads end in
+    C, G, T, C: their last all-A k-mer has another next base than the poly-A run's majority, which flags
+    them BAD, and the first of them holds the scan's first tuple (the all-A k-mer).  Four poly-C reads hold
+    the scan's last k-mer; every tuple before them has a BAD read or the k-mer 0, so the poly-C run is the
+    first valid run of its range.  "two_scans" adds eight (GC)* reads, whose k-mers sort above poly-C and
+    fill a second scan.  "last" puts the poly-C reads first, so that the BAD read's id is above the run's
+    root."""
+    L = 100
+    bad = ["A" * (L - 1) + c for c in "CGTC"]
+    poly_c = ["C" * L] * 4
+    gc = [("GC" * L)[:L]] * 8
+    reads = {"first": bad + poly_c, "two_scans": bad + poly_c + gc, "last": poly_c + bad}[BAD_ANCHOR[variant]]
+    return "".join(f"@b{i}\n{s}\n+\n{'I' * len(s)}\n" for i, s in enumerate(reads)).encode()
+
+
 def make_input(gen, ref_root: Path, k: int, min3: bool = False) -> bytes | None:
     from metapart_gb300 import synth
     name, n, seed = gen
@@ -103,6 +130,8 @@ def make_input(gen, ref_root: Path, k: int, min3: bool = False) -> bytes | None:
         return f.read_bytes() if f and f.exists() else None
     if name == "edge":
         return edge_fastq(n, seed, k, min3)
+    if name == "bad_anchor":
+        return bad_anchor_fastq(n)
     return synth.fastq_bytes(synth.workload(name, n, seed=seed))
 
 
@@ -113,13 +142,19 @@ def params(d: dict) -> pu.Params:
 def main():
     from metapart_gb300 import build
     build.build_synth()
-    if len(sys.argv) > 1:
-        os.environ["MP_REFERENCE_ROOT"] = sys.argv[1]
-    if not build.build_reference(force=len(sys.argv) > 1):
+    args = sys.argv[1:]
+    only = args[args.index("--only") + 1:] if "--only" in args else None
+    if only is not None:
+        args = args[:args.index("--only")]
+    if args:
+        os.environ["MP_REFERENCE_ROOT"] = args[0]
+    if not build.build_reference(force=bool(args)):
         raise SystemExit("reference sources not found: cannot regenerate golden digests")
     ref_root = build.reference_root()
-    out = {}
+    out = json.loads((HERE / "golden.json").read_text()) if only else {}
     for name, c in CASES.items():
+        if only and name not in only:
+            continue
         data = make_input(c["gen"], ref_root, c["p"]["k"], c["p"].get("min3", False))
         if data is None:
             continue

@@ -27,12 +27,21 @@ def test_oracle_equals_reference(tmp_path, built, name, n, seed, p):
         pytest.skip("reference programs not built here")
     fq = tmp_path / "in.fastq"
     synth.write_fastq(synth.workload(name, n, seed=seed), fq)
-    a = pu.outputs(pu.run("ref", tmp_path, [fq], p), p, "in.fastq")
     b = pu.outputs(pu.run("oracle", tmp_path, [fq], p), p, "in.fastq")
-    assert sorted(a) == sorted(b)
     # compSizes between scans: the reference's edge replay (unionFind, metapart.c:2736-2800) runs its
     # unionOp calls on every thread at once without atomics, so with giant components the sizes it
     # accumulates depend on thread timing; nothing reads them before the reset ahead of the mate union
     # (metapart.c:4010-4030), whose sizes are compared with everything else.
     racy = {f"dump/stats{s}_sizes.bin" for s in range(p.scans)}
-    assert pu.diff_keys(a, b, [x for x in sorted(a) if x not in racy]) == []
+    # The same replay also writes parents from every thread at once; a hook lost to another thread's write
+    # after the loser's last pass stays lost, so on rare runs (seen once in about 30 runs of this case)
+    # the reference's outputs differ from run to run.  The oracle is the union of all edges, the
+    # outcome of a run without such a loss: a mismatch runs the reference again, up to three runs.
+    diffs = []
+    for _ in range(3):
+        a = pu.outputs(pu.run("ref", tmp_path, [fq], p), p, "in.fastq")
+        assert sorted(a) == sorted(b)
+        diffs = pu.diff_keys(a, b, [x for x in sorted(a) if x not in racy])
+        if not diffs or p.threads == 1:
+            break
+    assert diffs == []
