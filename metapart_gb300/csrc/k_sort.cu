@@ -487,22 +487,26 @@ __device__ void seg_pass(SegSmemT<THREADS, CAP> &sm, int cur, uint32_t cnt, int 
         __syncwarp();
     }
     __syncthreads();
-    // thread d: exclusive prefix of digit d over the warps (into the rows), then the digit's start
-    uint32_t colsum = 0, x = 0;
-    const uint32_t d = threadIdx.x;
-    if (d < nbins) {  // nbins is a multiple of 32: whole warps take part in the shuffles
+    // thread t: digits 2t and 2t + 1 (one 32-bit word of each row): their exclusive prefixes over the warps
+    // (into the rows), then their starts
+    uint32_t clo = 0, chi = 0, x = 0;
+    const uint32_t t = threadIdx.x, npair = nbins / 2;  // nbins >= 32: at least 16 pairs
+    if (t < ((npair + 31) & ~31u)) {  // whole warps take part in the shuffles
+        if (t < npair) {
 #pragma unroll
-        for (int w0 = 0; w0 < SS_WARPS; w0 += 8) {
-            uint32_t t[8];
+            for (int w0 = 0; w0 < SS_WARPS; w0 += 8) {
+                uint32_t v[8];
 #pragma unroll
-            for (int i = 0; i < 8; i++) t[i] = sm.whist[w0 + i][d];
+                for (int i = 0; i < 8; i++) v[i] = reinterpret_cast<const uint32_t *>(sm.whist[w0 + i])[t];
 #pragma unroll
-            for (int i = 0; i < 8; i++) {
-                sm.whist[w0 + i][d] = (uint16_t)colsum;
-                colsum += t[i];
+                for (int i = 0; i < 8; i++) {
+                    reinterpret_cast<uint32_t *>(sm.whist[w0 + i])[t] = clo | (chi << 16);
+                    clo += v[i] & 0xFFFFu;
+                    chi += v[i] >> 16;
+                }
             }
         }
-        x = colsum;
+        x = clo + chi;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
             const uint32_t y = __shfl_up_sync(FULLM, x, o);
@@ -511,10 +515,10 @@ __device__ void seg_pass(SegSmemT<THREADS, CAP> &sm, int cur, uint32_t cnt, int 
         if (lane == 31) sm.wsum[warp] = x;
     }
     __syncthreads();
-    if (d < nbins) {
-        uint32_t before = x - colsum;
+    if (t < npair) {
+        uint32_t before = x - clo - chi;
         for (int w = 0; w < warp; w++) before += sm.wsum[w];
-        sm.dstart[d] = (uint16_t)before;
+        reinterpret_cast<uint32_t *>(sm.dstart)[t] = before | ((before + clo) << 16);
     }
     __syncthreads();
 #pragma unroll
