@@ -12,7 +12,7 @@ union, the 16 work partitions and the partition-FASTQ gather.
   cpu_baseline -- the CPU oracle (the reference's algorithm restated in C/OpenMP, all host cores) on a
             bounded sample of the same read set; the GPU's partition files of that sample are compared with
             the oracle's ("parity")
-  batch  -- the batching configuration (64 samples of 50k-5M reads): the samples back to back through one
+  batch  -- the batch workload (64 samples of 50k-5M reads): the samples back to back through one
             job ("plain") against mp_batch_run ("batched"), both from pinned host FASTQ to partition files
   serve  -- Poisson arrivals of partition requests into the request loop: p50/p99 job latency
 
@@ -380,7 +380,7 @@ def main():
     if dist.rank == 0 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(args)
         line["parity"] = line["cpu_baseline"]["gpu_parity"]["parity"]
-    # the metric's other halves: batched against plain on the batching configuration, and job latency
+    # the metric's other halves: batched against plain on the 64-sample batch workload, and job latency
     # under Poisson arrivals (rank 0 only: each is a single-GPU measurement)
     if dist.rank == 0 and not args.no_batch:
         b = batch_measure(args, dev, args.sample_scale)
@@ -550,7 +550,7 @@ def _checksum(t, n: int) -> tuple:
 
 
 def batch_measure(args, dev: int, scale: float) -> dict:
-    """The batching configuration: independent samples (read counts log-uniform 50k-5M x scale, lengths in
+    """The batch workload: independent samples (read counts log-uniform 50k-5M x scale, lengths in
     {100, 150, 250}) from pinned host FASTQ to partition files in pinned host memory, (a) plain: one after
     another through one job, every stage per sample, (b) batched: all of them through mp_batch_run.  The two
     runs' partition files are compared, and two samples' files with the CPU oracle's."""

@@ -4,7 +4,7 @@ The bucket sort (csrc/k_sort.cu) has three knobs: the bucket digits ("balanced":
 bits in passes of near-equal width; "bytes": the bucket's bytes), the unit sort's widest digit (5..9 bits;
 narrower digits mean more shared-memory passes over smaller histograms) and the digit pass's L2 prefetch
 distance (SM waves of tiles ahead; 0 = none).  This script partitions synthetic read sets of the shape of
-the large benchmark configuration at several sizes and both k of the benchmarks on the GPU, times the sort
+the 20M x 150 bp workload (plain_large) at several sizes and both k of the benchmarks on the GPU, times the sort
 stage for every combination of the knobs (best of two runs, device time from the job's own events), and
 writes the winners to sort_tuning.tsv beside this file, one row per (k, scan size class):
 

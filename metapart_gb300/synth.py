@@ -1,6 +1,6 @@
 """Seeded synthetic read sets (ctypes front end of csrc/synth.c).
 
-The named workloads restate the benchmark configurations by their shapes and
+The named workloads restate the benchmark workloads by their shapes and
 distributions; the reads themselves are generated here, never downloaded.
 """
 from __future__ import annotations

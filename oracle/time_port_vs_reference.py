@@ -26,8 +26,8 @@ BUF = 1 << 30  # fastqBufferSize: above the largest chunk (the reference allocat
 
 WORKLOADS = [
     # name, reads, k, scans
-    ("plain_small", 100_000, 27, 1),    # the first benchmark configuration at its full size
-    ("plain_large", 400_000, 31, 2),    # the large configuration's read set, the bench's CPU sample size
+    ("plain_small", 100_000, 27, 1),    # the 100k x 100 bp workload at its full size
+    ("plain_large", 400_000, 31, 2),    # the 20M x 150 bp workload's read set at the bench's CPU sample size
 ]
 
 

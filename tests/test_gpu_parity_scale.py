@@ -1,14 +1,15 @@
-"""GPU parity at the benchmark configurations' own sizes: the drop-in programs against the CPU oracle, byte
-for byte, on read sets with the shapes the numbers are quoted on.
+"""GPU parity at the benchmark workloads' own sizes: the drop-in programs against the CPU oracle, byte for byte,
+on read sets with the shapes the numbers are quoted on.
 
-  C1  100k single-end 100 bp reads from 20 genomes of 50 kb, k = 27, one scan (the full configuration),
+  100k x 100 bp: single-end reads from 20 genomes of 50 kb, k = 27, one scan (the whole small workload),
       16 threads / 64 chunks and 8 threads / 16 chunks; every stage dump is compared.
-  C2  the 20M-read configuration's read set (200 genomes of 1-5 Mb, log-normal abundance, 1 % errors, N at
-      1e-4) at 400k reads with every stage dump, and at 2M reads with the per-read dumps (BAD flags, parents
-      and sizes after every scan and the mate union) and the partition files; k = 31, 2 scans, 16 threads.
-  C3  the 3-minimizer configuration at its full 5M reads of 250 bp (Zipf abundance, 30 % of every genome
-      from 5 kb repeats shared across genomes: giant components and long runs of equal k-mers), k = 31, one
-      scan, 16 threads; every stage dump.
+  150 bp reads of the 20M-read workload's read set (200 genomes of 1-5 Mb, log-normal abundance, 1 % errors,
+      N at 1e-4) at 400k reads with every stage dump, and at 2M reads with the per-read dumps (BAD flags,
+      parents and sizes after every scan and the mate union) and the partition files; k = 31, 2 scans,
+      16 threads.
+  5M x 250 bp, 3-minimizer variant: the whole workload (Zipf abundance, 30 % of every genome from 5 kb
+      repeats shared across genomes: giant components and long runs of equal k-mers), k = 31, one scan,
+      16 threads; every stage dump.
 
 The oracle is the C restatement of the reference that tests/test_oracle_golden.py pins to the reference's
 own outputs; it runs with every host core.
@@ -26,11 +27,11 @@ CORES = str(os.cpu_count() or 4)
 
 CASES = [
     # id, workload, reads, params, dump tuple streams
-    ("C1-t16", "plain_small", 100_000, pu.Params(k=27, chunks=64, scans=1, threads=16), True),
-    ("C1-t8", "plain_small", 100_000, pu.Params(k=27, chunks=16, scans=1, threads=8), True),
-    ("C2-400k", "plain_large", 400_000, pu.Params(k=31, chunks=64, scans=2, threads=16), True),
-    ("C2-2M", "plain_large", 2_000_000, pu.Params(k=31, chunks=64, scans=2, threads=16), False),
-    ("C3-5M", "min3", 5_000_000, pu.Params(k=31, chunks=64, scans=1, threads=16, min3=True), True),
+    ("100k-x100bp-k27-t16", "plain_small", 100_000, pu.Params(k=27, chunks=64, scans=1, threads=16), True),
+    ("100k-x100bp-k27-t8", "plain_small", 100_000, pu.Params(k=27, chunks=16, scans=1, threads=8), True),
+    ("400k-x150bp-k31-s2", "plain_large", 400_000, pu.Params(k=31, chunks=64, scans=2, threads=16), True),
+    ("2M-x150bp-k31-s2", "plain_large", 2_000_000, pu.Params(k=31, chunks=64, scans=2, threads=16), False),
+    ("5M-x250bp-min3-k31", "min3", 5_000_000, pu.Params(k=31, chunks=64, scans=1, threads=16, min3=True), True),
 ]
 
 

@@ -14,9 +14,9 @@ CASES = [
     ("plain_large", 4000, 22, pu.Params(k=31, chunks=3, scans=1, threads=3)),
     ("min3", 2000, 23, pu.Params(k=29, chunks=2, scans=1, threads=1, min3=True)),
     ("interleaved_small", 3000, 24, pu.Params(k=17, chunks=4, scans=3, threads=2, interleaved=True)),
-    # the first benchmark configuration at its full size (100k x 100 bp, k = 27, one scan)
+    # the 100k x 100 bp workload at its full size (k = 27, one scan)
     ("plain_small", 100_000, 7, pu.Params(k=27, chunks=16, scans=1, threads=8)),
-    # the 3-minimizer configuration's shape (shared repeats, Zipf abundance) at 200k reads
+    # the 5M x 250 bp 3-minimizer workload's shape (shared repeats, Zipf abundance) at 200k reads
     ("min3", 200_000, 7, pu.Params(k=31, chunks=16, scans=1, threads=8, min3=True)),
 ]
 
