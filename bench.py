@@ -65,7 +65,7 @@ def parse_args():
     ap.add_argument("--pool", type=int, default=48, help="serve: distinct synthetic requests cycled")
     ap.add_argument("--samples", type=int, default=64, help="batch: samples")
     ap.add_argument("--sample-scale", type=float, default=1.0, help="batch: read-count scale")
-    ap.add_argument("--serve-seconds", type=float, default=15.0,
+    ap.add_argument("--serve-seconds", type=float, default=18.0,
                     help="plain mode: seconds of Poisson arrivals for the line's p50/p99 (0: none)")
     ap.add_argument("--no-batch", action="store_true", help="plain mode: leave out the batched-vs-plain run")
     ap.add_argument("--store", default="kmer_cache", choices=["kmer_cache", "packed", "fastq"],
