@@ -7,8 +7,10 @@ union, the 16 work partitions and the partition-FASTQ gather.
   value  -- bases/s with the FASTQ already in HBM (the step copies it into the job and runs every stage)
   e2e    -- the same through the C ABI from pinned host memory: FASTQ upload and partition-file download
             inside the timed region
-  roofline -- the radix-sort digit passes (the dominant kernel): algorithmic bytes per pass over their
-            CUDA-event time, against the measured HBM copy bandwidth
+  roofline -- the dominant kernel, the shared-memory unit sort (k_segsort: one launch per block shape and
+            scan): algorithmic bytes (25 B per tuple read and written) over its CUDA-event time, against the
+            measured HBM copy bandwidth; it is bound by shared memory, not HBM
+  roofline_digit_pass -- the same for the bucket-digit radix passes (k_onesweep), the HBM-streaming kernel
   cpu_baseline -- the CPU oracle (the reference's algorithm restated in C/OpenMP, all host cores) on a
             bounded sample of the same read set; the GPU's partition files of that sample are compared with
             the oracle's ("parity")
@@ -39,6 +41,7 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "bases/sec partitioned (k=31) batched vs plain on 1 GB300; p50/p99 job latency"
 ROOFLINE_TRAFFIC_FILE = ROOT / "profiles" / "onesweep_traffic.json"
+UNIT_SORT_TRAFFIC_FILE = ROOT / "profiles" / "unit_sort_traffic.json"
 
 
 def parse_args():
@@ -138,10 +141,10 @@ def measured_peak():
     return 6800.0, "fallback"
 
 
-def traffic_per_tuple():
-    """DRAM bytes per tuple of one onesweep pass from the committed ncu capture (null when absent)."""
+def traffic_per_tuple(path=ROOFLINE_TRAFFIC_FILE, key="dram_bytes_per_tuple_per_pass"):
+    """DRAM bytes per tuple of one launch from a committed ncu capture (null when absent)."""
     try:
-        return float(json.loads(ROOFLINE_TRAFFIC_FILE.read_text())["dram_bytes_per_tuple_per_pass"])
+        return float(json.loads(path.read_text())[key])
     except Exception:
         return None
 
@@ -335,6 +338,13 @@ def main():
     tuples_per_launch = sort_bytes / (2 * elt) / max(sort_passes, 1)
     tpt = traffic_per_tuple()
     traffic = tpt * tuples_per_launch if tpt else None
+    # the unit sort: every tuple outside the oversized buckets, read (key, high byte, id) and written (key, id)
+    # once per scan; its time per scan covers both block shapes
+    unit_tuples = (sort_tuples - split.get("big_tuples", 0)) / args.steps / max(args.scans, 1)
+    unit_ms = split.get("unit_sort_ms", 0.0) / args.steps / max(args.scans, 1)
+    unit_bytes = unit_tuples * (elt + 12)
+    unit_achieved = (unit_bytes / 1e9) / (unit_ms / 1e3) if unit_ms > 0 else 0.0
+    utpt = traffic_per_tuple(UNIT_SORT_TRAFFIC_FILE, "dram_bytes_per_tuple")
     line = {
         "metric": METRIC,
         "value": round(value, 1),
@@ -358,12 +368,18 @@ def main():
                 "scan_pieces": e2e_pieces,
                 "phase_ms": {kk: round(v / args.steps, 2) for kk, v in phase.items()},
                 "link_gbs": link, "clocks": clk_e2e.summary()},
-        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                     "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
-                     "kernel": "k_onesweep (radix digit pass)",
-                     "bytes_per_launch": int(per_launch_bytes),
-                     "launch_ms": round(sort_ms / max(sort_passes, 1), 4),
-                     "traffic": (round(traffic) if traffic else None)},
+        "roofline": {"bound": "hbm", "achieved": round(unit_achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(unit_achieved / peak, 4), "peak_kind": peak_kind,
+                     "kernel": "k_segsort (shared-memory unit sort, per scan)",
+                     "limiter": "shared memory: the dependent gathers and scatters of its digit passes",
+                     "bytes_per_launch": int(unit_bytes), "launch_ms": round(unit_ms, 4),
+                     "traffic": (round(utpt * unit_tuples) if utpt else None)},
+        "roofline_digit_pass": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                                "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
+                                "kernel": "k_onesweep (radix digit pass)",
+                                "bytes_per_launch": int(per_launch_bytes),
+                                "launch_ms": round(sort_ms / max(sort_passes, 1), 4),
+                                "traffic": (round(traffic) if traffic else None)},
         "read_stores": stores,
         "gpu_launches": int(launches),
         "stage_ms": {kk: round(v / args.steps, 3) for kk, v in stage.items()},
