@@ -367,7 +367,7 @@ def main():
                 "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": int(out_bytes) + 8 * (1 << 20) + 8,
                 "scan_pieces": e2e_pieces,
                 "phase_ms": {kk: round(v / args.steps, 2) for kk, v in phase.items()},
-                "link_gbs": link, "clocks": clk_e2e.summary()},
+                "link_gbs": link, "host": host_placement(dev), "clocks": clk_e2e.summary()},
         "roofline": {"bound": "hbm", "achieved": round(unit_achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(unit_achieved / peak, 4), "peak_kind": peak_kind,
                      "kernel": "k_segsort (shared-memory unit sort, per scan)",
@@ -433,6 +433,37 @@ def link_bandwidth(host_in, dev_buf, host_out) -> dict:
         up = max(up, n / a.elapsed_time(b) / 1e6)
         dn = max(dn, n / b.elapsed_time(c) / 1e6)
     return {"h2d": round(up, 1), "d2h": round(dn, 1), "bytes": int(n)}
+
+
+def host_placement(dev: int) -> dict:
+    """Where the host side of the copies lives: the GPU's NUMA node (from its PCI device), the host's NUMA
+    nodes with CPUs, and the nodes this process may allocate from (for reading the e2e phases)."""
+    out = {}
+    try:
+        bus = subprocess.run(["nvidia-smi", "--query-gpu=pci.bus_id", "--format=csv,noheader", "-i", str(dev)],
+                             stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True, timeout=20).stdout.strip()
+        if bus:
+            bdf = bus.lower()[-12:] if len(bus) > 12 else bus.lower()  # 0000:xx:yy.z
+            node = Path(f"/sys/bus/pci/devices/{bdf}/numa_node")
+            if node.exists():
+                out["gpu_numa_node"] = int(node.read_text().strip())
+    except Exception:
+        pass
+    try:
+        nodes = []
+        for d in sorted(Path("/sys/devices/system/node").glob("node[0-9]*")):
+            cpus = (d / "cpulist").read_text().strip()
+            nodes.append({"node": int(d.name[4:]), "cpus": cpus or None})
+        out["numa_nodes"] = nodes
+    except Exception:
+        pass
+    try:
+        for line in Path("/proc/self/status").read_text().splitlines():
+            if line.startswith("Mems_allowed_list:"):
+                out["mems_allowed"] = line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    return out
 
 
 # ------------------------------------------------- request loop and batches
