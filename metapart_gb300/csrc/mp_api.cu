@@ -478,7 +478,7 @@ static int load_common(mp_job *j, uint64_t nbytes, const uint64_t *file_sizes, i
     j->interleaved = interleaved;
     j->stage_ms[0] = 0;
     {
-        StageTimer tm(j->st, &j->stage_ms[0]);
+        StageTimer tm(j->st, j->stage_ms, 0);
         int rc = parse_fastq(j->d_fq, nbytes, &j->pr, j->arena, j->st);
         if (rc) return rc;
     }
@@ -580,7 +580,7 @@ int mp_job_count(mp_job *j, int k, int min3, const uint64_t *chunk_starts, int n
     if (cc) MP_CUDA(cudaMemsetAsync(cc, 0, (size_t)nchunks * NB * 4, j->st));
     drop_kmer_cache(j);
     {
-        StageTimer tm(j->st, &j->stage_ms[1]);
+        StageTimer tm(j->st, j->stage_ms, 1);
         const bool kc = j->store != STORE_FASTQ && !min3 && make_kmer_cache(j, k);
         const KcPiece q = kc ? j->kc[0] : KcPiece{};
         launch_count(j->d_fq, j->pr, k, min3, d_rec, nchunks, cc, glob, err, j->st, q.off, q.lo, q.hi, q.poff, q.pw, q.pn);
@@ -663,11 +663,11 @@ int load_count_pipelined(mp_job *j, const char *bytes, uint64_t nbytes, const ui
     for (int i = 0; i < S; i++) {
         MP_CUDA(cudaStreamWaitEvent(j->st, ev[i], 0));
         {
-            StageTimer tm(j->st, &j->stage_ms[0]);
+            StageTimer tm(j->st, j->stage_ms, 0);
             if (parse_fastq_range(j->d_fq, seg[i], seg[i + 1], &prs[i], j->arena, j->st)) return MP_EFMT;
         }
         R[i + 1] = R[i] + prs[i].n_reads;
-        StageTimer tm(j->st, &j->stage_ms[1]);
+        StageTimer tm(j->st, j->stage_ms, 1);
         KcPiece q;
         const bool made = j->store == STORE_PACKED ? make_pk_piece(j->arena, j->st, prs[i], R[i], k, &q)
                                                    : make_kc_piece(j->arena, j->st, prs[i], R[i], k, &q);
@@ -680,7 +680,7 @@ int load_count_pipelined(mp_job *j, const char *bytes, uint64_t nbytes, const ui
     const uint64_t N = R[S];
     if (N >= UMAX32 || (interleaved && (N & 1))) return MP_EFMT;
     {
-        StageTimer tm(j->st, &j->stage_ms[0]);
+        StageTimer tm(j->st, j->stage_ms, 0);
         j->pr.n_reads = N;
         j->pr.rec_start = j->arena.alloc_persistent<uint64_t>(N + 1);
         j->pr.seq_off = j->arena.alloc_persistent<uint64_t>(N + 1);
@@ -865,7 +865,7 @@ static int scan_in_pieces(mp_job *j, int s, int k, bool has_hi, uint64_t lo, uin
         SortBufs sb = sb0;
         uint64_t n = 0;
         {
-            StageTimer tm(j->st, &j->stage_ms[2]);
+            StageTimer tm(j->st, j->stage_ms, 2);
             int lrc = 0;
             if (use_kc)
                 for (const KcPiece &q : j->kc) lrc |= store_count_scans(q, j->pr.seq_len, k, d_b + 2 * i, 1, cnt, N + 1, err, j->st);
@@ -893,7 +893,7 @@ static int scan_in_pieces(mp_job *j, int s, int k, bool has_hi, uint64_t lo, uin
         if (herr) return set_error(MP_EDEVICE, "enumeration flags 0x%x", herr);
         int lo_buf = 0, hi_buf = 0;
         {
-            StageTimer tm(j->st, &j->stage_ms[3]);
+            StageTimer tm(j->st, j->stage_ms, 3);
             SortStats ss;
             int r = bucket_sort(sb, n, has_hi, k, d_hist, b0, b1, j->arena, j->st, &ss, &lo_buf, &hi_buf);
             if (r) return r;
@@ -921,7 +921,7 @@ static int scan_in_pieces(mp_job *j, int s, int k, bool has_hi, uint64_t lo, uin
         for (int t = 1; t <= T; t++)
             if (rb[t] > p0 && rb[t] <= p1) ends.push_back(rb[t] - p0);
         {
-            StageTimer tm(j->st, &j->stage_ms[4]);
+            StageTimer tm(j->st, j->stage_ms, 4);
             if ((rc = filter_scan(tp, ends, j->d_parent, j->d_filtered, j->arena, j->st, !j->dump_dir.empty()))) return rc;
         }
         zs[i] = tp.z;
@@ -979,7 +979,7 @@ static int scan_in_pieces(mp_job *j, int s, int k, bool has_hi, uint64_t lo, uin
         std::vector<uint8_t> part_seen(which.size()), has_valid;
         for (size_t q = 0; q < which.size(); q++) part_seen[q] = seen[which[q]];
         {
-            StageTimer tm(j->st, &j->stage_ms[5]);
+            StageTimer tm(j->st, j->stage_ms, 5);
             if ((rc = union_piece(tp, bounds, part_seen, last_kmer, first_id, first_parent != BAD, j->d_parent,
                                   j->d_filtered, j->arena, j->st, has_valid, anchor)))
                 return rc;
@@ -987,7 +987,7 @@ static int scan_in_pieces(mp_job *j, int s, int k, bool has_hi, uint64_t lo, uin
         for (size_t q = 0; q < which.size(); q++) seen[which[q]] |= has_valid[q];
     }
     {
-        StageTimer tm(j->st, &j->stage_ms[5]);
+        StageTimer tm(j->st, j->stage_ms, 5);
         if (have_first && first_parent == BAD) hook_bad_anchor(j->d_parent, first_id, anchor, anchor + 1, j->st);
         compress_parents(j->d_parent, N, j->st);
         MP_CUDA(cudaMemcpyAsync(&j->hooked_bad, anchor + 1, 4, cudaMemcpyDeviceToHost, j->st));
@@ -1073,7 +1073,7 @@ int mp_job_partition(mp_job *j, const mp_part_params *p, const uint64_t *chunk_s
             d_b = j->arena.alloc_persistent<uint32_t>(S + 1);
             if (!cnt_all || !d_b) return set_error(MP_ENOMEM, "device memory for enumeration counts");
             std::vector<uint32_t> hb(scanR.begin(), scanR.end());
-            StageTimer tm(j->st, &j->stage_ms[2]);
+            StageTimer tm(j->st, j->stage_ms, 2);
             MP_CUDA(cudaMemcpyAsync(d_b, hb.data(), (S + 1) * 4, cudaMemcpyHostToDevice, j->st));
             int lrc = 0;
             if (use_kc)
@@ -1125,7 +1125,7 @@ int mp_job_partition(mp_job *j, const mp_part_params *p, const uint64_t *chunk_s
         int lo_buf = 0, hi_buf = 0;
         uint64_t n = 0;
         {
-            StageTimer tm(j->st, &j->stage_ms[2]);
+            StageTimer tm(j->st, j->stage_ms, 2);
             if (!cnt_all) {
                 launch_enum_count(j->d_fq, j->pr, k, p->min3, (uint32_t)lo, (uint32_t)hi, cnt, err, j->st);
                 MP_CUDA(cudaMemsetAsync(cnt + N, 0, 4, j->st));
@@ -1168,7 +1168,7 @@ int mp_job_partition(mp_job *j, const mp_part_params *p, const uint64_t *chunk_s
         snprintf(name, sizeof name, "scan%d_enum.bin", s);
         if ((rc = dump_tuples(j, name, sb.lo[0], sb.hi[0], sb.id[0], n))) return rc;
         {
-            StageTimer tm(j->st, &j->stage_ms[3]);
+            StageTimer tm(j->st, j->stage_ms, 3);
             SortStats ss;
             if ((rc = bucket_sort(sb, n, has_hi, k, d_hist, lo, hi, j->arena, j->st, &ss, &lo_buf, &hi_buf))) return rc;
             add_sort_stats(j, ss, n);
@@ -1183,7 +1183,7 @@ int mp_job_partition(mp_job *j, const mp_part_params *p, const uint64_t *chunk_s
         std::vector<uint64_t> rb;
         if ((rc = range_bounds(hist, thrR.data() + (size_t)s * T, T, lo, hi, rb))) return rc;
         {
-            StageTimer tm(j->st, &j->stage_ms[4]);
+            StageTimer tm(j->st, j->stage_ms, 4);
             if ((rc = filter_scan(tp, rb, j->d_parent, j->d_filtered, j->arena, j->st, !j->dump_dir.empty()))) return rc;
         }
         snprintf(name, sizeof name, "scan%d_filtered.bin", s);
@@ -1197,7 +1197,7 @@ int mp_job_partition(mp_job *j, const mp_part_params *p, const uint64_t *chunk_s
             if (rc) return rc;
         }
         {
-            StageTimer tm(j->st, &j->stage_ms[5]);
+            StageTimer tm(j->st, j->stage_ms, 5);
             if ((rc = union_scan(tp, rb, j->d_parent, j->d_filtered, N, j->arena, j->st, j->hooked_bad, &j->hooked_bad)))
                 return rc;
         }
@@ -1210,7 +1210,7 @@ int mp_job_partition(mp_job *j, const mp_part_params *p, const uint64_t *chunk_s
     j->arena.free_persistent(d_hist);
     drop_kmer_cache(j);  // its HBM goes back before the mate union and the output
     {
-        StageTimer tm(j->st, &j->stage_ms[6]);
+        StageTimer tm(j->st, j->stage_ms, 6);
         if (!j->dump_dir.empty()) {
             MP_CUDA(cudaMemsetAsync(j->d_size, 0, N * 4, j->st));
             (mp::count_launch(), k_sizes_raw<<<gN, 256, 0, j->st>>>(j->d_parent, N, j->d_size));
@@ -1243,7 +1243,7 @@ namespace {
 int plan_job_output(mp_job *j)
 {
     if (j->output_ready) return 0;
-    StageTimer tm(j->st, &j->stage_ms[7]);
+    StageTimer tm(j->st, j->stage_ms, 7);
     j->stage_ms[7] = 0;
     int rc = plan_output(j->d_fq, j->pr, j->d_parent, j->bounds, j->chunk_rec.data(), j->nchunks, j->T, j->interleaved,
                          &j->out_plan, j->out_sizes, j->arena, j->st);
@@ -1258,7 +1258,7 @@ int plan_job_output(mp_job *j)
 int materialize_output(mp_job *j)
 {
     if (j->d_out) return 0;
-    StageTimer tm(j->st, &j->stage_ms[7]);
+    StageTimer tm(j->st, j->stage_ms, 7);
     j->d_out = j->arena.alloc_persistent<uint8_t>(j->out_total + 16);
     if (!j->d_out) return set_error(MP_ENOMEM, "device memory for the output bytes");
     return copy_output(j->out_plan, j->d_fq, j->d_out, j->st);
@@ -1293,7 +1293,7 @@ int materialize_and_download(mp_job *j, uint8_t *out)
     for (auto &x : ev) cudaEventCreateWithFlags(&x, cudaEventDisableTiming);
     int rc = 0;
     {
-        StageTimer tm(j->st, &j->stage_ms[7]);
+        StageTimer tm(j->st, j->stage_ms, 7);
         for (int b = 0; b < K && !rc; b++) {
             rc = copy_output_range(pl, e[b], e[b + 1], j->d_fq, j->d_out, j->st);
             cudaEventRecord(ev[b], j->st);

@@ -243,7 +243,7 @@ static int run_group(mp_batch *b, const mp_batch_params *p, const mp_batch_sampl
         const uint64_t b0 = g[qa].byte0, b1 = g[qb - 1].byte0 + smp[g[qb - 1].idx].nbytes;
         MP_CUDA(cudaStreamWaitEvent(st, ev[u], 0));
         {
-            StageTimer tm(st, &b->stage_ms[0]);
+            StageTimer tm(st, b->stage_ms, 0);
             rc = parse_fastq_range(d_fq, b0, b1, &prs[u], A, st);
         }
         if (rc) {  // name the sample: parse the segment's samples one by one until one fails
@@ -284,7 +284,7 @@ static int run_group(mp_batch *b, const mp_batch_params *p, const mp_batch_sampl
         }
         if (rc) return rc;
         RU[u + 1] = R[qb];
-        StageTimer tm(st, &b->stage_ms[1]);
+        StageTimer tm(st, b->stage_ms, 1);
         if (!make_kc_piece(A, st, prs[u], RU[u], k, &kc[u]))
             return set_error(MP_ENOMEM, "device memory for the k-mer cache of samples %d..%d", g[qa].idx, g[qb - 1].idx);
         std::vector<uint64_t> loc(qb - qa + 1);
@@ -299,7 +299,7 @@ static int run_group(mp_batch *b, const mp_batch_params *p, const mp_batch_sampl
     // ---- one read table for the group, global read ids
     ParsedReads pr;
     {
-        StageTimer tm(st, &b->stage_ms[0]);
+        StageTimer tm(st, b->stage_ms, 0);
         pr.n_reads = N;
         pr.rec_start = A.alloc_persistent<uint64_t>(N + 1);
         pr.seq_off = A.alloc_persistent<uint64_t>(N + 1);
@@ -330,7 +330,7 @@ static int run_group(mp_batch *b, const mp_batch_params *p, const mp_batch_sampl
     std::vector<int> hstat(nseg);
     uint32_t herr = 0;
     {
-        StageTimer tm(st, &b->stage_ms[1]);
+        StageTimer tm(st, b->stage_ms, 1);
         scan_u32_to_u64(cc, shist, (size_t)nseg * NB, shist + (size_t)nseg * NB, tmph, tbh, st);
         MP_CUDA(cudaMemcpyAsync(dT, hT.data(), nseg * 4, cudaMemcpyHostToDevice, st));
         MP_CUDA(cudaMemcpyAsync(drb0, hrb0.data(), (nseg + 1) * 4, cudaMemcpyHostToDevice, st));
@@ -358,7 +358,7 @@ static int run_group(mp_batch *b, const mp_batch_params *p, const mp_batch_sampl
     // ---- enumeration: every k-mer of every read (one scan per sample), read order
     SortBufs sb;
     {
-        StageTimer tm(st, &b->stage_ms[2]);
+        StageTimer tm(st, b->stage_ms, 2);
         uint32_t *cnt = A.alloc<uint32_t>(N + 1), *d_b = A.alloc<uint32_t>(2);
         uint64_t *off = A.alloc<uint64_t>(N + 2), *ntot = A.alloc<uint64_t>(1);
         const size_t tb = scan_tmp_bytes(N + 1);
@@ -397,7 +397,7 @@ static int run_group(mp_batch *b, const mp_batch_params *p, const mp_batch_sampl
     // ---- sort: every sample's tuples by (k-mer, adjacency), within the sample's range
     int lo_buf = 0, hi_buf = 0;
     {
-        StageTimer tm(st, &b->stage_ms[3]);
+        StageTimer tm(st, b->stage_ms, 3);
         SortStats ss;
         if ((rc = bucket_sort(sb, T_all, has_hi, k, shist, 0, (uint64_t)nseg * NB, A, st, &ss, &lo_buf, &hi_buf, &segs)))
             return rc;
@@ -423,14 +423,14 @@ static int run_group(mp_batch *b, const mp_batch_params *p, const mp_batch_sampl
     launch_init_parent(parent, N, st);
     MP_CUDA(cudaMemsetAsync(filtered, 0, N + 1, st));
     {
-        StageTimer tm(st, &b->stage_ms[4]);
+        StageTimer tm(st, b->stage_ms, 4);
         if ((rc = filter_scan(tp, rb, parent, filtered, A, st, false, true))) return rc;
     }
     {
         std::vector<uint32_t> rseg(Rn);
         for (int q = 0; q < nseg; q++)
             for (uint32_t t = hrb0[q]; t < hrb0[q + 1]; t++) rseg[t] = (uint32_t)q;
-        StageTimer tm(st, &b->stage_ms[5]);
+        StageTimer tm(st, b->stage_ms, 5);
         if ((rc = union_segments(tp, rb, rseg, segs.tstart, parent, filtered, N, A, st))) return rc;
     }
     A.release_scratch();
@@ -441,7 +441,7 @@ static int run_group(mp_batch *b, const mp_batch_params *p, const mp_batch_sampl
     // ---- mate union and every sample's partitions
     std::vector<uint64_t> bounds((size_t)nseg * 17);
     {
-        StageTimer tm(st, &b->stage_ms[6]);
+        StageTimer tm(st, b->stage_ms, 6);
         int rounds = 0;
         if ((rc = mate_union(parent, N, size, A, st, &rounds))) return rc;
         if ((rc = plan_partitions_segments(parent, size, N, R, bounds.data(), A, st))) return rc;
@@ -458,7 +458,7 @@ static int run_group(mp_batch *b, const mp_batch_params *p, const mp_batch_sampl
         Ts[q] = smp[g[q].idx].num_threads;
     }
     {
-        StageTimer tm(st, &b->stage_ms[7]);
+        StageTimer tm(st, b->stage_ms, 7);
         if ((rc = plan_output_batch(pr, parent, il, R, bounds, crec, Ts, &plan, fsz, file0, A, st))) return rc;
         A.release_scratch();
     }
@@ -496,7 +496,7 @@ static int run_group(mp_batch *b, const mp_batch_params *p, const mp_batch_sampl
     pending.out = d_out;
     {
         constexpr int KB = 8;
-        StageTimer tm(st, &b->stage_ms[7]);
+        StageTimer tm(st, b->stage_ms, 7);
         uint64_t e[KB + 1], o[KB + 1];
         for (int x = 0; x <= KB; x++) e[x] = plan.n * (uint64_t)x / KB;
         for (int x = 0; x < KB; x++)

@@ -1,5 +1,6 @@
 // Host-side pieces shared by the job driver (mp_api.cu) and the batch driver (mp_batch.cu).
 #pragma once
+#include <nvtx3/nvToolsExt.h>
 #include "k_reads.cuh"
 
 namespace mp {
@@ -41,12 +42,19 @@ void ctx_budget(mp_ctx *ctx, std::atomic<uint64_t> **used, uint64_t *limit);
 void launch_init_parent(uint32_t *parent, uint64_t n, cudaStream_t st);
 
 // Device time of the work queued on a stream while the timer lives, added to *slot (ms).
+// The stages of a job or batch, in the order of their time slots (mp_job_stage_ms, mp_batch_stage_ms).
+constexpr const char *STAGE_NAMES[8] = {"parse", "count", "enumerate", "sort", "filter", "union_find",
+                                        "mate_union_plan", "output"};
+
+// A stage's device time (CUDA events on its stream, added to its slot) and an NVTX range of the stage's
+// name for a profiler's timeline (a no-op without one attached).
 struct StageTimer {
     cudaEvent_t a, b;
     cudaStream_t st;
     double *acc;
-    StageTimer(cudaStream_t s, double *slot) : st(s), acc(slot)
+    StageTimer(cudaStream_t s, double *slots, int stage) : st(s), acc(slots + stage)
     {
+        nvtxRangePushA(STAGE_NAMES[stage]);
         cudaEventCreate(&a);
         cudaEventCreate(&b);
         cudaEventRecord(a, st);
@@ -60,6 +68,7 @@ struct StageTimer {
         *acc += ms;
         cudaEventDestroy(a);
         cudaEventDestroy(b);
+        nvtxRangePop();
     }
     StageTimer(const StageTimer &) = delete;
     StageTimer &operator=(const StageTimer &) = delete;
