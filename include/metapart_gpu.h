@@ -310,6 +310,16 @@ int mp_job_set_scan_piece_tuples(mp_job *job, uint64_t max_tuples);
  * metapart.c:2736-2800); these limits have no counterpart there. */
 int mp_job_set_wait_limits(mp_job *job, uint32_t lookback_spins, uint32_t union_retries, uint32_t mate_rounds);
 
+/* Self-checks of the job's intermediate results (off by default; the environment variable MP_CHECK=1
+ * turns them on for every job): after every scan's sort (or every piece's), that no adjacent tuple pair is
+ * out of (k-mer, adjacency) order; after the mate union, that every read's parent is a root or BAD.  A
+ * failed check makes mp_job_partition return MP_EDEVICE naming it.  The reference checks neither. */
+int mp_job_set_checks(mp_job *job, int on);
+
+/* Adjacent pairs out of (k-mer, adjacency) order in a device tuple array (lo and hi as mp_sort_tuples;
+ * hi NULL when 2k + 8 <= 64) into *out: 0 for a sorted array.  Returns after the count on `stream`. */
+int mp_count_unsorted(mp_ctx *ctx, const uint64_t *lo, const uint8_t *hi, uint64_t n, void *stream, uint64_t *out);
+
 /* Bucket-range pieces the last mp_job_partition ran its scans in, summed over the scans (numScans when
  * no scan was split).  Tracing only. */
 int mp_job_scan_pieces(const mp_job *job);

@@ -895,6 +895,34 @@ int union_piece(Tuples &tp, const std::vector<uint64_t> &bounds, const std::vect
     return 0;
 }
 
+// Reads whose parent is neither BAD nor a root (its own parent): none after a compression.
+__global__ void k_count_nonroot(const uint32_t *parent, uint64_t n, unsigned long long *out)
+{
+    unsigned long long c = 0;
+    for (uint64_t x = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; x < n; x += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t p = parent[x];
+        c += (p != BAD && (p >= n || parent[p] != p)) ? 1u : 0u;
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) c += __shfl_xor_sync(FULLW, c, o);
+    if ((threadIdx.x & 31) == 0 && c) atomicAdd(out, c);
+}
+
+int count_nonroot(const uint32_t *parent, uint64_t n, unsigned long long *d_count, cudaStream_t st, uint64_t *out)
+{
+    MP_CUDA(cudaMemsetAsync(d_count, 0, sizeof(unsigned long long), st));
+    if (n) {
+        const uint64_t blocks = std::min<uint64_t>((n + 255) / 256, 8ull * (uint64_t)sm_count());
+        (mp::count_launch(), k_count_nonroot<<<(unsigned)blocks, 256, 0, st>>>(parent, n, d_count));
+    }
+    unsigned long long h = 0;
+    MP_CUDA(cudaMemcpyAsync(&h, d_count, sizeof h, cudaMemcpyDeviceToHost, st));
+    MP_CUDA(cudaStreamSynchronize(st));
+    MP_CUDA(cudaGetLastError());
+    *out = h;
+    return 0;
+}
+
 void rebad_read(uint32_t *parent, uint32_t r, cudaStream_t st)
 {
     if (r != ~0u) (mp::count_launch(), k_rebad<<<1, 1, 0, st>>>(parent, r));

@@ -36,6 +36,8 @@ int union_piece(Tuples &tp, const std::vector<uint64_t> &bounds, const std::vect
                 uint32_t init_min, bool init_min_ok, uint32_t *parent, const uint8_t *filtered, DeviceArena &arena,
                 cudaStream_t st, std::vector<uint8_t> &has_valid, uint32_t *anchor_v);
 void rebad_read(uint32_t *parent, uint32_t r, cudaStream_t st);
+// Reads whose parent is neither BAD nor a root, counted on st into *out (d_count: one device word).
+int count_nonroot(const uint32_t *parent, uint64_t n, unsigned long long *d_count, cudaStream_t st, uint64_t *out);
 void hook_bad_anchor(uint32_t *parent, uint32_t b, const uint32_t *anchor_v, uint32_t *hooked, cudaStream_t st);
 void compress_parents(uint32_t *parent, uint64_t n_reads, cudaStream_t st);
 // K6: sizes, unionFindPeReads(1000), final compression and the 17 partition bounds (host).

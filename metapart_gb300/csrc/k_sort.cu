@@ -330,6 +330,35 @@ __global__ void __launch_bounds__(ST, 3) k_onesweep(const uint64_t *__restrict__
     }
 }
 
+// Adjacent pairs out of (k-mer, adjacency) order: (hi, lo) compared as one 72-bit key.
+__global__ void k_count_unsorted(const uint64_t *lo, const uint8_t *hi, uint64_t n, unsigned long long *out)
+{
+    unsigned long long c = 0;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x + 1; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t ha = hi ? hi[i - 1] : 0u, hb = hi ? hi[i] : 0u;
+        c += (ha > hb || (ha == hb && lo[i - 1] > lo[i])) ? 1u : 0u;
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) c += __shfl_xor_sync(FULLM, c, o);
+    if ((threadIdx.x & 31) == 0 && c) atomicAdd(out, c);
+}
+
+int count_unsorted(const uint64_t *lo, const uint8_t *hi, uint64_t n, unsigned long long *d_count, cudaStream_t st,
+                   uint64_t *out)
+{
+    MP_CUDA(cudaMemsetAsync(d_count, 0, sizeof(unsigned long long), st));
+    if (n > 1) {
+        const uint64_t blocks = std::min<uint64_t>((n + 255) / 256, 8ull * (uint64_t)sm_count());
+        (mp::count_launch(), k_count_unsorted<<<(unsigned)blocks, 256, 0, st>>>(lo, hi, n, d_count));
+    }
+    unsigned long long h = 0;
+    MP_CUDA(cudaMemcpyAsync(&h, d_count, sizeof h, cudaMemcpyDeviceToHost, st));
+    MP_CUDA(cudaStreamSynchronize(st));
+    MP_CUDA(cudaGetLastError());
+    *out = h;
+    return 0;
+}
+
 int radix_sort(SortBufs &b, uint64_t n, bool has_hi, DeviceArena &arena, cudaStream_t st, SortStats *stats)
 {
     if (stats) *stats = SortStats{};

@@ -30,6 +30,11 @@ struct SortStats {
                                    //   status words read and polls of unposted words, summed over tiles
 };
 
+// Adjacent tuple pairs of lo/hi (hi nullable) out of (k-mer, adjacency) order, counted on st into *out
+// (d_count: one device word of scratch).
+int count_unsorted(const uint64_t *lo, const uint8_t *hi, uint64_t n, unsigned long long *d_count, cudaStream_t st,
+                   uint64_t *out);
+
 // Stable sort of b[cur][0, n) by (hi, lo); on return b.cur names the sorted buffer.
 int radix_sort(SortBufs &b, uint64_t n, bool has_hi, DeviceArena &arena, cudaStream_t st, SortStats *stats);
 

@@ -231,6 +231,7 @@ struct mp_job {
     uint64_t piece_tuples = 0;  // most tuples a scan holds in HBM at once (0: from the free device memory)
     int pieces_total = 0;       // bucket-range pieces of the last partition, over all scans
     uint32_t hooked_bad = ~0u;  // a flagged read the last scan's unions hooked below a component (next scan: BAD)
+    bool checks = false;        // self-checks of the sorted tuples and the final forest (mp_job_set_checks)
 };
 
 // ------------------------------------------------------------------ helpers
@@ -454,6 +455,8 @@ int mp_job_create(mp_ctx *ctx, mp_job **out)
     j->arena.st = j->st;
     j->arena.budget_used = &ctx->used;
     j->arena.budget_limit = ctx->budget;
+    const char *ck = getenv("MP_CHECK");
+    j->checks = ck && *ck && *ck != '0';
     *out = j;
     return 0;
 }
@@ -825,6 +828,22 @@ static std::vector<uint64_t> plan_pieces(const uint64_t *hist, uint64_t lo, uint
 // taken before the first sweep.  A thread range's last run is exempt from the filter only where the range
 // ends, and each range's sweep starts from the scan's own initial state (metapart.c:2539-2548), however
 // the pieces cut it.
+// The sort self-check (mp_job_set_checks): no adjacent tuple pair out of (k-mer, adjacency) order.
+static int check_sorted(mp_job *j, const uint64_t *lo, const uint8_t *hi, uint64_t n, int scan)
+{
+    if (!j->checks) return 0;
+    unsigned long long *dc = j->arena.alloc<unsigned long long>(1);
+    if (!dc) return set_error(MP_ENOMEM, "device memory");
+    uint64_t bad = 0;
+    int rc = count_unsorted(lo, hi, n, dc, j->st, &bad);
+    j->arena.free_scratch(dc);
+    if (rc) return rc;
+    if (bad)
+        return set_error(MP_EDEVICE, "check: scan %d's sorted tuples hold %llu adjacent pairs out of order", scan,
+                         (unsigned long long)bad);
+    return 0;
+}
+
 static int scan_in_pieces(mp_job *j, int s, int k, bool has_hi, uint64_t lo, uint64_t hi, const std::vector<uint64_t> &pcs,
                           const std::vector<uint64_t> &rb, const uint64_t *hist, const uint64_t *d_hist, bool use_kc,
                           uint32_t *err)
@@ -915,6 +934,7 @@ static int scan_in_pieces(mp_job *j, int s, int k, bool has_hi, uint64_t lo, uin
         Tuples tp;
         if ((rc = piece_tuples(i, tp))) return rc;
         const uint64_t p0 = hist[pcs[i]] - scan0, p1 = hist[pcs[i + 1]] - scan0;
+        if ((rc = check_sorted(j, tp.lo, tp.hi, tp.n, s))) return rc;
         snprintf(name, sizeof name, "scan%d_sorted.bin", s);
         if ((rc = dump_tuples(j, name, tp.lo, tp.hi, tp.id, tp.n, i > 0))) return rc;
         std::vector<uint64_t> ends{0};  // the thread ranges ending inside the piece or at its end
@@ -1178,6 +1198,7 @@ int mp_job_partition(mp_job *j, const mp_part_params *p, const uint64_t *chunk_s
         tp.hi = has_hi ? sb.hi[hi_buf] : nullptr;
         tp.id = sb.id[lo_buf];
         tp.n = n;
+        if ((rc = check_sorted(j, tp.lo, tp.hi, n, s))) return rc;
         snprintf(name, sizeof name, "scan%d_sorted.bin", s);
         if ((rc = dump_tuples(j, name, tp.lo, tp.hi, tp.id, n))) return rc;
         std::vector<uint64_t> rb;
@@ -1219,6 +1240,14 @@ int mp_job_partition(mp_job *j, const mp_part_params *p, const uint64_t *chunk_s
             if ((rc = dump_state(j, name, name2))) return rc;
         }
         if ((rc = mate_union_and_plan(j->d_parent, N, j->d_size, j->bounds, j->arena, j->st, &j->pe_rounds))) return rc;
+    }
+    if (j->checks) {  // every read's parent a root (or BAD) after the final compression
+        unsigned long long *dc = j->arena.alloc<unsigned long long>(1);
+        uint64_t bad = 0;
+        if (!dc) return set_error(MP_ENOMEM, "device memory");
+        if ((rc = count_nonroot(j->d_parent, N, dc, j->st, &bad))) return rc;
+        if (bad) return set_error(MP_EDEVICE, "check: %llu reads' parents are not roots after the mate union",
+                                  (unsigned long long)bad);
     }
     j->arena.release_scratch();
     snprintf(name, sizeof name, "stats%d_parent.bin", S + 1);
@@ -1381,6 +1410,29 @@ int mp_job_set_wait_limits(mp_job *j, uint32_t lookback_spins, uint32_t union_re
     j->arena.lim.union_retries = union_retries ? union_retries : d.union_retries;
     j->arena.lim.mate_rounds = mate_rounds ? mate_rounds : d.mate_rounds;
     return 0;
+}
+
+int mp_job_set_checks(mp_job *j, int on)
+{
+    if (!j) return set_error(MP_EARG, "null job");
+    j->checks = on != 0;
+    return 0;
+}
+
+int mp_count_unsorted(mp_ctx *ctx, const uint64_t *lo, const uint8_t *hi, uint64_t n, void *stream, uint64_t *out)
+{
+    if (!ctx || !out || (n && !lo)) return set_error(MP_EARG, "null argument");
+    MP_CUDA(cudaSetDevice(ctx->device));
+    cudaStream_t st = (cudaStream_t)stream;
+    DeviceArena arena;
+    arena.st = st;
+    arena.budget_used = &ctx->used;
+    arena.budget_limit = ctx->budget;
+    unsigned long long *dc = arena.alloc<unsigned long long>(1);
+    if (!dc) return set_error(MP_ENOMEM, "device memory");
+    const int rc = count_unsorted(lo, hi, n, dc, st, out);
+    arena.release_all();
+    return rc;
 }
 
 int mp_job_set_scan_piece_tuples(mp_job *j, uint64_t max_tuples)

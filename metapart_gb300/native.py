@@ -65,6 +65,9 @@ def lib():
         L.mp_job_set_read_store.argtypes = [C.c_void_p, C.c_int]
         L.mp_job_read_store.argtypes = [C.c_void_p]
         L.mp_job_set_wait_limits.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32]
+        L.mp_job_set_checks.argtypes = [C.c_void_p, C.c_int]
+        L.mp_count_unsorted.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p,
+                                        C.POINTER(C.c_uint64)]
         L.mp_batch_set_wait_limits.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32]
         L.mp_job_scan_pieces.argtypes = [C.c_void_p]
         L.mp_job_stage_ms.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.c_int]
@@ -235,6 +238,10 @@ class Job:
         bucket-range pieces with the same results."""
         _check(lib().mp_job_set_scan_piece_tuples(self.h, int(max_tuples)), "set_scan_piece_tuples")
 
+    def set_checks(self, on: bool = True):
+        """Self-checks of the sorted tuples and the final forest (mp_job_set_checks)."""
+        _check(lib().mp_job_set_checks(self.h, int(bool(on))), "set_checks")
+
     def set_wait_limits(self, lookback_spins: int = 0, union_retries: int = 0, mate_rounds: int = 0):
         """Iteration limits of the bounded device waits (0: the default)."""
         _check(lib().mp_job_set_wait_limits(self.h, lookback_spins, union_retries, mate_rounds), "set_wait_limits")
@@ -345,6 +352,14 @@ def sort_tuples(ctx: Context, lo_in: int, hi_in: int | None, id_in: int, lo_out:
     """mp_sort_tuples on device addresses (e.g. torch tensors' data_ptr())."""
     _check(lib().mp_sort_tuples(ctx.h, lo_in, hi_in, id_in, lo_out, hi_out, id_out, n, stream or None),
            "mp_sort_tuples")
+
+
+def count_unsorted(ctx: Context, lo: int, hi: int | None, n: int, stream: int = 0) -> int:
+    """mp_count_unsorted on device addresses: adjacent tuple pairs out of (k-mer, adjacency) order."""
+    out = C.c_uint64(0)
+    _check(lib().mp_count_unsorted(ctx.h, C.c_void_p(lo), C.c_void_p(hi) if hi else None, C.c_uint64(n),
+                                   C.c_void_p(stream) if stream else None, C.byref(out)), "mp_count_unsorted")
+    return int(out.value)
 
 
 def launch_count() -> int:
