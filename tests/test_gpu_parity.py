@@ -26,6 +26,10 @@ CASES = [
     ("plain_small", 20000, pu.Params(k=13, chunks=4, scans=1, threads=4)),
     ("interleaved_small", 20000, pu.Params(k=27, chunks=4, scans=1, threads=2, interleaved=True)),
     ("interleaved_small", 20000, pu.Params(k=25, chunks=8, scans=2, threads=2, interleaved=True)),
+    # many thread ranges over few reads: empty ranges, ranges of one bucket, 256 threads (the most)
+    ("plain_small", 3000, pu.Params(k=27, chunks=64, scans=1, threads=64, buffer=1 << 24)),
+    ("plain_large", 6000, pu.Params(k=31, chunks=128, scans=2, threads=128, buffer=1 << 24)),
+    ("plain_small", 4000, pu.Params(k=23, chunks=256, scans=3, threads=256, buffer=1 << 24)),
 ]
 
 # The oracle also writes the compSizes array after every scan; the reference accumulates it without
@@ -76,8 +80,8 @@ def test_gpu_unit_sort_digit_width(tmp_path, built_gpu, name, n, p, bits):
     _compare(tmp_path, name, n, p, env_extra={"MP_UNIT_SORT_MAX_BITS": str(bits)})
 
 
-# The bucket's bytes as digits (three passes for a scan over half the bucket range) instead of the wide
-# passes of up to 10 bits that the sort takes by default.
+# The bucket's bytes as digits (three passes for a scan over half the bucket range) instead of the passes of
+# near-equal widths of at most 8 bits that the sort takes by default.
 @pytest.mark.parametrize("name,n,p", NARROW + [CASES[2], CASES[10]],
                          ids=[f"{c[0]}-k{c[2].k}-s{c[2].scans}" for c in NARROW + [CASES[2], CASES[10]]])
 def test_gpu_byte_bucket_digits(tmp_path, built_gpu, name, n, p):
@@ -100,3 +104,26 @@ PIECES = [
 def test_gpu_scan_in_pieces(tmp_path, built_gpu, name, n, p, cap):
     _compare(tmp_path, name, n, p, env_extra={"MP_SCAN_PIECE_TUPLES": str(cap)},
              skip={f"dump/scan{s}_enum.bin" for s in range(p.scans)})
+
+
+# Two input files of one sample (numSE = 2, or numInterleaved = 2): reads numbered across the files, the
+# index and histogram named after the first file, every partition file holding records of both.
+TWO_FILES = [
+    ("plain_small", "plain_large", 6000, 4000, pu.Params(k=27, chunks=8, scans=2, threads=4)),
+    ("plain_small", "plain_large", 5000, 3000, pu.Params(k=31, chunks=6, scans=1, threads=3)),
+    ("interleaved_small", "interleaved_small", 4000, 6000, pu.Params(k=25, chunks=4, scans=1, threads=2,
+                                                                      interleaved=True)),
+]
+
+
+@pytest.mark.parametrize("w1,w2,n1,n2,p", TWO_FILES, ids=[f"{c[0]}+{c[1]}-k{c[4].k}-s{c[4].scans}" for c in TWO_FILES])
+def test_gpu_matches_oracle_two_files(tmp_path, built_gpu, w1, w2, n1, n2, p):
+    f1, f2 = tmp_path / "a.fastq", tmp_path / "b.fastq"
+    synth.write_fastq(synth.workload(w1, n1, seed=3), f1)
+    synth.write_fastq(synth.workload(w2, n2, seed=4), f2)
+    do = pu.run("oracle", tmp_path, [f1, f2], p)
+    dg = pu.run("gpu", tmp_path, [f1, f2], p)
+    a, b = pu.outputs(do, p, "a.fastq"), pu.outputs(dg, p, "a.fastq")
+    keys = [x for x in _keys(a, p) if x not in SKIP]
+    assert not [k for k in keys if k not in b]
+    assert not pu.diff_keys(a, b, keys)
