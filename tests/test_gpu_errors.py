@@ -120,3 +120,13 @@ def test_no_kmers_at_all(ctx):
         with pytest.raises(native.MetapartError) as e:
             j.partition(27, 1, 1, starts, cnt.chunk_first_read, cnt.hist)
         assert code(e.value) == EUNSUP
+
+
+def test_empty_input(ctx):
+    """No bytes at all: a typed error (the index finds no record), never a crash."""
+    with native.Job(ctx) as j:
+        with pytest.raises(native.MetapartError):
+            j.load(b"")
+            starts = np.array([0, 0], dtype=np.uint64)
+            cnt = j.count(27, starts)
+            j.partition(27, 1, 1, starts, cnt.chunk_first_read, cnt.hist)

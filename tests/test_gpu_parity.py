@@ -30,6 +30,10 @@ CASES = [
     ("plain_small", 3000, pu.Params(k=27, chunks=64, scans=1, threads=64, buffer=1 << 24)),
     ("plain_large", 6000, pu.Params(k=31, chunks=128, scans=2, threads=128, buffer=1 << 24)),
     ("plain_small", 4000, pu.Params(k=23, chunks=256, scans=3, threads=256, buffer=1 << 24)),
+    # the smallest inputs: one pair of reads (one or two scans), two pairs over two threads
+    ("plain_small", 2, pu.Params(k=27, chunks=1, scans=1, threads=1)),
+    ("plain_small", 2, pu.Params(k=21, chunks=1, scans=2, threads=1)),
+    ("plain_small", 4, pu.Params(k=31, chunks=2, scans=1, threads=2)),
 ]
 
 # The oracle also writes the compSizes array after every scan; the reference accumulates it without

@@ -19,6 +19,8 @@ CASES = [
     ("plain_small", 3000, 31, pu.Params(k=27, chunks=64, scans=1, threads=64, buffer=1 << 24)),
     ("plain_large", 6000, 32, pu.Params(k=31, chunks=128, scans=2, threads=128, buffer=1 << 24)),
     ("plain_small", 4000, 33, pu.Params(k=23, chunks=256, scans=3, threads=256, buffer=1 << 24)),
+    # the smallest input: one pair of reads, two scans
+    ("plain_small", 2, 5, pu.Params(k=21, chunks=1, scans=2, threads=1)),
     # the 100k x 100 bp workload at its full size (k = 27, one scan)
     ("plain_small", 100_000, 7, pu.Params(k=27, chunks=16, scans=1, threads=8)),
     # the 5M x 250 bp 3-minimizer workload's shape (shared repeats, Zipf abundance) at 200k reads
