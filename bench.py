@@ -555,6 +555,32 @@ def serve_measure(args, dev: int, duration: float) -> dict:
         raise RuntimeError(f"{len(bad)} requests failed, first: {bad[0].error}")
     lat = np.array([r.latency_ms for _, r in results])
     qms = np.array([r.queue_ms for _, r in results])
+    # latency over the run (windows of a tenth of it) and by request size (thirds of the reads range, log scale)
+    ts = np.array([r.t_submit_ms for _, r in results])
+    ts = (ts - ts.min()) / 1e3
+    win = max(duration / 10, 1e-9)
+    dms = np.array([r.device_ms for _, r in results])
+    # host share of a request's service time: admission to done, less the device stages (copies to and from
+    # pinned memory, host indexing, launches)
+    hms = np.array([r.t_done_ms - r.t_admit_ms - r.device_ms for _, r in results])
+    by_time = []
+    for w in range(10):
+        m = (ts >= w * win) & (ts < (w + 1) * win)
+        if m.any():
+            by_time.append({"p50_ms": round(float(np.percentile(lat[m], 50)), 2),
+                            "p99_ms": round(float(np.percentile(lat[m], 99)), 2),
+                            "queue_mean_ms": round(float(qms[m].mean()), 2),
+                            "device_mean_ms": round(float(dms[m].mean()), 2),
+                            "host_mean_ms": round(float(hms[m].mean()), 2)})
+    nr = np.array([r.n_reads for _, r in results], dtype=np.float64)
+    edges = np.geomspace(max(nr.min(), 1), nr.max() + 1, 4)
+    by_size = []
+    for a, b in zip(edges[:-1], edges[1:]):
+        m = (nr >= a) & (nr < b)
+        if m.any():
+            by_size.append({"reads": [int(a), int(b)], "jobs": int(m.sum()),
+                            "p50_ms": round(float(np.percentile(lat[m], 50)), 2),
+                            "p99_ms": round(float(np.percentile(lat[m], 99)), 2)})
     bases = sum(pool[i][3] for i, _ in results)
     span = (max(r.t_done_ms for _, r in results) - min(r.t_submit_ms for _, r in results)) / 1e3
     dev_ms = sum(r.device_ms for _, r in results)
@@ -567,7 +593,8 @@ def serve_measure(args, dev: int, duration: float) -> dict:
         "mean_ms": round(float(lat.mean()), 2), "queue_p50_ms": round(float(np.percentile(qms, 50)), 2),
         "queue_p99_ms": round(float(np.percentile(qms, 99)), 2), "device_busy": round(dev_ms / 1e3 / span, 3),
         "peak_running": st["peak_running"], "peak_reserved_gb": round(st["peak_reserved"] / (1 << 30), 2),
-        "pool_stalls": stalls, "warmup_jobs": len(wt), "clocks": clk.summary(),
+        "pool_stalls": stalls, "warmup_jobs": len(wt), "by_tenth": by_time, "by_size": by_size,
+        "clocks": clk.summary(),
     }
 
 
