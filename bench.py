@@ -413,14 +413,15 @@ def main():
     dist.close()
 
 
-def link_bandwidth(host_in, dev_buf, host_out) -> dict:
-    """Host link rate of plain copies between the pinned buffers and HBM (GB/s, best of three), for
-    reading the e2e phases against.  Blocking copies: the pinned buffers carry no pending events into
-    interpreter shutdown."""
+def link_bandwidth(host_in, dev_buf, host_out, reps: int = 5) -> dict:
+    """Host link rate of plain copies between the pinned buffers and HBM (GB/s): the best of `reps` and
+    their harmonic mean (the host link has copies that run several times slower than the rest), for reading
+    the e2e phases against.  Blocking copies: the pinned buffers carry no pending events into interpreter
+    shutdown."""
     import torch
     n = min(host_in.numel(), dev_buf.numel(), host_out.numel())
-    up = dn = 0.0
-    for _ in range(3):
+    up, dn = [], []
+    for _ in range(reps):
         a = torch.cuda.Event(enable_timing=True)
         b = torch.cuda.Event(enable_timing=True)
         c = torch.cuda.Event(enable_timing=True)
@@ -430,9 +431,11 @@ def link_bandwidth(host_in, dev_buf, host_out) -> dict:
         host_out[:n].copy_(dev_buf[:n])
         c.record()
         c.synchronize()
-        up = max(up, n / a.elapsed_time(b) / 1e6)
-        dn = max(dn, n / b.elapsed_time(c) / 1e6)
-    return {"h2d": round(up, 1), "d2h": round(dn, 1), "bytes": int(n)}
+        up.append(a.elapsed_time(b))
+        dn.append(b.elapsed_time(c))
+    gbs = lambda ms: n / ms / 1e6
+    return {"h2d": round(gbs(min(up)), 1), "d2h": round(gbs(min(dn)), 1),
+            "h2d_mean": round(gbs(sum(up) / reps), 1), "d2h_mean": round(gbs(sum(dn) / reps), 1), "bytes": int(n)}
 
 
 def host_placement(dev: int) -> dict:
