@@ -262,7 +262,8 @@ int mp_server_submit(mp_server *s, const char *fastq, uint64_t nbytes, const mp_
                      uint64_t out_cap, uint64_t *file_sizes, uint32_t *labels, uint64_t labels_cap, uint64_t *ticket);
 
 /* 1 and *res when the request is done (its result is then released), 0 while it is pending; with
- * wait != 0 blocks until done. */
+ * wait != 0 blocks until done.  MP_EARG for a ticket never issued or whose result was released already
+ * (also to a second thread waiting on the same ticket when the first takes the result). */
 int mp_server_poll(mp_server *s, uint64_t ticket, int wait, mp_result *res);
 int mp_server_stats(mp_server *s, mp_server_stats_t *st);
 

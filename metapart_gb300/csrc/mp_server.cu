@@ -14,6 +14,7 @@
 #include <mutex>
 #include <thread>
 #include <unordered_map>
+#include <unordered_set>
 #include <vector>
 
 #include "metapart_gpu.h"
@@ -79,6 +80,7 @@ struct mp_server {
     std::condition_variable cv_work, cv_done;
     std::deque<Request> queue;
     std::unordered_map<uint64_t, mp_result> done;
+    std::unordered_set<uint64_t> open;  // tickets issued whose results have not been released yet
     std::vector<std::thread> workers;
     uint64_t next_ticket = 1;
     uint64_t reserved = 0, peak_reserved = 0;
@@ -246,6 +248,7 @@ int mp_server_submit(mp_server *s, const char *fastq, uint64_t nbytes, const mp_
     if (rq.footprint > s->budget) rq.exclusive = true;  // larger than the budget: alone, and the job's own checks decide
     rq.ticket = s->next_ticket++;
     rq.t_submit = ms_since(s->t0);
+    s->open.insert(rq.ticket);
     s->queue.push_back(rq);
     *ticket = rq.ticket;
     s->cv_work.notify_all();
@@ -256,14 +259,16 @@ int mp_server_poll(mp_server *s, uint64_t ticket, int wait, mp_result *res)
 {
     if (!s || !res) return MP_EARG;
     std::unique_lock<std::mutex> lk(s->mu);
-    if (ticket == 0 || ticket >= s->next_ticket) return MP_EARG;
     for (;;) {
         auto it = s->done.find(ticket);
         if (it != s->done.end()) {
             *res = it->second;
             s->done.erase(it);
+            s->open.erase(ticket);
+            s->cv_done.notify_all();  // other waiters on this ticket see it released
             return 1;
         }
+        if (!s->open.count(ticket)) return MP_EARG;  // never issued, or its result was released already
         if (!wait) return 0;
         s->cv_done.wait(lk);
     }

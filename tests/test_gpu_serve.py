@@ -92,5 +92,22 @@ def test_failing_request_reports_and_others_finish(ctx):
     assert np.array_equal(np.array(r_good.bounds, dtype=np.uint64), w_bounds)
 
 
+def test_released_or_unknown_ticket_is_refused(ctx):
+    """A result is released once: polling its ticket again (blocking or not), or a ticket never issued,
+    returns MP_EARG instead of waiting for a result that will not come."""
+    import torch
+    data = synth.fastq_bytes(synth.workload("plain_small", 2000, seed=7))
+    i = torch.frombuffer(bytearray(data), dtype=torch.uint8).pin_memory()
+    o = torch.empty(len(data) + 64, dtype=torch.uint8).pin_memory()
+    with serve.Server(ctx, slots=1) as srv:
+        t = srv.submit(i.data_ptr(), i.numel(), serve.RequestParams(27, 0, 1, 1, 2, 0), o.data_ptr(), o.numel())
+        assert srv.result(t).status == 0
+        for wait in (False, True):
+            with pytest.raises(native.MetapartError):
+                srv.result(t, wait=wait)
+        with pytest.raises(native.MetapartError):
+            srv.result(t + 1000, wait=True)
+
+
 def native_code(name):
     return {"MP_EARG": -1, "MP_ENOMEM": -4}[name]
