@@ -40,7 +40,8 @@ typedef struct mp_job mp_job;
 /* Thread-local message of the last failed call. */
 const char *mp_last_error(void);
 
-/* One context per device: stream pool, HBM budget accounting. */
+/* One context per device: stream pool, HBM budget accounting.  Jobs, batches and servers keep a pointer
+ * to their context: destroy it only after all of them are destroyed. */
 int mp_ctx_create(int device, uint64_t hbm_budget_bytes, mp_ctx **out);
 void mp_ctx_destroy(mp_ctx *ctx);
 uint64_t mp_ctx_hbm_in_use(const mp_ctx *ctx);
