@@ -10,11 +10,16 @@ on read sets with the shapes the numbers are quoted on.
   5M x 250 bp, 3-minimizer variant: the whole workload (Zipf abundance, 30 % of every genome from 5 kb
       repeats shared across genomes: giant components and long runs of equal k-mers), k = 31, one scan,
       16 threads; every stage dump.
+  The whole 20M x 150 bp workload, k = 31, 2 scans, 16 threads, with the per-read dumps and the partition
+      files, where the host has room for it (150 GB of memory and 60 GB of temporary disk free; about a
+      minute on 16 cores).
 
 The oracle is the C restatement of the reference that tests/test_oracle_golden.py pins to the reference's
 own outputs; it runs with every host core.
 """
 import os
+import shutil
+import tempfile
 
 import pytest
 
@@ -25,6 +30,31 @@ pytestmark = pytest.mark.gpu
 
 CORES = str(os.cpu_count() or 4)
 
+
+def _room_for_full_size():
+    """(run, why): the 20M-read case runs where the host has 150 GB of memory and 60 GB of temporary disk
+    free, or when MP_FULL_SIZE_PARITY=1; MP_FULL_SIZE_PARITY=0 leaves it out."""
+    flag = os.environ.get("MP_FULL_SIZE_PARITY")
+    if flag in ("0", "1"):
+        return flag == "1", "MP_FULL_SIZE_PARITY=0"
+    try:
+        mem = next(int(ln.split()[1]) * 1024 for ln in open("/proc/meminfo") if ln.startswith("MemAvailable:"))
+    except (OSError, StopIteration):
+        return False, "host memory unknown"
+    try:
+        cg = open("/sys/fs/cgroup/memory.max").read().strip()
+        if cg != "max":
+            mem = min(mem, int(cg))
+    except (OSError, ValueError):
+        pass
+    disk = shutil.disk_usage(tempfile.gettempdir()).free
+    if mem < 150 << 30 or disk < 60 << 30:
+        return False, f"full-size case needs 150 GB of memory and 60 GB of disk ({mem >> 30} GB, {disk >> 30} GB free)"
+    return True, ""
+
+
+FULL_SIZE = _room_for_full_size()
+
 CASES = [
     # id, workload, reads, params, dump tuple streams
     ("100k-x100bp-k27-t16", "plain_small", 100_000, pu.Params(k=27, chunks=64, scans=1, threads=16), True),
@@ -32,6 +62,9 @@ CASES = [
     ("400k-x150bp-k31-s2", "plain_large", 400_000, pu.Params(k=31, chunks=64, scans=2, threads=16), True),
     ("2M-x150bp-k31-s2", "plain_large", 2_000_000, pu.Params(k=31, chunks=64, scans=2, threads=16), False),
     ("5M-x250bp-min3-k31", "min3", 5_000_000, pu.Params(k=31, chunks=64, scans=1, threads=16, min3=True), True),
+    # the whole 20M-read workload: 6.3 GB of FASTQ, about 40 GB of disk, about 75 GB of host memory for the oracle
+    pytest.param("20M-x150bp-k31-s2", "plain_large", 20_000_000, pu.Params(k=31, chunks=64, scans=2, threads=16),
+                 False, marks=pytest.mark.skipif(not FULL_SIZE[0], reason=FULL_SIZE[1])),
 ]
 
 
@@ -46,7 +79,8 @@ def _keys(res, p, tuples):
     return ks
 
 
-@pytest.mark.parametrize("name,work,n,p,tuples", CASES, ids=[c[0] for c in CASES])
+@pytest.mark.parametrize("name,work,n,p,tuples", CASES,
+                         ids=[c.values[0] if hasattr(c, "values") else c[0] for c in CASES])
 def test_gpu_matches_oracle_at_config_size(tmp_path, built_gpu, name, work, n, p, tuples):
     fq = tmp_path / "in.fastq"
     synth.write_fastq(synth.workload(work, n, seed=7), fq)
@@ -61,4 +95,7 @@ def test_gpu_matches_oracle_at_config_size(tmp_path, built_gpu, name, work, n, p
     assert not missing, f"missing outputs {missing}"
     assert sum(1 for k in keys if k.startswith("part/")) == 16 * p.threads
     diff = pu.diff_keys(a, b, keys)
+    del a, b
+    for d in (do, dg):  # the large cases' files are not needed once compared
+        shutil.rmtree(d, ignore_errors=True)
     assert not diff, f"GPU output differs from the oracle in {diff}"
